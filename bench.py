@@ -1,0 +1,330 @@
+"""Benchmark of the VlaPy time step on GB300 (one JSON line on rank 0).
+
+A "step" is one full time step (VP step, Fokker-Planck step, storage step) of
+the named workload.  ``value`` is phase-space cell-updates per second timed on
+the device with CUDA events around a CUDA graph of K steps (inputs resident in
+HBM); ``e2e`` is the same metric through the C-ABI entry point with the
+step's inputs copied from pinned host memory and its stored fields/series
+read back every step.  ``roofline`` is the dominant kernel's algorithmic
+bytes per launch over its CUDA-event launch time in a profiled pass.
+``--impl reference`` times the CPU oracle (a NumPy restatement of the
+reference path) on the host cores instead.
+
+Workloads (synthetic inputs of the reference's shapes; no datasets involved):
+  large   nx=4096, nv=8192, xmax=2pi/0.3, vmax=8, two-stream f, nu=1e-4 DG, dt=0.05
+  driven  nx=64, nv=1024, k=0.3, vmax=6.4, sin^2-enveloped driver, nu=1e-3 DG, dt=0.1
+  landau  nx=32, nv=512, k=0.3, vmax=6.4, A=1e-4, nu=0, dt=0.1
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    "large": dict(nx=4096, nv=8192, k=0.3, vmax=8.0, dt=0.05, nu=1e-4, op="dg", kind="two-stream"),
+    "driven": dict(nx=64, nv=1024, k=0.3, vmax=6.4, dt=0.1, nu=1e-3, op="dg", kind="driven"),
+    "landau": dict(nx=32, nv=512, k=0.3, vmax=6.4, dt=0.1, nu=0.0, op="dg", kind="landau"),
+}
+
+
+def initial_state(w, seed=4):
+    """Initial f of a workload (host, float64)."""
+    from vlapy_gb300 import initializers as I
+    nx, nv, k, vmax = w["nx"], w["nv"], w["k"], w["vmax"]
+    dx, x, kx, inv = I.initialize_spatial_quantities(0.0, 2 * np.pi / k, nx)
+    dv, v, kv = I.initialize_velocity_quantities(vmax, nv)
+    if w["kind"] == "two-stream":
+        rng = np.random.default_rng(seed)
+        ph = rng.uniform(0, 2 * np.pi, 16)
+        m = np.arange(1, 17)
+        pert = 1e-3 * np.cos(m[None, :] * k * x[:, None] + ph[None, :]).sum(axis=1)
+        fv = 0.5 * (np.exp(-((v - 3.0) ** 2) / 2.0) + np.exp(-((v + 3.0) ** 2) / 2.0))
+        fv = fv / np.trapezoid(fv, dx=dv)
+        f = fv[None, :] * (1.0 + pert)[:, None]
+    elif w["kind"] == "driven":
+        f = I.initialize_distribution(nx, nv, vmax)
+    else:
+        f = I.initialize_distribution(nx, nv, vmax) * (1.0 + 1e-4 * np.cos(k * x))[:, None]
+    return dict(x=x, v=v, kx=kx, kv=kv, inv=inv, dx=dx, dv=dv, f=f)
+
+
+def pulses_of(w):
+    if w["kind"] != "driven":
+        return []
+    from vlapy_gb300 import dispersion
+    wr = float(np.real(dispersion.get_roots_to_electrostatic_dispersion(1.0, 1.0, w["k"])))
+    return [{"k0": w["k"], "w0": wr, "a0": 1e-2, "t_L": 0.0, "t_R": 100.0, "envelope": 1}]
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join("/tmp", "vg_clocks_%d_%d.csv" % (os.getpid(), index))
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), parts[5:9]))
+            except ValueError:
+                continue
+        if not rows:
+            return None
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i, flag in enumerate(r[2]) if flag.lower() == "active"})
+        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows)}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def run_gpu(args, w, rank, world):
+    import torch
+    from vlapy_gb300 import _lib
+    from vlapy_gb300.plan import Plan, history_struct
+
+    torch.cuda.set_device(rank % max(1, torch.cuda.device_count()))
+    _lib.load()
+    st = initial_state(w)
+    nx, nv = w["nx"], w["nv"]
+    plan = Plan(nx, nv, st["x"], st["v"], st["kx"], st["kv"], st["inv"], st["dx"], st["dv"], dt=w["dt"],
+                nu=w["nu"], collision=w["op"] if w["nu"] > 0 else "none", pulses=pulses_of(w),
+                precision=args.precision)
+    dev = torch.device("cuda")
+    K, W = args.steps, args.warmup
+    nt = W + K + args.prof_steps
+    dt = w["dt"]
+    tb_host = dt * np.arange(nt)
+    drv_host = np.zeros((nt, nx))
+    if pulses_of(w):
+        from vlapy_gb300 import field_driver
+        pd = field_driver.PulseDriver(st["x"], {"p": dict(pulses_of(w)[0], envelope="sin2")})
+        drv_host = field_driver.make_driver_array(pd, st["x"], tb_host)
+    f = torch.as_tensor(st["f"], dtype=torch.float64, device=dev).contiguous()
+    e = torch.zeros(nx, dtype=torch.float64, device=dev)
+    tb = torch.as_tensor(tb_host, device=dev)
+    db = torch.as_tensor(drv_host, device=dev)
+    z = lambda *s: torch.zeros(s, dtype=torch.float64, device=dev)  # noqa: E731
+    storage = {"stored_f": torch.zeros((nt, 2, nv), dtype=torch.complex64, device=dev),
+               "fields": {k: z(nt, nx) for k in ("e", "driver", "n", "j", "T", "q", "fv4", "vN")},
+               "series": {k: z(nt) for k in ("mean_n", "mean_j", "mean_T", "mean_e2", "mean_de2",
+                                             "mean_f2", "mean_flogf")}}
+    hist = history_struct(storage, nx, 2)
+    stream = torch.cuda.Stream()
+    with torch.cuda.stream(stream):
+        plan.run_steps(f, e, hist, tb, db, 0, W, use_graph=False, stream=stream)
+        # capture the K timed steps once, then replay it (a second capture
+        # key would be a second graph; reuse the warm one for the timing)
+        plan.run_steps(f, e, hist, tb, db, W, K, use_graph=True, stream=stream)
+    torch.cuda.synchronize()
+    f.copy_(torch.as_tensor(st["f"], dtype=torch.float64, device=dev))
+    e.zero_()
+    with torch.cuda.stream(stream):
+        plan.run_steps(f, e, hist, tb, db, 0, W, use_graph=False, stream=stream)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    with torch.cuda.stream(stream):
+        plan.run_steps(f, e, hist, tb, db, W, K, use_graph=True, stream=stream)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    clk = clocks.stop()
+    if not torch.isfinite(e).all():
+        raise RuntimeError("non-finite field after the timed steps")
+    # profiled pass: per-kernel launch times (graph bypassed)
+    plan.profile(True)
+    with torch.cuda.stream(stream):
+        plan.run_steps(f, e, hist, tb, db, W + K, args.prof_steps, use_graph=False, stream=stream)
+    prof = plan.profile_read()
+    plan.profile(False)
+    # e2e: per step, pinned host time/driver in, stored fields + series out
+    e2e = run_e2e(plan, f, e, storage, hist, tb_host, drv_host, W, K, stream, torch)
+    return ms, prof, clk, e2e, plan
+
+
+def run_e2e(plan, f, e, storage, hist, tb_host, drv_host, W, K, stream, torch):
+    nx = plan.nx
+    dev = torch.device("cuda")
+    pin_t = torch.as_tensor(tb_host).pin_memory()
+    pin_d = torch.as_tensor(drv_host).pin_memory()
+    tb = torch.empty_like(pin_t, device=dev)
+    db = torch.empty_like(pin_d, device=dev)
+    out_fields = torch.empty((8, nx), dtype=torch.float64).pin_memory()
+    out_series = torch.empty(7, dtype=torch.float64).pin_memory()
+    fk = ("e", "driver", "n", "j", "T", "q", "fv4", "vN")
+    sk = ("mean_n", "mean_j", "mean_T", "mean_e2", "mean_de2", "mean_f2", "mean_flogf")
+    h2d = pin_t[0].numel() * 8 + pin_d[0].numel() * 8
+    d2h = out_fields.numel() * 8 + out_series.numel() * 8
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    with torch.cuda.stream(stream):
+        for i in range(W, W + K):
+            tb[i].copy_(pin_t[i], non_blocking=True)
+            db[i].copy_(pin_d[i], non_blocking=True)
+            plan.run_steps(f, e, hist, tb, db, i, 1, use_graph=False, stream=stream)
+            for q, k in enumerate(fk):
+                out_fields[q].copy_(storage["fields"][k][i], non_blocking=True)
+            for q, k in enumerate(sk):
+                out_series[q:q + 1].copy_(storage["series"][k][i:i + 1], non_blocking=True)
+            stream.synchronize()
+    t1 = time.perf_counter()
+    return (t1 - t0), h2d, d2h
+
+
+def cpu_baseline(w, steps, reps_cap=3):
+    """Oracle (NumPy restatement of the reference step) on the host cores."""
+    from oracle import vlapy_oracle as vo
+    st = initial_state(w)
+    nx, nv = w["nx"], w["nv"]
+    pl = pulses_of(w)
+    drv = None
+    if pl:
+        p = pl[0]
+        drv = lambda t: vo.driver_sin2(st["x"], p["k0"], p["w0"], p["a0"], p["t_R"], t)  # noqa: E731
+    run = vo.OracleRun(nx, nv, 2 * np.pi / w["k"], w["vmax"], w["dt"], nu=w["nu"], operator=w["op"],
+                       driver=drv, n_modes=2)
+    n = max(1, min(steps, reps_cap))
+    stg = vo.new_storage(st["f"], np.zeros(nx), n, 2)
+    stg["time_batch"] = w["dt"] * np.arange(n)
+    stg["driver_array_batch"] = np.zeros((n, nx))
+    t0 = time.perf_counter()
+    for i in range(n):
+        run.timestep(stg, i)
+    dt = time.perf_counter() - t0
+    return nx * nv * n / dt, n, dt
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="large", choices=sorted(WORKLOADS))
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32-deltaf"])
+    ap.add_argument("--prof-steps", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    w = WORKLOADS[args.workload]
+    cells = w["nx"] * w["nv"]
+    metric = "cell-updates/s"
+    cfg = {"workload": args.workload, "nx": w["nx"], "nv": w["nv"], "dt": w["dt"], "nu": w["nu"],
+           "collision": w["op"] if w["nu"] > 0 else "none", "integrator": "leapfrog",
+           "precision": args.precision, "storage": "fields+series+k0,k1 modes every step",
+           "l2": "f (%.0f MB) larger than L2" % (cells * 8 / 1e6)}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        val, n, sec = cpu_baseline(w, args.steps)
+        line = {"metric": metric, "value": val, "unit": "cell-updates/s", "n_gpus": args.gpus,
+                "steps": n, "warmup": 0, "ms_per_step": 1e3 * sec / n, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": cfg, "impl": "reference",
+                "cpu_baseline": {"value": val, "unit": "cell-updates/s", "cores": 1, "kind": "port",
+                                 "sample": "%d full oracle step(s) of the workload" % n},
+                "e2e": {"value": val, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    import torch
+    if world > 1:
+        torch.distributed.init_process_group("nccl")
+    ms, prof, clk, e2e, plan = run_gpu(args, w, int(os.environ.get("LOCAL_RANK", rank)), world)
+    t_max = ms
+    if world > 1:
+        tt = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_max = float(tt.item())
+    value = world * cells * args.steps / (t_max / 1e3)
+    e2e_sec, h2d, d2h = e2e
+    e2e_val = world * cells * args.steps / e2e_sec
+    dom = max(prof.items(), key=lambda kv: kv[1]["total_ms"])
+    name, pd = dom
+    avg_ms = pd["total_ms"] / pd["launches"]
+    peak, peak_kind = peaks()
+    achieved = pd["bytes_per_launch"] / (avg_ms / 1e3) / 1e9
+    launches_per_step = 0
+    for k, d in prof.items():
+        per = d["launches"] / args.prof_steps
+        launches_per_step += per * (3 if k == "storage" else 1)
+    if rank != 0:
+        return
+    cpu = None
+    if not args.no_cpu_baseline:
+        cval, n, sec = cpu_baseline(w, args.steps, reps_cap=1)
+        cpu = {"value": cval, "unit": "cell-updates/s", "cores": 1, "kind": "port",
+               "sample": "%d full oracle step (VP+FP+storage) of the %dx%d workload, %.1f s" % (n, w["nx"], w["nv"], sec)}
+    line = {
+        "metric": metric, "value": value, "unit": "cell-updates/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32",
+        "data": "synthetic", "config": cfg,
+        "e2e": {"value": e2e_val, "unit": "cell-updates/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None, "kernel": name,
+                     "peak_source": peak_kind,
+                     "kernel_ms": avg_ms, "bytes_per_launch": pd["bytes_per_launch"]},
+        "kernels": {k: {"launches": d["launches"], "avg_ms": d["total_ms"] / d["launches"]} for k, d in prof.items()},
+        "gpu_launches": int(round(launches_per_step * args.steps)),
+        "clocks": clk,
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

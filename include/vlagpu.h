@@ -1,0 +1,162 @@
+/*
+ * vlagpu.h -- C ABI of the GB300 VlaPy time step (libvlagpu.so).
+ *
+ * The reference (joglekara/VlaPy) is pure Python: its "plugin interface" for
+ * the hot path is a set of closures built from the parameter dictionary.
+ * Each entry point below replaces one of them and names the reference code it
+ * stands in for.  All array arguments of the compute calls are DEVICE
+ * pointers owned by the caller (PyTorch tensors in the Python host layer);
+ * the plan owns only its constants and scratch.  Every call returns an int
+ * status (VG_OK == 0); vg_last_error() gives the message of the last failure
+ * on the calling thread.  Calls on one plan must be serialised on one stream;
+ * different plans are independent.
+ *
+ * Layouts (C order, as in the reference): f[nx][nv] with v contiguous,
+ * e[nx], driver[nx].  In VG_F64 mode f is float64 and the arithmetic follows
+ * the reference's NumPy path; in VG_F32_DELTA_F mode the state is the FP32
+ * deviation g = f - f0(v) from a fixed background f0 given at plan creation.
+ */
+#ifndef VLAGPU_H
+#define VLAGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct vg_plan vg_plan;
+/* a cudaStream_t, passed opaquely; NULL is the legacy default stream */
+typedef void* vg_stream;
+
+enum {
+  VG_OK = 0,
+  VG_ERR_ARG = 1,          /* bad argument or descriptor */
+  VG_ERR_CUDA = 2,         /* a CUDA runtime call failed */
+  VG_ERR_UNSUPPORTED = 3,  /* valid in the reference, not implemented here */
+  VG_ERR_NUMERIC = 4,      /* NaN/Inf detected in the field */
+  VG_ERR_TIMEOUT = 5,      /* a bounded wait ran out */
+  VG_ERR_STATE = 6         /* call out of order (e.g. history too small) */
+};
+
+enum { VG_F64 = 0, VG_F32_DELTA_F = 1 };
+/* all_params["fokker-planck"]["type"], vlapy/core/collisions.py:292-317 */
+enum { VG_COLL_NONE = 0, VG_COLL_LB = 1, VG_COLL_DG = 2 };
+/* all_params["vlasov-poisson"]["time"], vlapy/core/vlasov_poisson.py:235-280 */
+enum { VG_LEAPFROG = 0, VG_PEFRL = 1, VG_H_SIXTH = 2 };
+/* pulse envelopes: VG_ENV_TANH is vlapy/field_driver.py:24-50;
+ * VG_ENV_SIN2 is a0*sin(k x - w t)*sin^2(pi t / t_R) on [0, t_R], 0 after. */
+enum { VG_ENV_TANH = 0, VG_ENV_SIN2 = 1 };
+
+typedef struct vg_pulse {
+  double k0, w0, a0, t_L, t_R, t_wL, t_wR;
+  int32_t envelope;
+  int32_t reserved;
+} vg_pulse;
+
+/* Run descriptor: the derived quantities of stuff_for_time_loop
+ * (vlapy/outer_loop.py:125-144).  Array members are HOST pointers copied at
+ * vg_plan_create; computing them with NumPy on the host (as the reference
+ * does, vlapy/initializers.py:56-89) keeps the grids bit-identical. */
+typedef struct vg_run_desc {
+  int32_t nx, nv;
+  int32_t precision;   /* VG_F64 | VG_F32_DELTA_F */
+  int32_t collision;   /* VG_COLL_* ; VG_COLL_NONE when nu == 0 */
+  int32_t integrator;  /* VG_LEAPFROG | VG_PEFRL | VG_H_SIXTH */
+  int32_t n_pulses;
+  double dt, nu, dx, dv;
+  double dv_sq;               /* dv ** 2.0 evaluated by the host */
+  const double* x;            /* [nx] */
+  const double* v;            /* [nv] */
+  const double* kx;           /* [nx] */
+  const double* kv;           /* [nv] */
+  const double* one_over_kx;  /* [nx] */
+  const double* v_pow;        /* [5][nv]: v**2.0, v**2, v**3, v**4, v**5 as NumPy evaluates them */
+  const vg_pulse* pulses;     /* [n_pulses] */
+  const double* f_background; /* [nv] background f0(v) for VG_F32_DELTA_F; NULL for VG_F64 */
+} vg_run_desc;
+
+/* Per-step storage of the inner loop (vlapy/outer_loop.py:149-215). DEVICE
+ * pointers; any may be NULL to skip that output. */
+typedef struct vg_history {
+  int32_t nt;          /* steps the arrays hold (first dimension) */
+  int32_t store_all;   /* 1: stored_f is float64 [nt][nx][nv]; 0: complex64 [nt][n_slots][nv] */
+  int32_t n_modes;     /* x-Fourier modes computed per step when store_all == 0 */
+  int32_t n_slots;     /* modes stored per step; n_modes must equal it or be 1 (broadcast) */
+  double* fields[8];   /* e, driver, n, j, T, q, fv4, vN: each [nt][nx] */
+  double* series[7];   /* mean_n, mean_j, mean_T, mean_e2, mean_de2, mean_f2, mean_flogf: [nt] */
+  void* stored_f;
+} vg_history;
+
+/* ---- plan lifetime ---------------------------------------------------- */
+/* Builds the per-run constants (grids, FFT twiddles, NumPy summation trees)
+ * and allocates the plan's scratch with cudaMalloc on the current device.
+ * Replaces the closure factories of vlapy/core/step.py:29-113. */
+int vg_plan_create(const vg_run_desc* desc, vg_plan** out);
+int vg_plan_destroy(vg_plan* plan);
+const char* vg_last_error(void);
+int vg_version(void);
+
+/* ---- sub-operators (the reference's closures) -------------------------- */
+/* v-advection f <- Re IFFT_v(exp(-i kv e dt) FFT_v f), in place.
+ * Replaces step_edfdv_exponential, vlapy/core/vlasov.py:113-140. */
+int vg_edfdv(vg_plan* plan, void* f, const double* e, double dt, vg_stream stream);
+/* x-advection f <- Re IFFT_x(exp(-i kx v dt) FFT_x f), in place.
+ * Replaces step_vdfdx_exponential, vlapy/core/vlasov.py:83-110. */
+int vg_vdfdx(vg_plan* plan, void* f, double dt, vg_stream stream);
+/* n(x) = trapz_v f.  Replaces compute_charges, vlapy/core/field.py:27-36. */
+int vg_charge_density(vg_plan* plan, const void* f, double* n, vg_stream stream);
+/* e = Re IFFT(i/kx FFT(rho)) for a net charge rho[nx] (nx any size).
+ * Replaces __fft_solve__, vlapy/core/field.py:39-49. */
+int vg_poisson(vg_plan* plan, const double* rho, double* e, vg_stream stream);
+/* e = driver + field of (1 - trapz_v f); driver may be NULL (zero).
+ * Replaces solve_total_electric_field, vlapy/core/field.py:66-88. */
+int vg_field_solve(vg_plan* plan, const void* f, const double* driver, double* e, vg_stream stream);
+/* Implicit Fokker-Planck step of the plan's operator, in place.
+ * Replaces take_collision_step, vlapy/core/step.py:70-113
+ * (matrix makers vlapy/core/collisions.py:26-160, solver :222-265). */
+int vg_collision_step(vg_plan* plan, void* f, vg_stream stream);
+/* Storage step at index i: stored_f, the eight fields and seven series.
+ * Replaces storage_step, vlapy/core/step.py:231-283. */
+int vg_storage_step(vg_plan* plan, const void* f, const double* e, const double* de,
+                    const vg_history* hist, int32_t i, vg_stream stream);
+/* Driver field at time t into out[nx].  Replaces driver_function,
+ * vlapy/field_driver.py:24-50. */
+int vg_driver(vg_plan* plan, double t, double* out, vg_stream stream);
+
+/* ---- the time step ----------------------------------------------------- */
+/* Runs nsteps full steps (VP step, FP step, storage step) for storage
+ * indices i0 .. i0+nsteps-1, reading t_i from time_batch[i] and the stored
+ * driver de_i from driver_batch[i][:] (both DEVICE arrays of the batch), and
+ * evaluating the pulses at the integrator's sub-step times.  f and e are
+ * updated in place.  Replaces timestep, vlapy/core/step.py:286-328, looped
+ * as in inner_loop, vlapy/outer_loop.py:265-272.  With use_graph != 0 the
+ * launch sequence is captured once into a CUDA graph per (pointer set,
+ * i0, nsteps) and replayed. */
+int vg_run_steps(vg_plan* plan, void* f, double* e, const vg_history* hist,
+                 const double* time_batch, const double* driver_batch,
+                 int32_t i0, int32_t nsteps, int32_t use_graph, vg_stream stream);
+
+/* ---- measurement ----------------------------------------------------- */
+/* Per-kernel device timing of vg_run_steps: while enabled, every kernel of
+ * the step sequence is bracketed by CUDA events on the plan's stream and the
+ * graph path is bypassed.  vg_profile_read synchronises the stream, then
+ * fills up to max entries (kernel name, launches, total milliseconds,
+ * algorithmic DRAM bytes per launch) and clears the record.  No reference
+ * counterpart (the reference only logs wall-clock per step,
+ * vlapy/manager.py:144-146). */
+typedef struct vg_prof_entry {
+  char name[32];
+  int64_t launches;
+  double total_ms;
+  double bytes_per_launch;
+} vg_prof_entry;
+int vg_profile_enable(vg_plan* plan, int32_t enable);
+int vg_profile_read(vg_plan* plan, vg_prof_entry* out, int32_t max, int32_t* n_out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* VLAGPU_H */

@@ -1,0 +1,73 @@
+"""Plans built from the reference's stuff_for_time_loop dictionary and cached
+on it, so the closure factories of vlasov/field/step share one device plan."""
+
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from ..field_driver import PulseDriver
+from ..plan import Plan
+
+_KEY = "_vlagpu_plans"
+_AUX = {}
+
+
+def precision_of(all_params) -> str:
+    if not all_params:
+        return "fp64"
+    return all_params.get("backend", {}).get("precision", "fp64")
+
+
+def collision_name(all_params) -> str:
+    if not all_params or all_params.get("nu", 0.0) == 0.0:
+        return "none"
+    fp = all_params.get("fokker-planck", {})
+    return fp.get("type", "lb")
+
+
+def plan_for(stuff: dict, all_params=None, collision=None, integrator=None) -> Plan:
+    collision = collision_name(all_params) if collision is None else collision
+    if integrator is None:
+        integrator = (all_params or {}).get("vlasov-poisson", {}).get("time", "leapfrog")
+    precision = precision_of(all_params)
+    drv = stuff.get("driver_function")
+    pulses = drv.pulses if isinstance(drv, PulseDriver) else []
+    key = (collision, integrator, precision, float(stuff.get("dt", 0.0)), float(stuff.get("nu", 0.0)),
+           id(drv))
+    cache = stuff.setdefault(_KEY, {})
+    if key in cache:
+        return cache[key]
+    nx, nv = int(stuff["nx"]), int(stuff["nv"])
+    dv = float(stuff["dv"])
+    v = np.asarray(stuff["v"], dtype=np.float64)
+    x = np.asarray(stuff.get("x", np.zeros(nx)), dtype=np.float64)
+    kx = np.asarray(stuff.get("kx", np.zeros(nx)), dtype=np.float64)
+    kv = np.asarray(stuff.get("kv", np.fft.fftfreq(nv, d=dv) * 2.0 * np.pi), dtype=np.float64)
+    inv = np.asarray(stuff.get("one_over_kx", np.zeros(nx)), dtype=np.float64)
+    dx = float(x[1] - x[0]) if nx > 1 else 0.0
+    p = Plan(nx, nv, x, v, kx, kv, inv, dx, dv, dt=float(stuff.get("dt", 0.0)),
+             nu=float(stuff.get("nu", 0.0)), collision=collision, integrator=integrator,
+             pulses=pulses, precision=precision)
+    cache[key] = p
+    return p
+
+
+def aux_plan(nx: int, nv: int, dv: float, one_over_kx=None) -> Plan:
+    """Plan for the stand-alone field functions (compute_charges,
+    solve_for_field), keyed by the grid it needs."""
+    inv = np.zeros(nx) if one_over_kx is None else np.asarray(one_over_kx, dtype=np.float64)
+    key = (nx, nv, float(dv), inv.tobytes())
+    if key not in _AUX:
+        v = np.linspace(-1.0, 1.0, nv)
+        _AUX[key] = Plan(nx, nv, np.zeros(nx), v, np.zeros(nx), np.zeros(nv), inv, 1.0, dv)
+    return _AUX[key]
+
+
+def as_device(a, dtype=torch.float64):
+    """A CUDA tensor for a, copying host data (NumPy or CPU tensor) if needed."""
+    if isinstance(a, torch.Tensor):
+        if a.is_cuda and a.dtype == dtype and a.is_contiguous():
+            return a
+        return a.to(device="cuda", dtype=dtype).contiguous()
+    return torch.as_tensor(np.ascontiguousarray(a), dtype=dtype, device="cuda")

@@ -1,0 +1,616 @@
+// C ABI of libvlagpu.so: plan lifetime, sub-operators and the time step.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "vg_internal.cuh"
+
+namespace vg {
+
+static thread_local std::string g_err;
+
+void set_error(const std::string& msg) { g_err = msg; }
+
+int cuda_status(cudaError_t err, const char* what) {
+  if (err == cudaSuccess) return VG_OK;
+  set_error(std::string(what) + ": " + cudaGetErrorName(err) + " (" + cudaGetErrorString(err) + ")");
+  return VG_ERR_CUDA;
+}
+
+// NumPy pairwise-sum tree (numpy/_core/src/umath/loops_utils.h.src,
+// pairwise_sum): blocks of <= 128 terms summed with 8 accumulators, larger
+// ranges split at n/2 rounded down to a multiple of 8.
+static void pairwise_tree(int start, int len, std::vector<int>& leaves, std::vector<int>& prog) {
+  if (len <= 128) {
+    prog.push_back((int)(leaves.size() / 2));
+    leaves.push_back(start);
+    leaves.push_back(len);
+    return;
+  }
+  int half = len / 2;
+  half -= half % 8;
+  pairwise_tree(start, half, leaves, prog);
+  pairwise_tree(start + half, len - half, leaves, prog);
+  prog.push_back(-1);
+}
+
+static std::vector<int> pairwise_table(int n) {
+  std::vector<int> leaves, prog;
+  pairwise_tree(0, n, leaves, prog);
+  std::vector<int> out;
+  out.push_back((int)(leaves.size() / 2));
+  out.push_back((int)prog.size());
+  out.insert(out.end(), leaves.begin(), leaves.end());
+  out.insert(out.end(), prog.begin(), prog.end());
+  return out;
+}
+
+struct GraphKey {
+  const void* f;
+  const void* e;
+  const void* tb;
+  const void* db;
+  vg_history h;
+  int i0, n;
+  cudaStream_t s;
+  bool operator<(const GraphKey& o) const { return std::memcmp(this, &o, sizeof(GraphKey)) < 0; }
+};
+struct GraphCache {
+  std::map<GraphKey, cudaGraphExec_t> execs;
+};
+
+// Kernel kinds of the step sequence, for vg_profile_*.
+enum ProfKind { PK_EDFDV = 0, PK_VDFDX, PK_DENSITY, PK_POISSON, PK_FP_MOMENTS, PK_FP_SOLVE, PK_STORAGE, PK_COUNT };
+static const char* kProfNames[PK_COUNT] = {"edfdv", "vdfdx", "density", "poisson",
+                                            "fp_moments", "fp_solve", "storage"};
+
+struct ProfState {
+  bool enabled = false;
+  std::vector<cudaEvent_t> pool;
+  size_t used = 0;
+  struct Rec { int kind; cudaEvent_t b, e; };
+  std::vector<Rec> recs;
+  ~ProfState() {
+    for (cudaEvent_t ev : pool) cudaEventDestroy(ev);
+  }
+  cudaEvent_t next() {
+    if (used == pool.size()) {
+      cudaEvent_t ev;
+      if (cudaEventCreate(&ev) != cudaSuccess) return nullptr;
+      pool.push_back(ev);
+    }
+    return pool[used++];
+  }
+};
+
+// algorithmic DRAM bytes of one launch of each kind: the f traffic the
+// operation cannot avoid (read + write of f for in-place transforms, one
+// read for reductions), FP64 elements
+static double prof_bytes(const vg_plan* p, int kind) {
+  const double cells = (double)p->nx * (double)p->nv;
+  const double es = p->precision == VG_F64 ? 8.0 : 4.0;
+  switch (kind) {
+    case PK_EDFDV:
+    case PK_VDFDX:
+    case PK_FP_SOLVE: return 2.0 * es * cells;
+    case PK_DENSITY:
+    case PK_FP_MOMENTS:
+    case PK_STORAGE: return es * cells;
+    default: return 3.0 * 8.0 * p->nx;
+  }
+}
+
+}  // namespace vg
+
+using namespace vg;
+
+namespace {
+
+template <typename T>
+int dev_copy(T** dst, const T* src, size_t n, const char* what) {
+  *dst = nullptr;
+  if (n == 0) return VG_OK;
+  cudaError_t err = cudaMalloc(reinterpret_cast<void**>(dst), n * sizeof(T));
+  if (err != cudaSuccess) return cuda_status(err, what);
+  if (src) {
+    err = cudaMemcpy(*dst, src, n * sizeof(T), cudaMemcpyHostToDevice);
+    if (err != cudaSuccess) return cuda_status(err, what);
+  } else {
+    err = cudaMemset(*dst, 0, n * sizeof(T));
+    if (err != cudaSuccess) return cuda_status(err, what);
+  }
+  return VG_OK;
+}
+
+void free_plan(vg_plan* p) {
+  if (!p) return;
+  void* ptrs[] = {p->x, p->v, p->kx, p->kv, p->inv_kx, p->v_pow, p->f_bg, p->pulses, p->tw64, p->tw32,
+                  p->pw_v, p->pw_x, p->dens, p->mom, p->bb, p->rho, p->etmp};
+  for (void* q : ptrs)
+    if (q) cudaFree(q);
+  if (p->graph_cache) {
+    auto* gc = static_cast<GraphCache*>(p->graph_cache);
+    for (auto& kv : gc->execs) cudaGraphExecDestroy(kv.second);
+    delete gc;
+  }
+  delete static_cast<ProfState*>(p->prof);
+  delete p;
+}
+
+#define VG_CHECK(expr)            \
+  do {                            \
+    int _st = (expr);             \
+    if (_st != VG_OK) return _st; \
+  } while (0)
+
+int require_plan(const vg_plan* p) {
+  if (!p) {
+    set_error("null plan");
+    return VG_ERR_ARG;
+  }
+  return VG_OK;
+}
+
+int require_f64(const vg_plan* p) {
+  if (p->precision != VG_F64) {
+    set_error("operation not available in this precision mode");
+    return VG_ERR_UNSUPPORTED;
+  }
+  return VG_OK;
+}
+
+int require_fft_v(const vg_plan* p) {
+  if (!p->nv_pow2 || p->nv > 8192) {
+    set_error("v-advection needs nv a power of two <= 8192, got " + std::to_string(p->nv));
+    return VG_ERR_UNSUPPORTED;
+  }
+  return VG_OK;
+}
+
+int require_fft_x(const vg_plan* p) {
+  if (!p->nx_pow2 || p->nx > 8192) {
+    set_error("x-advection needs nx a power of two <= 8192, got " + std::to_string(p->nx));
+    return VG_ERR_UNSUPPORTED;
+  }
+  return VG_OK;
+}
+
+// Run one launcher, bracketed by events when profiling is on.
+template <typename Fn>
+cudaError_t prof_run(vg_plan* p, int kind, cudaStream_t s, Fn fn) {
+  auto* ps = static_cast<ProfState*>(p->prof);
+  if (!ps || !ps->enabled) return fn();
+  cudaEvent_t b = ps->next(), e = ps->next();
+  if (!b || !e) return cudaErrorMemoryAllocation;
+  cudaError_t err = cudaEventRecord(b, s);
+  if (err != cudaSuccess) return err;
+  err = fn();
+  if (err != cudaSuccess) return err;
+  err = cudaEventRecord(e, s);
+  ps->recs.push_back({kind, b, e});
+  return err;
+}
+
+// One FP step: moments of the operator, then the tridiagonal solve.
+int collision_f64(vg_plan* p, double* f, cudaStream_t s) {
+  if (p->collision == VG_COLL_NONE) return VG_OK;
+  MomSpec spec;
+  if (p->collision == VG_COLL_DG) {
+    spec.nm = 2;
+    spec.kind[0] = MOM_V;   // vbar = trapz(f v)
+    spec.arg[0] = 0;
+    spec.kind[1] = MOM_DG2; // v0t^2 = trapz(f (v - vbar)^2)
+    spec.arg[1] = 0;
+  } else {
+    spec.nm = 2;
+    spec.kind[0] = MOM_ONE;  // unused slot, keeps the column layout of the DG case
+    spec.arg[0] = 0;
+    spec.kind[1] = MOM_W;    // v0t^2 = trapz(f v**2.0)
+    spec.arg[1] = 0;
+  }
+  VG_CHECK(cuda_status(prof_run(p, PK_FP_MOMENTS, s, [&] { return launch_row_moments_f64(*p, f, spec, p->mom, MOM_STRIDE, s); }),
+                       "collision moments"));
+  return cuda_status(prof_run(p, PK_FP_SOLVE, s, [&] { return launch_thomas_f64(*p, f, p->mom, 0, 1, s); }),
+                     "tridiagonal solve");
+}
+
+int field_f64(vg_plan* p, const double* f, const double* driver, const FieldTime& ft, double* e,
+              cudaStream_t s) {
+  MomSpec spec;
+  spec.nm = 1;
+  spec.kind[0] = MOM_ONE;
+  spec.arg[0] = 0;
+  VG_CHECK(cuda_status(prof_run(p, PK_DENSITY, s, [&] { return launch_row_moments_f64(*p, f, spec, p->dens, 1, s); }),
+                       "charge density"));
+  return cuda_status(prof_run(p, PK_POISSON, s, [&] { return launch_poisson_f64(*p, p->dens, 1, driver, ft, e, s); }),
+                     "poisson");
+}
+
+// The launch sequence of nsteps steps (vlapy/core/step.py:302-326).
+int step_sequence_f64(vg_plan* p, double* f, double* e, const vg_history* h, const double* tb,
+                      const double* db, int i0, int nsteps, cudaStream_t s) {
+  const double dt = p->dt;
+  for (int k = 0; k < nsteps; ++k) {
+    const int i = i0 + k;
+    FieldTime ft;
+    ft.t_ptr = tb + i;
+    ft.t_host = 0.0;
+    ft.use_pulses = p->n_pulses > 0;
+    auto field_at = [&](std::initializer_list<double> adds) {
+      ft.nadd = 0;
+      for (double a : adds) ft.add[ft.nadd++] = a;
+      return field_f64(p, f, nullptr, ft, e, s);
+    };
+    auto E = [&](double d) {
+      return cuda_status(prof_run(p, PK_EDFDV, s, [&] { return launch_edfdv_f64(*p, f, e, d, s); }), "edfdv");
+    };
+    auto X = [&](double d) {
+      return cuda_status(prof_run(p, PK_VDFDX, s, [&] { return launch_vdfdx_f64(*p, f, d, s); }), "vdfdx");
+    };
+    if (p->integrator == VG_LEAPFROG) {
+      // vlapy/core/vlasov_poisson.py:36-58
+      VG_CHECK(E(0.5 * dt));
+      VG_CHECK(X(dt));
+      VG_CHECK(field_at({dt}));
+      VG_CHECK(E(0.5 * dt));
+    } else if (p->integrator == VG_PEFRL) {
+      // vlapy/core/vlasov_poisson.py:82-152
+      const double xsi = 0.1786178958448091, lambd = -0.2123418310626054, chi = -0.6626458266981849e-1;
+      const double d1 = xsi * dt, d2 = chi * dt, d3 = (1.0 - 2.0 * (chi + xsi)) * dt, d4 = d2, d5 = d1;
+      const double k1 = 0.5 * (1.0 - 2.0 * lambd) * dt, k2 = lambd * dt, k3 = k2, k4 = k1;
+      VG_CHECK(X(d1));
+      VG_CHECK(field_at({d1}));
+      VG_CHECK(E(k1));
+      VG_CHECK(X(d2));
+      VG_CHECK(field_at({d1, d2}));
+      VG_CHECK(E(k2));
+      VG_CHECK(X(d3));
+      VG_CHECK(field_at({d1, d2, d3}));
+      VG_CHECK(E(k3));
+      VG_CHECK(X(d4));
+      VG_CHECK(field_at({d1, d2, d3, d4}));
+      VG_CHECK(E(k4));
+      VG_CHECK(X(d5));
+      VG_CHECK(field_at({d1, d2, d3, d4, d5}));
+    } else {
+      // vlapy/core/vlasov_poisson.py:157-232
+      const double a1 = 0.168735950563437422448196, a2 = 0.377851589220928303880766,
+                   a3 = -0.093175079568731452657924, b1 = 0.049086460976116245491441,
+                   b2 = 0.264177609888976700200146, b3 = 0.186735929134907054308413,
+                   c1 = -0.000069728715055305084099, c2 = -0.000625704827430047189169,
+                   c3 = -0.002213085124045325561636, d2c = -2.916600457689847816445691e-6,
+                   d3c = 3.048480261700038788680723e-5, e3 = 4.985549387875068121593988e-7;
+      const double D1 = b1 + 2.0 * c1 * std::pow(dt, 2.0);
+      const double D2 = b2 + 2.0 * c2 * std::pow(dt, 2.0) + 4.0 * d2c * std::pow(dt, 4.0);
+      const double D3 = b3 + 2.0 * c3 * std::pow(dt, 2.0) + 4.0 * d3c * std::pow(dt, 4.0) -
+                        8.0 * e3 * std::pow(dt, 6.0);
+      const double xs[5] = {a1, a2, a3, a2, a1};
+      const double ks[5] = {D2, D3, D3, D2, D1};
+      VG_CHECK(E(D1 * dt));
+      for (int q = 0; q < 5; ++q) {
+        VG_CHECK(X(xs[q] * dt));
+        VG_CHECK(field_at({xs[q] * dt}));
+        VG_CHECK(E(ks[q] * dt));
+      }
+    }
+    VG_CHECK(collision_f64(p, f, s));
+    if (h) {
+      const double* de = db ? db + (size_t)i * p->nx : nullptr;
+      VG_CHECK(cuda_status(prof_run(p, PK_STORAGE, s, [&] { return launch_storage_f64(*p, f, e, de, *h, i, s); }),
+                           "storage step"));
+    }
+  }
+  return VG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int vg_version(void) { return 1; }
+
+const char* vg_last_error(void) { return g_err.c_str(); }
+
+int vg_plan_create(const vg_run_desc* d, vg_plan** out) {
+  if (!d || !out) {
+    set_error("null descriptor or output pointer");
+    return VG_ERR_ARG;
+  }
+  *out = nullptr;
+  if (d->nx < 2 || d->nv < 2) {
+    set_error("nx and nv must be >= 2");
+    return VG_ERR_ARG;
+  }
+  if (!d->x || !d->v || !d->kx || !d->kv || !d->one_over_kx || !d->v_pow) {
+    set_error("descriptor arrays x, v, kx, kv, one_over_kx, v_pow are required");
+    return VG_ERR_ARG;
+  }
+  if (d->precision != VG_F64 && d->precision != VG_F32_DELTA_F) {
+    set_error("unknown precision mode");
+    return VG_ERR_ARG;
+  }
+  if (d->precision == VG_F32_DELTA_F && !d->f_background) {
+    set_error("VG_F32_DELTA_F needs f_background");
+    return VG_ERR_ARG;
+  }
+  if (d->collision < VG_COLL_NONE || d->collision > VG_COLL_DG || d->integrator < VG_LEAPFROG ||
+      d->integrator > VG_H_SIXTH || d->n_pulses < 0 || (d->n_pulses > 0 && !d->pulses)) {
+    set_error("bad collision, integrator or pulse fields");
+    return VG_ERR_ARG;
+  }
+  vg_plan* p = new vg_plan();
+  std::memset(p, 0, sizeof(vg_plan));
+  p->nx = d->nx;
+  p->nv = d->nv;
+  p->precision = d->precision;
+  p->collision = d->collision;
+  p->integrator = d->integrator;
+  p->n_pulses = d->n_pulses;
+  p->dt = d->dt;
+  p->nu = d->nu;
+  p->dx = d->dx;
+  p->dv = d->dv;
+  p->dv_sq = d->dv_sq;
+  p->nudt = d->nu * d->dt;
+  p->nx_pow2 = is_pow2(d->nx);
+  p->nv_pow2 = is_pow2(d->nv);
+  const size_t nx = d->nx, nv = d->nv;
+  int st = VG_OK;
+#define TRY(expr)                         \
+  do {                                    \
+    st = (expr);                          \
+    if (st != VG_OK) {                    \
+      free_plan(p);                       \
+      return st;                          \
+    }                                     \
+  } while (0)
+  TRY(dev_copy(&p->x, d->x, nx, "x"));
+  TRY(dev_copy(&p->v, d->v, nv, "v"));
+  TRY(dev_copy(&p->kx, d->kx, nx, "kx"));
+  TRY(dev_copy(&p->kv, d->kv, nv, "kv"));
+  TRY(dev_copy(&p->inv_kx, d->one_over_kx, nx, "one_over_kx"));
+  TRY(dev_copy(&p->v_pow, d->v_pow, 5 * nv, "v_pow"));
+  if (d->f_background) TRY(dev_copy(&p->f_bg, d->f_background, nv, "f_background"));
+  if (d->n_pulses > 0) TRY(dev_copy(&p->pulses, d->pulses, (size_t)d->n_pulses, "pulses"));
+  TRY(dev_copy<cx<double>>(&p->tw64, nullptr, FFT_NMAX, "twiddles"));
+  TRY(dev_copy<cx<float>>(&p->tw32, nullptr, FFT_NMAX, "twiddles"));
+  std::vector<int> tv = pairwise_table(d->nv - 1), tx = pairwise_table(d->nx);
+  p->pw_v_leaves = tv[0];
+  p->pw_x_leaves = tx[0];
+  p->pw_v_words = (int)tv.size();
+  p->pw_x_words = (int)tx.size();
+  TRY(dev_copy(&p->pw_v, tv.data(), tv.size(), "pairwise table"));
+  TRY(dev_copy(&p->pw_x, tx.data(), tx.size(), "pairwise table"));
+  TRY(dev_copy<double>(&p->dens, nullptr, nx, "scratch"));
+  TRY(dev_copy<double>(&p->mom, nullptr, nx * MOM_STRIDE, "scratch"));
+  TRY(dev_copy<double>(&p->rho, nullptr, nx, "scratch"));
+  TRY(dev_copy<double>(&p->etmp, nullptr, 4 * nx + 4, "scratch"));
+  if (d->precision == VG_F64 && d->collision != VG_COLL_NONE)
+    TRY(dev_copy<double>(&p->bb, nullptr, nx * nv, "thomas scratch"));
+  TRY(cuda_status(launch_twiddles(*p, 0), "twiddles"));
+  TRY(cuda_status(cudaDeviceSynchronize(), "plan setup"));
+  p->graph_cache = new GraphCache();
+  p->prof = new ProfState();
+#undef TRY
+  *out = p;
+  return VG_OK;
+}
+
+int vg_plan_destroy(vg_plan* p) {
+  if (!p) return VG_OK;
+  cudaDeviceSynchronize();
+  free_plan(p);
+  return VG_OK;
+}
+
+int vg_edfdv(vg_plan* p, void* f, const double* e, double dt, vg_stream stream) {
+  VG_CHECK(require_plan(p));
+  VG_CHECK(require_f64(p));
+  VG_CHECK(require_fft_v(p));
+  if (!f || !e) {
+    set_error("null f or e");
+    return VG_ERR_ARG;
+  }
+  return cuda_status(launch_edfdv_f64(*p, static_cast<double*>(f), e, dt, (cudaStream_t)stream), "edfdv");
+}
+
+int vg_vdfdx(vg_plan* p, void* f, double dt, vg_stream stream) {
+  VG_CHECK(require_plan(p));
+  VG_CHECK(require_f64(p));
+  VG_CHECK(require_fft_x(p));
+  if (!f) {
+    set_error("null f");
+    return VG_ERR_ARG;
+  }
+  return cuda_status(launch_vdfdx_f64(*p, static_cast<double*>(f), dt, (cudaStream_t)stream), "vdfdx");
+}
+
+int vg_charge_density(vg_plan* p, const void* f, double* n, vg_stream stream) {
+  VG_CHECK(require_plan(p));
+  VG_CHECK(require_f64(p));
+  if (!f || !n) {
+    set_error("null f or n");
+    return VG_ERR_ARG;
+  }
+  MomSpec spec;
+  spec.nm = 1;
+  spec.kind[0] = MOM_ONE;
+  spec.arg[0] = 0;
+  return cuda_status(launch_row_moments_f64(*p, static_cast<const double*>(f), spec, n, 1, (cudaStream_t)stream),
+                     "charge density");
+}
+
+int vg_poisson(vg_plan* p, const double* rho, double* e, vg_stream stream) {
+  VG_CHECK(require_plan(p));
+  if (!rho || !e) {
+    set_error("null rho or e");
+    return VG_ERR_ARG;
+  }
+  FieldTime ft{};
+  ft.use_pulses = 0;
+  return cuda_status(launch_poisson_f64(*p, rho, 0, nullptr, ft, e, (cudaStream_t)stream), "poisson");
+}
+
+int vg_field_solve(vg_plan* p, const void* f, const double* driver, double* e, vg_stream stream) {
+  VG_CHECK(require_plan(p));
+  VG_CHECK(require_f64(p));
+  if (!f || !e) {
+    set_error("null f or e");
+    return VG_ERR_ARG;
+  }
+  FieldTime ft{};
+  ft.use_pulses = 0;
+  return field_f64(p, static_cast<const double*>(f), driver, ft, e, (cudaStream_t)stream);
+}
+
+int vg_collision_step(vg_plan* p, void* f, vg_stream stream) {
+  VG_CHECK(require_plan(p));
+  VG_CHECK(require_f64(p));
+  if (!f) {
+    set_error("null f");
+    return VG_ERR_ARG;
+  }
+  return collision_f64(p, static_cast<double*>(f), (cudaStream_t)stream);
+}
+
+static int check_history(const vg_plan* p, const vg_history* h, int i_last) {
+  if (!h) return VG_OK;
+  if (i_last >= h->nt) {
+    set_error("storage index beyond the history length");
+    return VG_ERR_STATE;
+  }
+  if (h->stored_f && !h->store_all) {
+    if (h->n_slots < 1 || h->n_modes < 1 || (h->n_modes != 1 && h->n_modes != h->n_slots) ||
+        h->n_modes > p->nx) {
+      set_error("stored_f: n_modes must be 1 or equal n_slots, and <= nx");
+      return VG_ERR_ARG;
+    }
+  }
+  return VG_OK;
+}
+
+int vg_storage_step(vg_plan* p, const void* f, const double* e, const double* de, const vg_history* h,
+                    int32_t i, vg_stream stream) {
+  VG_CHECK(require_plan(p));
+  VG_CHECK(require_f64(p));
+  if (!f || !e || !h || i < 0) {
+    set_error("null f, e or history, or negative index");
+    return VG_ERR_ARG;
+  }
+  VG_CHECK(check_history(p, h, i));
+  return cuda_status(launch_storage_f64(*p, static_cast<const double*>(f), e, de, *h, i, (cudaStream_t)stream),
+                     "storage step");
+}
+
+int vg_driver(vg_plan* p, double t, double* out, vg_stream stream) {
+  VG_CHECK(require_plan(p));
+  if (!out) {
+    set_error("null output");
+    return VG_ERR_ARG;
+  }
+  FieldTime ft{};
+  ft.t_ptr = nullptr;
+  ft.t_host = t;
+  ft.nadd = 0;
+  ft.use_pulses = 1;
+  return cuda_status(launch_driver(*p, ft, out, (cudaStream_t)stream), "driver");
+}
+
+int vg_run_steps(vg_plan* p, void* f, double* e, const vg_history* h, const double* time_batch,
+                 const double* driver_batch, int32_t i0, int32_t nsteps, int32_t use_graph, vg_stream stream) {
+  VG_CHECK(require_plan(p));
+  VG_CHECK(require_f64(p));
+  VG_CHECK(require_fft_v(p));
+  VG_CHECK(require_fft_x(p));
+  if (!f || !e || !time_batch || i0 < 0 || nsteps < 0) {
+    set_error("null f, e or time_batch, or negative step range");
+    return VG_ERR_ARG;
+  }
+  if (nsteps == 0) return VG_OK;
+  VG_CHECK(check_history(p, h, i0 + nsteps - 1));
+  cudaStream_t s = (cudaStream_t)stream;
+  double* fd = static_cast<double*>(f);
+  if (static_cast<ProfState*>(p->prof)->enabled) use_graph = 0;
+  if (!use_graph) return step_sequence_f64(p, fd, e, h, time_batch, driver_batch, i0, nsteps, s);
+  auto* gc = static_cast<GraphCache*>(p->graph_cache);
+  GraphKey key;
+  std::memset(&key, 0, sizeof(key));
+  key.f = f;
+  key.e = e;
+  key.tb = time_batch;
+  key.db = driver_batch;
+  if (h) key.h = *h;
+  key.i0 = i0;
+  key.n = nsteps;
+  key.s = s;
+  auto it = gc->execs.find(key);
+  if (it == gc->execs.end()) {
+    if (s == 0) {
+      set_error("graph mode needs a non-default stream");
+      return VG_ERR_ARG;
+    }
+    VG_CHECK(cuda_status(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed), "begin capture"));
+    int st = step_sequence_f64(p, fd, e, h, time_batch, driver_batch, i0, nsteps, s);
+    cudaGraph_t graph = nullptr;
+    cudaError_t cerr = cudaStreamEndCapture(s, &graph);
+    if (st != VG_OK) {
+      if (graph) cudaGraphDestroy(graph);
+      return st;
+    }
+    VG_CHECK(cuda_status(cerr, "end capture"));
+    cudaGraphExec_t exec = nullptr;
+    cerr = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    VG_CHECK(cuda_status(cerr, "graph instantiate"));
+    it = gc->execs.emplace(key, exec).first;
+  }
+  return cuda_status(cudaGraphLaunch(it->second, s), "graph launch");
+}
+
+int vg_profile_enable(vg_plan* p, int32_t enable) {
+  VG_CHECK(require_plan(p));
+  auto* ps = static_cast<ProfState*>(p->prof);
+  ps->enabled = enable != 0;
+  return VG_OK;
+}
+
+int vg_profile_read(vg_plan* p, vg_prof_entry* out, int32_t max, int32_t* n_out) {
+  VG_CHECK(require_plan(p));
+  if (!n_out || (max > 0 && !out)) {
+    set_error("null output");
+    return VG_ERR_ARG;
+  }
+  auto* ps = static_cast<ProfState*>(p->prof);
+  double ms[PK_COUNT] = {0};
+  int64_t cnt[PK_COUNT] = {0};
+  for (auto& r : ps->recs) {
+    VG_CHECK(cuda_status(cudaEventSynchronize(r.e), "profile sync"));
+    float t = 0.f;
+    VG_CHECK(cuda_status(cudaEventElapsedTime(&t, r.b, r.e), "profile elapsed"));
+    ms[r.kind] += t;
+    cnt[r.kind] += 1;
+  }
+  ps->recs.clear();
+  ps->used = 0;
+  int n = 0;
+  for (int k = 0; k < PK_COUNT; ++k) {
+    if (!cnt[k]) continue;
+    if (n < max) {
+      std::memset(&out[n], 0, sizeof(vg_prof_entry));
+      std::snprintf(out[n].name, sizeof(out[n].name), "%s", kProfNames[k]);
+      out[n].launches = cnt[k];
+      out[n].total_ms = ms[k];
+      out[n].bytes_per_launch = prof_bytes(p, k);
+    }
+    ++n;
+  }
+  *n_out = n < max ? n : max;
+  return VG_OK;
+}
+
+}  // extern "C"

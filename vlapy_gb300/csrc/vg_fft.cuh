@@ -1,0 +1,175 @@
+// Shared-memory Stockham FFT for one CTA-cooperative complex sequence.
+//
+// A length-N sequence (N a power of two, 2..16384) lives in shared memory.
+// N/R threads cooperate on it: every pass each thread loads R (or fewer, on
+// the last, shorter-radix pass) elements with stride N/r, applies the
+// twiddles exp(-+2 pi i m k / (Ns r)), does a radix-r DFT in registers and
+// writes the results back in Stockham autosort order, so the output is in
+// natural order with no bit reversal.  All sequences of a CTA run the same
+// passes in lockstep and synchronise with __syncthreads, so every thread of
+// the CTA must call the transform.
+//
+// Twiddles come from one table tw[q] = exp(-2 pi i q / FFT_NMAX) built once
+// per plan (sincospi in FP64), indexed with stride FFT_NMAX / (Ns r).
+#pragma once
+
+#include "vg_common.cuh"
+
+namespace vg {
+
+constexpr int FFT_LOG_NMAX = 14;
+constexpr int FFT_NMAX = 1 << FFT_LOG_NMAX;
+
+// Radix used per pass for a length-N transform of element type T: the whole
+// sequence in one thread for N <= 8, otherwise radix 8, or radix 16 where
+// radix 8 would need more than 256 (FP64) / 1024 (FP32) threads per sequence
+// and so cap the registers per thread.
+template <typename T>
+__host__ __device__ constexpr int fft_radix(int n) {
+  return n <= 8 ? n : (sizeof(T) == 8 ? (n <= 2048 ? 8 : 16) : (n <= 8192 ? 8 : 16));
+}
+template <typename T>
+__host__ __device__ constexpr int fft_threads(int n) { return n / fft_radix<T>(n); }
+// CTA sizes of the row (pairs of rows) and column (tiles of columns) kernels
+template <typename T>
+__host__ __device__ constexpr int row_block(int n) {
+  return fft_threads<T>(n) >= 256 ? fft_threads<T>(n) : 256;
+}
+template <typename T>
+__host__ __device__ constexpr int col_seqs(int nx) {
+  return (256 / fft_threads<T>(nx) >= 2) ? 256 / fft_threads<T>(nx)
+       : (2 * fft_threads<T>(nx) <= 512 ? 2 : 1);
+}
+
+// multiply by exp(-+2 pi i k / R), forward sign '-' unless INV
+template <typename T, int R, bool INV>
+__device__ __forceinline__ cx<T> rot_const(int k, cx<T> a) {
+  if (k == 0) return a;
+  if (4 * k == R) return INV ? cx<T>{-a.y, a.x} : cx<T>{a.y, -a.x};
+  const int j = (16 / R) * k;
+  const T c = (T)cos16(j), s = (T)sin16(j);
+  if (INV) return {a.x * c - a.y * s, a.x * s + a.y * c};
+  return {a.x * c + a.y * s, a.y * c - a.x * s};
+}
+
+template <typename T, int R, bool INV>
+struct Dft {
+  static __device__ __forceinline__ void run(cx<T>* a) {
+    cx<T> e[R / 2], o[R / 2];
+#pragma unroll
+    for (int i = 0; i < R / 2; ++i) {
+      e[i] = a[2 * i];
+      o[i] = a[2 * i + 1];
+    }
+    Dft<T, R / 2, INV>::run(e);
+    Dft<T, R / 2, INV>::run(o);
+#pragma unroll
+    for (int k = 0; k < R / 2; ++k) {
+      const cx<T> t = rot_const<T, R, INV>(k, o[k]);
+      a[k] = e[k] + t;
+      a[k + R / 2] = e[k] - t;
+    }
+  }
+};
+template <typename T, bool INV>
+struct Dft<T, 2, INV> {
+  static __device__ __forceinline__ void run(cx<T>* a) {
+    const cx<T> t = a[0];
+    a[0] = t + a[1];
+    a[1] = t - a[1];
+  }
+};
+template <typename T, bool INV>
+struct Dft<T, 1, INV> {
+  static __device__ __forceinline__ void run(cx<T>*) {}
+};
+
+template <typename T>
+__device__ __forceinline__ cx<T> twiddle(const cx<T>* __restrict__ tw, int q, bool inv) {
+  cx<T> w = tw[q];
+  if (inv) w.y = -w.y;
+  return w;
+}
+
+template <typename T, int N, bool INV, int NS>
+struct StockhamPass {
+  static __device__ __forceinline__ void run(cx<T>* s, int t, const cx<T>* __restrict__ tw) {
+    constexpr int R = fft_radix<T>(N);
+    constexpr int r = (N / NS < R) ? (N / NS) : R;
+    constexpr int NB = N / r;      // butterflies in this pass
+    constexpr int G = N / R;       // threads per sequence
+    constexpr int BPT = NB / G;    // butterflies per thread
+    constexpr int TWS = FFT_NMAX / (NS * r);
+    cx<T> a[BPT][r];
+#pragma unroll
+    for (int b = 0; b < BPT; ++b) {
+      const int j = t + b * G;
+      const int k = j & (NS - 1);
+#pragma unroll
+      for (int m = 0; m < r; ++m) a[b][m] = s[j + m * NB];
+      if (NS > 1) {
+#pragma unroll
+        for (int m = 1; m < r; ++m) a[b][m] = cmul(a[b][m], twiddle(tw, m * k * TWS, INV));
+      }
+      Dft<T, r, INV>::run(a[b]);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int b = 0; b < BPT; ++b) {
+      const int j = t + b * G;
+      const int k = j & (NS - 1);
+      const int base = (j - k) * r + k;
+#pragma unroll
+      for (int m = 0; m < r; ++m) s[base + m * NS] = a[b][m];
+    }
+    __syncthreads();
+    StockhamPass<T, N, INV, NS * r>::run(s, t, tw);
+  }
+};
+template <typename T, int N, bool INV>
+struct StockhamPass<T, N, INV, N> {
+  static __device__ __forceinline__ void run(cx<T>*, int, const cx<T>* __restrict__) {}
+};
+
+// In-place unnormalised transform of s[0..N) by the N/R threads t = 0..N/R-1.
+// Caller must have synchronised after writing s; the result is visible to
+// the whole CTA on return.
+template <typename T, int N, bool INV>
+__device__ __forceinline__ void block_fft(cx<T>* s, int t, const cx<T>* __restrict__ tw) {
+  StockhamPass<T, N, INV, 1>::run(s, t, tw);
+}
+
+// Two real sequences a, b packed as z = a + i b; s holds Z = FFT(z).  Replace
+// it by FFT(a' + i b') where a' = Re IFFT(Pa . FFT(a)), b' likewise, and
+// P(k) = cos(th(k)) + i sin(th(k)).  At the Nyquist bin only Re(P) acts,
+// which is what taking the real part of the inverse transform does to the
+// reference's full complex product.  phase(k, &ca, &sa, &cb, &sb) returns the
+// two rotations for bin k.
+template <typename T, typename PhaseFn>
+__device__ __forceinline__ void two_real_rotate(cx<T>* s, int N, int t, int G, PhaseFn phase) {
+  for (int k = t; k <= N / 2; k += G) {
+    T ca, sa, cb, sb;
+    if (k == 0) {
+      phase(0, ca, sa, cb, sb);
+      const cx<T> z = s[0];
+      // DC bins of both real sequences are real: only Re(P) survives
+      s[0] = {z.x * ca, z.y * cb};
+      continue;
+    }
+    phase(k, ca, sa, cb, sb);
+    if (2 * k == N) {
+      const cx<T> z = s[k];
+      s[k] = {z.x * ca, z.y * cb};
+      continue;
+    }
+    const cx<T> zk = s[k], zm = s[N - k];
+    const cx<T> fa = {(zk.x + zm.x) * T(0.5), (zk.y - zm.y) * T(0.5)};
+    const cx<T> fb = {(zk.y + zm.y) * T(0.5), (zm.x - zk.x) * T(0.5)};
+    const cx<T> ga = {ca * fa.x - sa * fa.y, ca * fa.y + sa * fa.x};
+    const cx<T> gb = {cb * fb.x - sb * fb.y, cb * fb.y + sb * fb.x};
+    s[k] = {ga.x - gb.y, ga.y + gb.x};
+    s[N - k] = {ga.x + gb.y, gb.x - ga.y};
+  }
+}
+
+}  // namespace vg

@@ -1,0 +1,77 @@
+// Internal plan layout and kernel launchers shared by the translation units.
+#pragma once
+
+#include <string>
+
+#include "vg_common.cuh"
+#include "vg_fft.cuh"
+#include "vlagpu.h"
+
+struct vg_plan {
+  // scalars of the run
+  int nx, nv, precision, collision, integrator, n_pulses;
+  double dt, nu, dx, dv, dv_sq, nudt;
+  int nx_pow2, nv_pow2;
+  // device constants
+  double* x;
+  double* v;
+  double* kx;
+  double* kv;
+  double* inv_kx;
+  double* v_pow;     // [5][nv]
+  double* f_bg;      // [nv] (delta-f background) or null
+  vg_pulse* pulses;  // [n_pulses]
+  vg::cx<double>* tw64;  // [FFT_NMAX]
+  vg::cx<float>* tw32;   // [FFT_NMAX]
+  int* pw_v;   // NumPy pairwise tree over nv-1 trapz terms
+  int* pw_x;   // NumPy pairwise tree over nx values (x-means)
+  int pw_v_leaves, pw_x_leaves, pw_v_words, pw_x_words;
+  // scratch
+  double* dens;   // [nx]
+  double* mom;    // [nx][MOM_STRIDE]
+  double* bb;     // [nx][nv] Thomas elimination scratch (FP64 mode)
+  double* rho;    // [nx]
+  double* etmp;   // [nx]
+  // graph cache and per-kernel profiling state
+  void* graph_cache;
+  void* prof;
+};
+
+namespace vg {
+
+constexpr int MOM_STRIDE = 8;
+
+// moment kinds for the pairwise-trapz row kernel
+enum MomKind : int { MOM_ONE = 0, MOM_W = 1, MOM_SQ = 2, MOM_FLOGF = 3, MOM_DG2 = 4, MOM_V = 5 };
+struct MomSpec {
+  int nm;
+  int kind[MOM_STRIDE];
+  int arg[MOM_STRIDE];  // MOM_W: row of v_pow; MOM_DG2: index of the vbar moment
+};
+
+void set_error(const std::string& msg);
+int cuda_status(cudaError_t err, const char* what);
+
+// launchers (return cudaError_t of the launch)
+cudaError_t launch_edfdv_f64(const vg_plan& p, double* f, const double* e, double dt, cudaStream_t s);
+cudaError_t launch_vdfdx_f64(const vg_plan& p, double* f, double dt, cudaStream_t s);
+cudaError_t launch_row_moments_f64(const vg_plan& p, const double* f, const MomSpec& spec,
+                                   double* out, int out_stride, cudaStream_t s);
+// e = [driver or pulses(t)] + Re IFFT(i/kx FFT(rho)), rho = 1 - dens (dens_is_density) or dens
+struct FieldTime {
+  const double* t_ptr;  // device time value (time_batch + i) or null -> t_host
+  double t_host;
+  int nadd;
+  double add[6];        // sub-step offsets added left to right
+  int use_pulses;
+};
+cudaError_t launch_poisson_f64(const vg_plan& p, const double* dens, int dens_is_density,
+                               const double* driver, const FieldTime& ft, double* e, cudaStream_t s);
+cudaError_t launch_thomas_f64(const vg_plan& p, double* f, const double* mom, int vbar_col,
+                              int vth_col, cudaStream_t s);
+cudaError_t launch_storage_f64(const vg_plan& p, const double* f, const double* e, const double* de,
+                               const vg_history& h, int i, cudaStream_t s);
+cudaError_t launch_driver(const vg_plan& p, const FieldTime& ft, double* out, cudaStream_t s);
+cudaError_t launch_twiddles(vg_plan& p, cudaStream_t s);
+
+}  // namespace vg

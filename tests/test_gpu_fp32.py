@@ -1,0 +1,178 @@
+"""FP32 delta-f mode against the FP64 CPU oracle.
+
+The FP32 state is g = f - f0(v); errors are measured relative to the size of
+the perturbation (||f_ref - f0||), which is what FP32 can resolve, and the
+physics bars are the ones of the method: Landau damping rate within 1% and
+field-energy history within 1e-3 (relative) of the FP64 oracle.
+"""
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from oracle import vlapy_oracle as vo  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+TOL_OP = 2e-5       # per operator, relative to the perturbation
+TOL_STEP = 5e-5     # after a few full steps
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib_loaded():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from vlapy_gb300 import _lib
+    _lib.load()
+
+
+def setup(nx, nv, k=0.3, vmax=6.4, amp=1e-3, nu=0.0, op="dg", dt=0.1, seed=1, shift=0.0):
+    from vlapy_gb300.plan import Plan
+    dx, x, kx, inv = vo.spatial_axis(0.0, 2 * np.pi / k, nx)
+    dv, v, kv = vo.velocity_axis(vmax, nv)
+    rng = np.random.default_rng(seed)
+    pert = np.zeros(nx)
+    for m in range(1, min(4, nx // 2 + 1)):
+        pert += amp * rng.uniform(0.3, 1.0) * np.cos(m * k * x + rng.uniform(0, 2 * np.pi))
+    fv = np.exp(-((v - shift) ** 2) / 2.0)
+    fv = fv / np.trapezoid(fv, dx=dv)
+    f = fv[None, :] * (1.0 + pert)[:, None]
+    f0 = f.mean(axis=0)
+    p = Plan(nx, nv, x, v, kx, kv, inv, dx, dv, dt=dt, nu=nu, collision=op if nu > 0 else "none",
+             precision="fp32-deltaf", f_background=f0)
+    return p, f, f0, (x, v, kx, kv, inv, dx, dv)
+
+
+def g_of(f, f0):
+    return torch.as_tensor((f - f0[None, :]).astype(np.float32), device="cuda")
+
+
+def f_of(g, f0):
+    return g.double().cpu().numpy() + f0[None, :]
+
+
+def rel_pert(f_gpu, f_ref, f0):
+    return np.linalg.norm(f_gpu - f_ref) / np.linalg.norm(f_ref - f0[None, :])
+
+
+SHAPES = [(32, 512), (16, 256), (64, 1024), (128, 256), (2, 64), (256, 8192), (4096, 64)]
+
+
+@pytest.mark.parametrize("nx,nv", SHAPES)
+@pytest.mark.parametrize("amp", [1e-3, 1e-6])
+def test_fp32_edfdv(nx, nv, amp):
+    p, f, f0, (x, v, kx, kv, inv, dx, dv) = setup(nx, nv, amp=amp)
+    e = amp * (3.0 * np.sin(0.3 * x) + 0.5)
+    ref = vo.edfdv_exponential(f, e, kv, 0.05)
+    g = g_of(f, f0)
+    p.edfdv(g, torch.as_tensor(e, device="cuda"), 0.05)
+    assert rel_pert(f_of(g, f0), ref, f0) <= TOL_OP
+
+
+@pytest.mark.parametrize("nx,nv", SHAPES)
+@pytest.mark.parametrize("amp", [1e-3, 1e-6])
+def test_fp32_vdfdx(nx, nv, amp):
+    p, f, f0, (x, v, kx, kv, inv, dx, dv) = setup(nx, nv, amp=amp)
+    for dt in (0.1, 0.05):
+        ref = vo.vdfdx_exponential(f, kx, v, dt)
+        g = g_of(f, f0)
+        p.vdfdx(g, dt)
+        assert rel_pert(f_of(g, f0), ref, f0) <= TOL_OP
+
+
+@pytest.mark.parametrize("op", ["dg", "lb"])
+@pytest.mark.parametrize("nx,nv", [(4, 1024), (32, 512), (16, 8192), (8, 16)])
+def test_fp32_collision(op, nx, nv):
+    p, f, f0, (x, v, kx, kv, inv, dx, dv) = setup(nx, nv, amp=1e-3, nu=1e-2, op=op, shift=0.3)
+    g = g_of(f, f0)
+    ref = f.copy()
+    for _ in range(4):
+        ref = vo.collision_step(ref, v, 1e-2, 0.1, dv, op)
+        p.collision_step(g)
+    # the collision operator moves the whole of f (drift/heating of f0 too):
+    # compare relative to the change it makes plus the perturbation
+    scale = np.linalg.norm(ref - f) + np.linalg.norm(f - f0[None, :])
+    assert np.linalg.norm(f_of(g, f0) - ref) / scale <= TOL_OP
+
+
+@pytest.mark.parametrize("nx,nv", [(32, 512), (64, 1024), (8, 256)])
+def test_fp32_field(nx, nv):
+    p, f, f0, (x, v, kx, kv, inv, dx, dv) = setup(nx, nv, amp=1e-4)
+    ref = vo.total_field(np.zeros(nx), f, dv, inv)
+    out = torch.empty(nx, dtype=torch.float64, device="cuda")
+    p.field_solve(g_of(f, f0), None, out)
+    assert np.linalg.norm(out.cpu().numpy() - ref) / np.linalg.norm(ref) <= TOL_OP
+
+
+def _run_both(nx, nv, nsteps, nu=0.0, amp=1e-3, store=True, k=0.3, vmax=6.4, dt=0.1):
+    """nsteps leapfrog (+FP) steps on the GPU (fused, FP32) and in the oracle (FP64)."""
+    from vlapy_gb300.plan import history_struct
+    p, f, f0, (x, v, kx, kv, inv, dx, dv) = setup(nx, nv, amp=amp, nu=nu, k=k, vmax=vmax, dt=dt)
+    run = vo.OracleRun(nx, nv, 2 * np.pi / k, vmax, dt, nu=nu, operator="dg", n_modes=2)
+    st = vo.new_storage(f, np.zeros(nx), nsteps, 2)
+    st["time_batch"] = dt * np.arange(nsteps)
+    st["driver_array_batch"] = np.zeros((nsteps, nx))
+    dev = torch.device("cuda")
+    z = lambda *s: torch.zeros(s, dtype=torch.float64, device=dev)  # noqa: E731
+    gst = {"stored_f": torch.zeros((nsteps, 2, nv), dtype=torch.complex64, device=dev),
+           "fields": {kk: z(nsteps, nx) for kk in vo.FIELD_KEYS},
+           "series": {kk: z(nsteps) for kk in vo.SERIES_KEYS}}
+    hist = history_struct(gst, nx, 2) if store else None
+    g = g_of(f, f0)
+    e = z(nx)
+    tb = torch.as_tensor(st["time_batch"], device=dev)
+    db = z(nsteps, nx)
+    p.run_steps(g, e, hist, tb, db, 0, nsteps, use_graph=False)
+    for i in range(nsteps):
+        run.timestep(st, i)
+    return p, f0, g, e, gst, st
+
+
+def test_fp32_steps_match_oracle():
+    p, f0, g, e, gst, st = _run_both(32, 512, 10, nu=1e-3)
+    assert rel_pert(f_of(g, f0), st["f"], f0) <= TOL_STEP
+    assert np.linalg.norm(e.cpu().numpy() - st["e"]) / np.linalg.norm(st["e"]) <= TOL_STEP
+    for kk in ("e", "n", "T"):
+        got, ref = gst["fields"][kk].cpu().numpy(), st["fields"][kk]
+        np.testing.assert_allclose(got, ref, rtol=1e-6, atol=1e-6 * np.abs(ref).max(), err_msg=kk)
+    for kk in ("mean_n", "mean_T", "mean_e2", "mean_f2"):
+        np.testing.assert_allclose(gst["series"][kk].cpu().numpy(), st["series"][kk], rtol=1e-5, err_msg=kk)
+    sf, rf = gst["stored_f"].cpu().numpy(), st["stored_f"]
+    np.testing.assert_allclose(sf[:, 0], rf[:, 0], rtol=1e-5, atol=1e-6 * np.abs(rf[:, 0]).max())
+    np.testing.assert_allclose(sf[:, 1], rf[:, 1], atol=2e-5 * np.abs(rf[:, 1]).max())
+
+
+def test_fp32_graph_equals_direct():
+    """The captured graph of the fused FP32 step replays the direct launches."""
+    from vlapy_gb300.plan import history_struct
+    p, f, f0, (x, v, kx, kv, inv, dx, dv) = setup(64, 1024, amp=1e-3, nu=1e-3)
+    g1, g2 = g_of(f, f0), g_of(f, f0)
+    e1 = torch.zeros(64, dtype=torch.float64, device="cuda")
+    e2 = e1.clone()
+    tb = torch.as_tensor(0.1 * np.arange(20), device="cuda")
+    p.run_steps(g1, e1, None, tb, None, 0, 20, use_graph=False)
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        p.run_steps(g2, e2, None, tb, None, 0, 20, use_graph=True, stream=s)
+    torch.cuda.synchronize()
+    assert torch.equal(g1, g2) and torch.equal(e1, e2)
+
+
+def test_fp32_landau_damping_rate():
+    """Plain Landau damping workload (32x512, k=0.3, A=1e-4, dt=0.1, 1000 steps):
+    the FP32 damping rate and frequency are within 1% of the FP64 oracle's, and
+    the field-energy history within 1e-3 relative."""
+    nx, nv, k, nsteps = 32, 512, 0.3, 1000
+    p, f0, g, e, gst, st = _run_both(nx, nv, nsteps, amp=1e-4, store=True)
+    t = 0.1 * np.arange(1, nsteps + 1)
+    a_gpu = vo.mode_amplitude(gst["fields"]["e"].cpu().numpy())
+    a_ref = vo.mode_amplitude(st["fields"]["e"])
+    r_gpu, w_gpu = vo.envelope_fit(t, a_gpu, t_min=5.0)
+    r_ref, w_ref = vo.envelope_fit(t, a_ref, t_min=5.0)
+    assert abs(r_gpu - r_ref) <= 0.01 * abs(r_ref)
+    assert abs(w_gpu - w_ref) <= 0.01 * abs(w_ref)
+    root = vo.epw_root(k)
+    assert abs(r_ref - root.imag) <= 0.02 * abs(root.imag)
+    e2_gpu = gst["series"]["mean_e2"].cpu().numpy()
+    e2_ref = st["series"]["mean_e2"]
+    assert np.linalg.norm(e2_gpu - e2_ref) / np.linalg.norm(e2_ref) <= 1e-3

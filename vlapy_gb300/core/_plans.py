@@ -46,11 +46,38 @@ def plan_for(stuff: dict, all_params=None, collision=None, integrator=None) -> P
     kv = np.asarray(stuff.get("kv", np.fft.fftfreq(nv, d=dv) * 2.0 * np.pi), dtype=np.float64)
     inv = np.asarray(stuff.get("one_over_kx", np.zeros(nx)), dtype=np.float64)
     dx = float(x[1] - x[0]) if nx > 1 else 0.0
+    f_bg = None
+    if precision == "fp32-deltaf":
+        # the fixed background of the delta-f state: the x-average of the initial f
+        f_bg = background_of(stuff["f"])
     p = Plan(nx, nv, x, v, kx, kv, inv, dx, dv, dt=float(stuff.get("dt", 0.0)),
              nu=float(stuff.get("nu", 0.0)), collision=collision, integrator=integrator,
-             pulses=pulses, precision=precision)
+             pulses=pulses, precision=precision, f_background=f_bg)
     cache[key] = p
     return p
+
+
+def background_of(f) -> np.ndarray:
+    """x-average of a distribution function (host float64)."""
+    if isinstance(f, torch.Tensor):
+        f = f.detach().cpu().numpy()
+    return np.asarray(f, dtype=np.float64).mean(axis=0)
+
+
+def to_deviation(plan, f):
+    """FP32 deviation g = f - f0 of a plan in the delta-f mode (CUDA tensor)."""
+    f0 = torch.as_tensor(plan._fbg, device="cuda")
+    return (as_device(f) - f0[None, :]).to(torch.float32).contiguous()
+
+
+def from_deviation(plan, g, out=None):
+    """f = g + f0 as float64 (into out if given)."""
+    f0 = torch.as_tensor(plan._fbg, device="cuda")
+    f = g.to(torch.float64) + f0[None, :]
+    if out is not None:
+        out.copy_(f)
+        return out
+    return f
 
 
 def aux_plan(nx: int, nv: int, dv: float, one_over_kx=None) -> Plan:

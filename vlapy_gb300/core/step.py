@@ -16,7 +16,7 @@ import torch
 from ..field_driver import PulseDriver
 from ..plan import history_struct
 from . import collisions, field, vlasov, vlasov_poisson
-from ._plans import as_device, plan_for
+from ._plans import as_device, from_deviation, plan_for, to_deviation
 
 
 def get_vlasov_poisson_step(all_params, stuff_for_time_loop):
@@ -100,8 +100,15 @@ def get_timestep(all_params, stuff_for_time_loop):
             _device_batches(temp_storage)
             f, e = temp_storage["f"], temp_storage["e"]
             hist = history_struct(temp_storage, plan.nx, n_modes)
-            plan.run_steps(f, e, hist, temp_storage["time_batch"], temp_storage["driver_array_batch"],
-                           i, 1, use_graph=False)
+            if plan.precision == "fp32-deltaf":
+                # the delta-f state lives in FP32; f is refreshed from it after the step
+                g = to_deviation(plan, f)
+                plan.run_steps(g, e, hist, temp_storage["time_batch"], temp_storage["driver_array_batch"],
+                               i, 1, use_graph=False)
+                from_deviation(plan, g, out=f)
+            else:
+                plan.run_steps(f, e, hist, temp_storage["time_batch"], temp_storage["driver_array_batch"],
+                               i, 1, use_graph=False)
             return temp_storage, i
 
         timestep.plan = plan

@@ -112,7 +112,7 @@ cudaError_t edfdv_n(const vg_plan& p, double* f, const double* e, double dt, cud
   const int pairs = (p.nx + 1) / 2;
   const int blocks = div_up(pairs, P);
   const size_t smem = (size_t)P * N * sizeof(cx<double>);
-  cudaError_t err = cudaFuncSetAttribute(k_edfdv_f64<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t err = ensure_smem((const void*)k_edfdv_f64<N>, smem);
   if (err != cudaSuccess) return err;
   k_edfdv_f64<N><<<blocks, P * G, smem, s>>>(f, p.nx, e, p.kv, dt, p.tw64);
   return cudaGetLastError();
@@ -125,7 +125,7 @@ cudaError_t vdfdx_n(const vg_plan& p, double* f, double dt, cudaStream_t s) {
   if (2 * S > p.nv) S = p.nv / 2;
   const int W = 2 * S;
   const size_t smem = (size_t)S * (NX + COL_PAD) * sizeof(cx<double>);
-  cudaError_t err = cudaFuncSetAttribute(k_vdfdx_f64<NX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t err = ensure_smem((const void*)k_vdfdx_f64<NX>, smem);
   if (err != cudaSuccess) return err;
   k_vdfdx_f64<NX><<<div_up(p.nv, W), S * G, smem, s>>>(f, p.nv, W, p.kx, p.v, dt, p.tw64);
   return cudaGetLastError();

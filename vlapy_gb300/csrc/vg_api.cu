@@ -22,6 +22,20 @@ int cuda_status(cudaError_t err, const char* what) {
   return VG_ERR_CUDA;
 }
 
+cudaError_t ensure_smem(const void* kernel, size_t bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<const void*, int>, size_t> done;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lk(mu);
+  const auto key = std::make_pair(kernel, dev);
+  auto it = done.find(key);
+  if (it != done.end() && it->second >= bytes) return cudaSuccess;
+  cudaError_t err = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (err == cudaSuccess) done[key] = bytes;
+  return err;
+}
+
 // NumPy pairwise-sum tree (numpy/_core/src/umath/loops_utils.h.src,
 // pairwise_sum): blocks of <= 128 terms summed with 8 accumulators, larger
 // ranges split at n/2 rounded down to a multiple of 8.
@@ -65,9 +79,13 @@ struct GraphCache {
 };
 
 // Kernel kinds of the step sequence, for vg_profile_*.
-enum ProfKind { PK_EDFDV = 0, PK_VDFDX, PK_DENSITY, PK_POISSON, PK_FP_MOMENTS, PK_FP_SOLVE, PK_STORAGE, PK_COUNT };
-static const char* kProfNames[PK_COUNT] = {"edfdv", "vdfdx", "density", "poisson",
-                                            "fp_moments", "fp_solve", "storage"};
+enum ProfKind {
+  PK_EDFDV = 0, PK_VDFDX, PK_DENSITY, PK_POISSON, PK_FP_MOMENTS, PK_FP_SOLVE, PK_STORAGE,
+  PK_X_DRIFT32, PK_FIELD32, PK_ROW32, PK_KICK32, PK_STORE32, PK_COUNT
+};
+static const char* kProfNames[PK_COUNT] = {"edfdv", "vdfdx", "density", "poisson", "fp_moments", "fp_solve",
+                                            "storage", "x_drift_f32", "field_f32", "row_pass_f32", "kick_f32",
+                                            "store_f32"};
 
 struct ProfState {
   bool enabled = false;
@@ -101,6 +119,10 @@ static double prof_bytes(const vg_plan* p, int kind) {
     case PK_DENSITY:
     case PK_FP_MOMENTS:
     case PK_STORAGE: return es * cells;
+    case PK_X_DRIFT32:
+    case PK_ROW32:
+    case PK_KICK32: return 2.0 * 4.0 * cells;
+    case PK_STORE32: return 8.0 * 8.0 * p->nx;
     default: return 3.0 * 8.0 * p->nx;
   }
 }
@@ -139,6 +161,13 @@ void free_plan(vg_plan* p) {
     delete gc;
   }
   delete static_cast<ProfState*>(p->prof);
+  if (p->f32) {
+    F32Plan* q = p->f32;
+    void* qp[] = {q->F0, q->v32, q->f0_32, q->S, q->Mv, q->D, q->dpart, q->mpart};
+    for (void* x : qp)
+      if (x) cudaFree(x);
+    delete q;
+  }
   delete p;
 }
 
@@ -152,14 +181,6 @@ int require_plan(const vg_plan* p) {
   if (!p) {
     set_error("null plan");
     return VG_ERR_ARG;
-  }
-  return VG_OK;
-}
-
-int require_f64(const vg_plan* p) {
-  if (p->precision != VG_F64) {
-    set_error("operation not available in this precision mode");
-    return VG_ERR_UNSUPPORTED;
   }
   return VG_OK;
 }
@@ -308,6 +329,204 @@ int step_sequence_f64(vg_plan* p, double* f, double* e, const vg_history* h, con
   return VG_OK;
 }
 
+// forward FFT (sign -1) of a power-of-two length, host double precision
+void host_fft(std::vector<double>& re, std::vector<double>& im) {
+  const size_t n = re.size();
+  for (size_t i = 1, j = 0; i < n; ++i) {
+    size_t bit = n >> 1;
+    for (; j & bit; bit >>= 1) j ^= bit;
+    j ^= bit;
+    if (i < j) {
+      std::swap(re[i], re[j]);
+      std::swap(im[i], im[j]);
+    }
+  }
+  for (size_t len = 2; len <= n; len <<= 1) {
+    const double ang = -2.0 * M_PI / (double)len;
+    for (size_t i = 0; i < n; i += len) {
+      for (size_t k = 0; k < len / 2; ++k) {
+        const double c = std::cos(ang * k), sn = std::sin(ang * k);
+        const double ur = re[i + k], ui = im[i + k];
+        const double vr = re[i + k + len / 2] * c - im[i + k + len / 2] * sn;
+        const double vi = re[i + k + len / 2] * sn + im[i + k + len / 2] * c;
+        re[i + k] = ur + vr;
+        im[i + k] = ui + vi;
+        re[i + k + len / 2] = ur - vr;
+        im[i + k + len / 2] = ui - vi;
+      }
+    }
+  }
+}
+
+template <typename T>
+int upload(T** dst, const std::vector<T>& src, const char* what) {
+  return dev_copy(dst, src.data(), src.size(), what);
+}
+
+// Constants of the delta-f path: the background f0 in FP32, its collision
+// stencils and spectrum, and its moments in FP64.
+int setup_f32(vg_plan* p, const vg_run_desc* d) {
+  if (!p->nv_pow2 || !p->nx_pow2 || p->nv > 16384 || p->nx > 8192) {
+    set_error("the FP32 delta-f mode needs power-of-two nx <= 8192 and nv <= 16384");
+    return VG_ERR_UNSUPPORTED;
+  }
+  F32Plan* q = new F32Plan();
+  std::memset(q, 0, sizeof(F32Plan));
+  p->f32 = q;
+  const int nv = d->nv, nx = d->nx;
+  const double dv = d->dv, dv2 = d->dv_sq;
+  const double* f0 = d->f_background;
+  const double* v = d->v;
+  std::vector<float> v32(nv), f32v(nv), S(nv), Mv(nv), D(nv);
+  double mom[7] = {0, 0, 0, 0, 0, 0, 0};
+  for (int j = 0; j < nv; ++j) {
+    const double fm = j > 0 ? f0[j - 1] : 0.0, fp = j < nv - 1 ? f0[j + 1] : 0.0;
+    const double vm = j > 0 ? v[j - 1] : 0.0, vp = j < nv - 1 ? v[j + 1] : 0.0;
+    S[j] = (float)((fm - 2.0 * f0[j] + fp) / dv2);
+    Mv[j] = (float)((vm * fm - vp * fp) / (2.0 * dv));
+    D[j] = (float)((fm - fp) / (2.0 * dv));
+    v32[j] = (float)v[j];
+    f32v[j] = (float)f0[j];
+    const double w = (j == 0 || j == nv - 1) ? 0.5 : 1.0;
+    double vp_ = 1.0;
+    for (int k = 0; k < 6; ++k) {
+      mom[k] += w * f0[j] * vp_;
+      vp_ *= v[j];
+    }
+    mom[6] += w * f0[j] * f0[j];
+  }
+  for (int k = 0; k < 7; ++k) mom[k] *= dv;
+  std::vector<double> re(f0, f0 + nv), im(nv, 0.0);
+  host_fft(re, im);
+  std::vector<cx<float>> F0(nv / 2 + 1);
+  for (int k = 0; k <= nv / 2; ++k) F0[k] = {(float)re[k], (float)im[k]};
+  VG_CHECK(upload(&q->v32, v32, "f32 constants"));
+  VG_CHECK(upload(&q->f0_32, f32v, "f32 constants"));
+  VG_CHECK(upload(&q->S, S, "f32 constants"));
+  VG_CHECK(upload(&q->Mv, Mv, "f32 constants"));
+  VG_CHECK(upload(&q->D, D, "f32 constants"));
+  VG_CHECK(upload(&q->F0, F0, "f32 constants"));
+  q->dkx = nx > 1 ? d->kx[1] : 0.0;
+  q->dkv = d->kv[1];
+  q->c0 = mom[0] - 1.0;
+  q->rc.v = q->v32;
+  q->rc.f0 = q->f0_32;
+  q->rc.S = q->S;
+  q->rc.Mv = q->Mv;
+  q->rc.D = q->D;
+  q->rc.dv = dv;
+  q->rc.dv_sq = dv2;
+  q->rc.dkv = q->dkv;
+  for (int k = 0; k < 7; ++k) q->rc.f0m[k] = mom[k];
+  int dev = 0, nsm = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  q->n_sm = nsm;
+  q->col_grid_max = 8 * nsm;
+  q->row_grid_max = 8 * nsm;
+  VG_CHECK(dev_copy<float2>(&q->dpart, nullptr, (size_t)q->col_grid_max * nx, "density partials"));
+  VG_CHECK(dev_copy<cx<float>>(&q->mpart, nullptr, (size_t)q->row_grid_max * F32_MAX_MODES * nv, "mode partials"));
+  return VG_OK;
+}
+
+int modes_of(const vg_history* h) {
+  return (h && h->stored_f && !h->store_all) ? h->n_modes : 0;
+}
+
+// The FP32 delta-f launch sequence of nsteps steps.  For leapfrog the second
+// half kick of step n and the first of step n+1 use the same field and run in
+// the same row pass, around the collision step and the storage moments.
+int step_sequence_f32(vg_plan* p, float* g, double* e, const vg_history* h, const double* tb, const double* db,
+                      int i0, int nsteps, cudaStream_t s) {
+  const double dt = p->dt;
+  const int nm = modes_of(h);
+  auto X = [&](double d) {
+    return cuda_status(prof_run(p, PK_X_DRIFT32, s, [&] { return launch_col_f32(*p, g, d, s); }), "x drift");
+  };
+  auto K = [&](double d) {
+    return cuda_status(prof_run(p, PK_KICK32, s, [&] { return launch_row_f32(*p, g, e, d, 0.0, 0, 0, 0, s); }),
+                       "kick");
+  };
+  FieldTime ft;
+  ft.t_host = 0.0;
+  ft.use_pulses = p->n_pulses > 0;
+  auto F = [&](int i, std::initializer_list<double> adds) {
+    ft.t_ptr = tb + i;
+    ft.nadd = 0;
+    for (double a : adds) ft.add[ft.nadd++] = a;
+    return cuda_status(prof_run(p, PK_FIELD32, s, [&] { return launch_field_f32(*p, nullptr, ft, e, s); }),
+                       "field");
+  };
+  auto STORE = [&](int i) -> int {
+    if (!h) return VG_OK;
+    const double* de = db ? db + (size_t)i * p->nx : nullptr;
+    return cuda_status(prof_run(p, PK_STORE32, s, [&] { return launch_store_f32(*p, g, e, de, *h, i, nm, s); }),
+                       "store");
+  };
+  if (p->integrator == VG_LEAPFROG) {
+    VG_CHECK(K(0.5 * dt));
+    for (int k = 0; k < nsteps; ++k) {
+      const int i = i0 + k;
+      VG_CHECK(X(dt));
+      VG_CHECK(F(i, {dt}));
+      const double trail = (k + 1 < nsteps) ? 0.5 * dt : 0.0;
+      VG_CHECK(cuda_status(prof_run(p, PK_ROW32, s, [&] {
+                             return launch_row_f32(*p, g, e, 0.5 * dt, trail, 1, h != nullptr, nm, s);
+                           }),
+                           "row pass"));
+      VG_CHECK(STORE(i));
+    }
+    return VG_OK;
+  }
+  for (int k = 0; k < nsteps; ++k) {
+    const int i = i0 + k;
+    if (p->integrator == VG_PEFRL) {
+      const double xsi = 0.1786178958448091, lambd = -0.2123418310626054, chi = -0.6626458266981849e-1;
+      const double d1 = xsi * dt, d2 = chi * dt, d3 = (1.0 - 2.0 * (chi + xsi)) * dt, d4 = d2, d5 = d1;
+      const double k1 = 0.5 * (1.0 - 2.0 * lambd) * dt, k2 = lambd * dt, k3 = k2, k4 = k1;
+      VG_CHECK(X(d1));
+      VG_CHECK(F(i, {d1}));
+      VG_CHECK(K(k1));
+      VG_CHECK(X(d2));
+      VG_CHECK(F(i, {d1, d2}));
+      VG_CHECK(K(k2));
+      VG_CHECK(X(d3));
+      VG_CHECK(F(i, {d1, d2, d3}));
+      VG_CHECK(K(k3));
+      VG_CHECK(X(d4));
+      VG_CHECK(F(i, {d1, d2, d3, d4}));
+      VG_CHECK(K(k4));
+      VG_CHECK(X(d5));
+      VG_CHECK(F(i, {d1, d2, d3, d4, d5}));
+    } else {
+      const double a1 = 0.168735950563437422448196, a2 = 0.377851589220928303880766,
+                   a3 = -0.093175079568731452657924, b1 = 0.049086460976116245491441,
+                   b2 = 0.264177609888976700200146, b3 = 0.186735929134907054308413,
+                   c1 = -0.000069728715055305084099, c2 = -0.000625704827430047189169,
+                   c3 = -0.002213085124045325561636, d2c = -2.916600457689847816445691e-6,
+                   d3c = 3.048480261700038788680723e-5, e3 = 4.985549387875068121593988e-7;
+      const double D1 = b1 + 2.0 * c1 * std::pow(dt, 2.0);
+      const double D2 = b2 + 2.0 * c2 * std::pow(dt, 2.0) + 4.0 * d2c * std::pow(dt, 4.0);
+      const double D3 = b3 + 2.0 * c3 * std::pow(dt, 2.0) + 4.0 * d3c * std::pow(dt, 4.0) -
+                        8.0 * e3 * std::pow(dt, 6.0);
+      const double xs[5] = {a1, a2, a3, a2, a1};
+      const double ks[5] = {D2, D3, D3, D2, D1};
+      VG_CHECK(K(D1 * dt));
+      for (int q = 0; q < 5; ++q) {
+        VG_CHECK(X(xs[q] * dt));
+        VG_CHECK(F(i, {xs[q] * dt}));
+        VG_CHECK(K(ks[q] * dt));
+      }
+    }
+    VG_CHECK(cuda_status(prof_run(p, PK_ROW32, s, [&] {
+                           return launch_row_f32(*p, g, e, 0.0, 0.0, 1, h != nullptr, nm, s);
+                         }),
+                         "row pass"));
+    VG_CHECK(STORE(i));
+  }
+  return VG_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -392,6 +611,7 @@ int vg_plan_create(const vg_run_desc* d, vg_plan** out) {
   TRY(dev_copy<double>(&p->etmp, nullptr, 4 * nx + 4, "scratch"));
   if (d->precision == VG_F64 && d->collision != VG_COLL_NONE)
     TRY(dev_copy<double>(&p->bb, nullptr, nx * nv, "thomas scratch"));
+  if (d->precision == VG_F32_DELTA_F) TRY(setup_f32(p, d));
   TRY(cuda_status(launch_twiddles(*p, 0), "twiddles"));
   TRY(cuda_status(cudaDeviceSynchronize(), "plan setup"));
   p->graph_cache = new GraphCache();
@@ -410,33 +630,37 @@ int vg_plan_destroy(vg_plan* p) {
 
 int vg_edfdv(vg_plan* p, void* f, const double* e, double dt, vg_stream stream) {
   VG_CHECK(require_plan(p));
-  VG_CHECK(require_f64(p));
-  VG_CHECK(require_fft_v(p));
   if (!f || !e) {
     set_error("null f or e");
     return VG_ERR_ARG;
   }
+  if (p->f32)
+    return cuda_status(launch_row_f32(*p, static_cast<float*>(f), e, dt, 0.0, 0, 0, 0, (cudaStream_t)stream),
+                       "edfdv");
+  VG_CHECK(require_fft_v(p));
   return cuda_status(launch_edfdv_f64(*p, static_cast<double*>(f), e, dt, (cudaStream_t)stream), "edfdv");
 }
 
 int vg_vdfdx(vg_plan* p, void* f, double dt, vg_stream stream) {
   VG_CHECK(require_plan(p));
-  VG_CHECK(require_f64(p));
-  VG_CHECK(require_fft_x(p));
   if (!f) {
     set_error("null f");
     return VG_ERR_ARG;
   }
+  if (p->f32) return cuda_status(launch_col_f32(*p, static_cast<float*>(f), dt, (cudaStream_t)stream), "vdfdx");
+  VG_CHECK(require_fft_x(p));
   return cuda_status(launch_vdfdx_f64(*p, static_cast<double*>(f), dt, (cudaStream_t)stream), "vdfdx");
 }
 
 int vg_charge_density(vg_plan* p, const void* f, double* n, vg_stream stream) {
   VG_CHECK(require_plan(p));
-  VG_CHECK(require_f64(p));
   if (!f || !n) {
     set_error("null f or n");
     return VG_ERR_ARG;
   }
+  if (p->f32)
+    return cuda_status(launch_dens_rows_f32(*p, static_cast<const float*>(f), n, 1, (cudaStream_t)stream),
+                       "charge density");
   MomSpec spec;
   spec.nm = 1;
   spec.kind[0] = MOM_ONE;
@@ -458,22 +682,30 @@ int vg_poisson(vg_plan* p, const double* rho, double* e, vg_stream stream) {
 
 int vg_field_solve(vg_plan* p, const void* f, const double* driver, double* e, vg_stream stream) {
   VG_CHECK(require_plan(p));
-  VG_CHECK(require_f64(p));
   if (!f || !e) {
     set_error("null f or e");
     return VG_ERR_ARG;
   }
   FieldTime ft{};
   ft.use_pulses = 0;
+  if (p->f32) {
+    cudaStream_t s = (cudaStream_t)stream;
+    VG_CHECK(cuda_status(launch_dens_rows_f32(*p, static_cast<const float*>(f), p->rho, 0, s), "density"));
+    return cuda_status(launch_poisson_only_f32(*p, p->rho, driver, ft, e, s), "poisson");
+  }
   return field_f64(p, static_cast<const double*>(f), driver, ft, e, (cudaStream_t)stream);
 }
 
 int vg_collision_step(vg_plan* p, void* f, vg_stream stream) {
   VG_CHECK(require_plan(p));
-  VG_CHECK(require_f64(p));
   if (!f) {
     set_error("null f");
     return VG_ERR_ARG;
+  }
+  if (p->f32) {
+    if (p->collision == VG_COLL_NONE) return VG_OK;
+    return cuda_status(launch_row_f32(*p, static_cast<float*>(f), nullptr, 0.0, 0.0, 1, 0, 0, (cudaStream_t)stream),
+                       "collision step");
   }
   return collision_f64(p, static_cast<double*>(f), (cudaStream_t)stream);
 }
@@ -497,12 +729,18 @@ static int check_history(const vg_plan* p, const vg_history* h, int i_last) {
 int vg_storage_step(vg_plan* p, const void* f, const double* e, const double* de, const vg_history* h,
                     int32_t i, vg_stream stream) {
   VG_CHECK(require_plan(p));
-  VG_CHECK(require_f64(p));
   if (!f || !e || !h || i < 0) {
     set_error("null f, e or history, or negative index");
     return VG_ERR_ARG;
   }
   VG_CHECK(check_history(p, h, i));
+  if (p->f32) {
+    cudaStream_t s = (cudaStream_t)stream;
+    const int nm = modes_of(h);
+    float* g = const_cast<float*>(static_cast<const float*>(f));
+    VG_CHECK(cuda_status(launch_row_f32(*p, g, e, 0.0, 0.0, 0, 1, nm, s), "storage moments"));
+    return cuda_status(launch_store_f32(*p, g, e, de, *h, i, nm, s), "storage step");
+  }
   return cuda_status(launch_storage_f64(*p, static_cast<const double*>(f), e, de, *h, i, (cudaStream_t)stream),
                      "storage step");
 }
@@ -524,19 +762,28 @@ int vg_driver(vg_plan* p, double t, double* out, vg_stream stream) {
 int vg_run_steps(vg_plan* p, void* f, double* e, const vg_history* h, const double* time_batch,
                  const double* driver_batch, int32_t i0, int32_t nsteps, int32_t use_graph, vg_stream stream) {
   VG_CHECK(require_plan(p));
-  VG_CHECK(require_f64(p));
-  VG_CHECK(require_fft_v(p));
-  VG_CHECK(require_fft_x(p));
+  if (!p->f32) {
+    VG_CHECK(require_fft_v(p));
+    VG_CHECK(require_fft_x(p));
+  }
   if (!f || !e || !time_batch || i0 < 0 || nsteps < 0) {
     set_error("null f, e or time_batch, or negative step range");
     return VG_ERR_ARG;
   }
   if (nsteps == 0) return VG_OK;
   VG_CHECK(check_history(p, h, i0 + nsteps - 1));
+  if (p->f32 && modes_of(h) > F32_MAX_MODES) {
+    set_error("the FP32 delta-f mode stores at most 4 x-Fourier modes per step");
+    return VG_ERR_UNSUPPORTED;
+  }
   cudaStream_t s = (cudaStream_t)stream;
   double* fd = static_cast<double*>(f);
   if (static_cast<ProfState*>(p->prof)->enabled) use_graph = 0;
-  if (!use_graph) return step_sequence_f64(p, fd, e, h, time_batch, driver_batch, i0, nsteps, s);
+  auto seq = [&]() {
+    return p->f32 ? step_sequence_f32(p, static_cast<float*>(f), e, h, time_batch, driver_batch, i0, nsteps, s)
+                  : step_sequence_f64(p, fd, e, h, time_batch, driver_batch, i0, nsteps, s);
+  };
+  if (!use_graph) return seq();
   auto* gc = static_cast<GraphCache*>(p->graph_cache);
   GraphKey key;
   std::memset(&key, 0, sizeof(key));
@@ -555,7 +802,7 @@ int vg_run_steps(vg_plan* p, void* f, double* e, const vg_history* h, const doub
       return VG_ERR_ARG;
     }
     VG_CHECK(cuda_status(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed), "begin capture"));
-    int st = step_sequence_f64(p, fd, e, h, time_batch, driver_batch, i0, nsteps, s);
+    int st = seq();
     cudaGraph_t graph = nullptr;
     cudaError_t cerr = cudaStreamEndCapture(s, &graph);
     if (st != VG_OK) {

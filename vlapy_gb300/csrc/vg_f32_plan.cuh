@@ -1,0 +1,68 @@
+// Plan state and launch shapes of the FP32 delta-f path.
+#pragma once
+
+#include "vg_common.cuh"
+
+namespace vg {
+
+// Per-run constants of the delta-f row pass (all device pointers, FP32 copies
+// of FP64 host values; the moments of f0 stay FP64).
+struct RowConsts {
+  const float* v;   // [nv]
+  const float* f0;  // [nv] background
+  const float* S;   // [nv] (f0[j-1] - 2 f0[j] + f0[j+1]) / dv^2, truncated at the ends
+  const float* Mv;  // [nv] (v[j-1] f0[j-1] - v[j+1] f0[j+1]) / (2 dv)
+  const float* D;   // [nv] (f0[j-1] - f0[j+1]) / (2 dv)
+  double dv, dv_sq, dkv;
+  double f0m[7];    // trapz(f0 v^p), p = 0..5, and trapz(f0^2)
+};
+
+struct RowArgs {
+  float* g;
+  int nx;
+  const double* e;
+  double dt1, dt2;  // leading / trailing half-kick steps (0: skip)
+  int fp, dougherty;
+  double nudt;
+  int want_mom;     // storage moments + x modes of the post-collision state
+  double* mom;      // [nx][8]
+  int n_modes;
+  cx<float>* mpart; // [grid][n_modes][nv] per-CTA partial x modes
+  const cx<float>* F0;  // [nv/2+1] unnormalised FFT_v(f0)
+  const cx<float>* tw;
+  RowConsts rc;
+};
+
+struct F32Plan {
+  double dkx, dkv, c0;  // kx[1], kv[1], trapz(f0) - 1
+  cx<float>* F0;
+  float* v32;
+  float* f0_32;
+  float* S;
+  float* Mv;
+  float* D;
+  RowConsts rc;
+  float2* dpart;       // [max col grid][nx] density partials (hi, lo)
+  int npart;
+  cx<float>* mpart;    // [max row grid][4][nv]
+  int mgrid;
+  int col_grid_max, row_grid_max, col_grid, row_grid;
+  int n_sm;
+};
+
+// launch shapes (shared by kernels' __launch_bounds__ and the launchers)
+__host__ __device__ constexpr int col32_radix(int nx) { return nx <= 8 ? nx : (nx <= 2048 ? 8 : 16); }
+__host__ __device__ constexpr int col32_seqs(int nx, int r) {
+  return ((nx / r) * ((256 / (nx / r)) > 4 ? (256 / (nx / r)) : 4) <= 1024)
+             ? ((256 / (nx / r)) > 4 ? (256 / (nx / r)) : 4)
+             : (1024 / (nx / r) > 1 ? 1024 / (nx / r) : 1);
+}
+__host__ __device__ constexpr int row32_radix(int n) { return n <= 8 ? n : (n <= 4096 ? 8 : 16); }
+__host__ __device__ constexpr int row32_block(int n, int r) { return (n / r) >= 256 ? (n / r) : 256; }
+__host__ __device__ constexpr size_t row32_group_bytes(int n, int r) {
+  return (size_t)n * 8 + (size_t)8 * (n / r) * 4 + (size_t)((n / r) / 32 + 1) * 9 * 8;
+}
+
+constexpr int F32_MAX_MODES = 4;
+
+}  // namespace vg

@@ -91,10 +91,9 @@ __device__ __forceinline__ cx<T> twiddle(const cx<T>* __restrict__ tw, int q, bo
   return w;
 }
 
-template <typename T, int N, bool INV, int NS>
+template <typename T, int N, int R, bool INV, int NS>
 struct StockhamPass {
   static __device__ __forceinline__ void run(cx<T>* s, int t, const cx<T>* __restrict__ tw) {
-    constexpr int R = fft_radix<T>(N);
     constexpr int r = (N / NS < R) ? (N / NS) : R;
     constexpr int NB = N / r;      // butterflies in this pass
     constexpr int G = N / R;       // threads per sequence
@@ -123,20 +122,20 @@ struct StockhamPass {
       for (int m = 0; m < r; ++m) s[base + m * NS] = a[b][m];
     }
     __syncthreads();
-    StockhamPass<T, N, INV, NS * r>::run(s, t, tw);
+    StockhamPass<T, N, R, INV, NS * r>::run(s, t, tw);
   }
 };
-template <typename T, int N, bool INV>
-struct StockhamPass<T, N, INV, N> {
+template <typename T, int N, int R, bool INV>
+struct StockhamPass<T, N, R, INV, N> {
   static __device__ __forceinline__ void run(cx<T>*, int, const cx<T>* __restrict__) {}
 };
 
-// In-place unnormalised transform of s[0..N) by the N/R threads t = 0..N/R-1.
-// Caller must have synchronised after writing s; the result is visible to
-// the whole CTA on return.
-template <typename T, int N, bool INV>
+// In-place unnormalised transform of s[0..N) by the N/R threads t = 0..N/R-1
+// (R defaults to fft_radix<T>(N)).  Caller must have synchronised after
+// writing s; the result is visible to the whole CTA on return.
+template <typename T, int N, bool INV, int R = fft_radix<T>(N)>
 __device__ __forceinline__ void block_fft(cx<T>* s, int t, const cx<T>* __restrict__ tw) {
-  StockhamPass<T, N, INV, 1>::run(s, t, tw);
+  StockhamPass<T, N, (R < N ? R : N), INV, 1>::run(s, t, tw);
 }
 
 // Two real sequences a, b packed as z = a + i b; s holds Z = FFT(z).  Replace

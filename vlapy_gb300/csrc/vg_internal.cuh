@@ -4,6 +4,7 @@
 #include <string>
 
 #include "vg_common.cuh"
+#include "vg_f32_plan.cuh"
 #include "vg_fft.cuh"
 #include "vlagpu.h"
 
@@ -35,6 +36,8 @@ struct vg_plan {
   // graph cache and per-kernel profiling state
   void* graph_cache;
   void* prof;
+  // FP32 delta-f state (null in FP64 mode)
+  vg::F32Plan* f32;
 };
 
 namespace vg {
@@ -51,6 +54,9 @@ struct MomSpec {
 
 void set_error(const std::string& msg);
 int cuda_status(cudaError_t err, const char* what);
+// raise a kernel's dynamic shared-memory limit once (not a stream operation,
+// so it is legal while a stream is being captured)
+cudaError_t ensure_smem(const void* kernel, size_t bytes);
 
 // launchers (return cudaError_t of the launch)
 cudaError_t launch_edfdv_f64(const vg_plan& p, double* f, const double* e, double dt, cudaStream_t s);
@@ -73,5 +79,18 @@ cudaError_t launch_storage_f64(const vg_plan& p, const double* f, const double* 
                                const vg_history& h, int i, cudaStream_t s);
 cudaError_t launch_driver(const vg_plan& p, const FieldTime& ft, double* out, cudaStream_t s);
 cudaError_t launch_twiddles(vg_plan& p, cudaStream_t s);
+
+// FP32 delta-f path (vg_step_f32.cu)
+cudaError_t launch_col_f32(const vg_plan& p, float* g, double dt, cudaStream_t s);
+cudaError_t launch_field_f32(const vg_plan& p, const double* driver, const FieldTime& ft, double* e,
+                             cudaStream_t s);
+cudaError_t launch_dens_rows_f32(const vg_plan& p, const float* g, double* rho_out, int as_density,
+                                 cudaStream_t s);
+cudaError_t launch_poisson_only_f32(const vg_plan& p, const double* rho, const double* driver,
+                                    const FieldTime& ft, double* e, cudaStream_t s);
+cudaError_t launch_row_f32(const vg_plan& p, float* g, const double* e, double dt1, double dt2, int fp, int mom,
+                           int n_modes, cudaStream_t s);
+cudaError_t launch_store_f32(const vg_plan& p, const float* g, const double* e, const double* de,
+                             const vg_history& h, int i, int n_modes, cudaStream_t s);
 
 }  // namespace vg

@@ -123,7 +123,7 @@ __global__ void k_row_moments_f64(const double* __restrict__ f, int nv, const do
 cudaError_t launch_row_moments_f64(const vg_plan& p, const double* f, const MomSpec& spec,
                                    double* out, int out_stride, cudaStream_t s) {
   const size_t smem = ((size_t)p.nv + (size_t)spec.nm * p.pw_v_leaves) * sizeof(double);
-  cudaError_t err = cudaFuncSetAttribute(k_row_moments_f64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t err = ensure_smem((const void*)k_row_moments_f64, smem);
   if (err != cudaSuccess) return err;
   k_row_moments_f64<<<p.nx, 256, smem, s>>>(f, p.nv, p.v, p.v_pow, spec, p.pw_v, p.dv, out, out_stride);
   return cudaGetLastError();
@@ -274,7 +274,7 @@ cudaError_t poisson_n(const vg_plan& p, const double* dens, int is_density, cons
                       const FieldTime& ft, double* e, cudaStream_t s) {
   constexpr int G = fft_threads<double>(NX);
   const size_t smem = (size_t)NX * sizeof(cx<double>);
-  cudaError_t err = cudaFuncSetAttribute(k_poisson_fft_f64<NX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t err = ensure_smem((const void*)k_poisson_fft_f64<NX>, smem);
   if (err != cudaSuccess) return err;
   k_poisson_fft_f64<NX><<<1, G, smem, s>>>(dens, is_density, p.inv_kx, driver, ft.use_pulses, p.pulses,
                                            p.n_pulses, p.x, to_dev(ft), p.tw64, e);

@@ -26,7 +26,7 @@ __global__ void __launch_bounds__(row_block<double>(N)) k_edfdv_f64(double* __re
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int P = blockDim.x / G;
   const int g = threadIdx.x / G, t = threadIdx.x - g * G;
-  cx<double>* s = reinterpret_cast<cx<double>*>(smem_raw) + (size_t)g * N;
+  cx<double>* s = reinterpret_cast<cx<double>*>(smem_raw) + (size_t)g * sp_len<double>(N);
   const int pair = blockIdx.x * P + g;
   const int ra = 2 * pair, rb = ra + 1;
   const bool va = ra < nrows, vb = rb < nrows;
@@ -35,7 +35,7 @@ __global__ void __launch_bounds__(row_block<double>(N)) k_edfdv_f64(double* __re
 #pragma unroll
   for (int i = 0; i < R; ++i) {
     const int n = t + i * G;
-    s[n] = {va ? fa[n] : 0.0, vb ? fb[n] : 0.0};
+    s[sp<double>(n)] = {va ? fa[n] : 0.0, vb ? fb[n] : 0.0};
   }
   __syncthreads();
   block_fft<double, N, false>(s, t, tw);
@@ -52,7 +52,7 @@ __global__ void __launch_bounds__(row_block<double>(N)) k_edfdv_f64(double* __re
 #pragma unroll
   for (int i = 0; i < R; ++i) {
     const int n = t + i * G;
-    const cx<double> z = s[n];
+    const cx<double> z = s[sp<double>(n)];
     if (va) fa[n] = z.x * sc;
     if (vb) fb[n] = z.y * sc;
   }
@@ -68,7 +68,7 @@ __global__ void __launch_bounds__(col_seqs<double>(NX) * fft_threads<double>(NX)
                                                     const cx<double>* __restrict__ tw) {
   constexpr int R = fft_radix<double>(NX);
   constexpr int G = NX / R;
-  constexpr int LD = NX + COL_PAD;
+  constexpr int LD = sp_len<double>(NX) + COL_PAD;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cx<double>* s = reinterpret_cast<cx<double>*>(smem_raw);
   double* sd = reinterpret_cast<double*>(smem_raw);
@@ -78,7 +78,7 @@ __global__ void __launch_bounds__(col_seqs<double>(NX) * fft_threads<double>(NX)
     const int x = q / W, c = q - x * W;
     const int col = c0 + c;
     const double val = col < nv ? f[(size_t)x * nv + col] : 0.0;
-    sd[2 * ((c >> 1) * LD + x) + (c & 1)] = val;
+    sd[2 * ((c >> 1) * LD + sp<double>(x)) + (c & 1)] = val;
   }
   __syncthreads();
   const int g = threadIdx.x / G, t = threadIdx.x - g * G;
@@ -99,7 +99,7 @@ __global__ void __launch_bounds__(col_seqs<double>(NX) * fft_threads<double>(NX)
   for (int q = threadIdx.x; q < total; q += blockDim.x) {
     const int x = q / W, c = q - x * W;
     const int col = c0 + c;
-    if (col < nv) f[(size_t)x * nv + col] = sd[2 * ((c >> 1) * LD + x) + (c & 1)] * sc;
+    if (col < nv) f[(size_t)x * nv + col] = sd[2 * ((c >> 1) * LD + sp<double>(x)) + (c & 1)] * sc;
   }
 }
 
@@ -111,7 +111,7 @@ cudaError_t edfdv_n(const vg_plan& p, double* f, const double* e, double dt, cud
   const int P = row_block<double>(N) / G;
   const int pairs = (p.nx + 1) / 2;
   const int blocks = div_up(pairs, P);
-  const size_t smem = (size_t)P * N * sizeof(cx<double>);
+  const size_t smem = (size_t)P * sp_len<double>(N) * sizeof(cx<double>);
   cudaError_t err = ensure_smem((const void*)k_edfdv_f64<N>, smem);
   if (err != cudaSuccess) return err;
   k_edfdv_f64<N><<<blocks, P * G, smem, s>>>(f, p.nx, e, p.kv, dt, p.tw64);
@@ -124,7 +124,7 @@ cudaError_t vdfdx_n(const vg_plan& p, double* f, double dt, cudaStream_t s) {
   int S = col_seqs<double>(NX);
   if (2 * S > p.nv) S = p.nv / 2;
   const int W = 2 * S;
-  const size_t smem = (size_t)S * (NX + COL_PAD) * sizeof(cx<double>);
+  const size_t smem = (size_t)S * (sp_len<double>(NX) + COL_PAD) * sizeof(cx<double>);
   cudaError_t err = ensure_smem((const void*)k_vdfdx_f64<NX>, smem);
   if (err != cudaSuccess) return err;
   k_vdfdx_f64<NX><<<div_up(p.nv, W), S * G, smem, s>>>(f, p.nv, W, p.kx, p.v, dt, p.tw64);

@@ -113,15 +113,16 @@ __device__ __forceinline__ void group_df_sum(df32 (&v)[NQ], df32* red, int G, in
 
 // ---- tridiagonal solve: partition (interior Thomas) + PCR ---------------
 // Solves rows j = 0..N-1: l(j) x[j-1] + b x[j] + u(j) x[j+1] = x_in[j]
-// (l(0) and u(N-1) ignored).  x lives in shared memory with element stride
-// XS floats; thread t of G owns the contiguous chunk [t*m, t*m+m), m = N/G >= 2.
+// (l(0) and u(N-1) ignored).  x is one component of a padded complex-float
+// sequence in shared memory (element j at float offset 2*sp<float>(j)); thread
+// t of G owns the contiguous chunk [t*m, t*m+m), m = N/G >= 2.
 // red: shared scratch of 4 * 2G floats.  All threads of the CTA must call it.
 template <int M, typename LFn, typename UFn>
-__device__ __forceinline__ void partition_solve(float* x, int XS, int t, int G, float b, LFn lf, UFn uf,
+__device__ __forceinline__ void partition_solve(float* x, int t, int G, float b, LFn lf, UFn uf,
                                                 float* red) {
   const int s = t * M, e = s + M - 1;
   float y[M > 2 ? M - 2 : 1], al[M > 2 ? M - 2 : 1], be[M > 2 ? M - 2 : 1];
-  float r_s = x[s * XS], r_e = x[e * XS];
+  float r_s = x[2 * sp<float>(s)], r_e = x[2 * sp<float>(e)];
   float RA0, RB0, RC0, RD0, RA1, RB1, RC1, RD1;
   const float l_s = (s == 0) ? 0.f : lf(s);
   const float u_s = uf(s);
@@ -137,7 +138,7 @@ __device__ __forceinline__ void partition_solve(float* x, int XS, int t, int G, 
       const float den = (i == 0) ? b : b - lj * cp[i - 1];
       const float inv = 1.f / den;
       cp[i] = uj * inv;
-      const float rj = x[j * XS];
+      const float rj = x[2 * sp<float>(j)];
       y[i] = (i == 0) ? rj * inv : (rj - lj * y[i - 1]) * inv;
       al[i] = (i == 0) ? -lj * inv : (-lj * al[i - 1]) * inv;
       const float bsrc = (i == M - 3) ? -uj : 0.f;
@@ -220,11 +221,11 @@ __device__ __forceinline__ void partition_solve(float* x, int XS, int t, int G, 
   }
   const float xs = D[2 * t] / B[2 * t];
   const float xe = D[2 * t + 1] / B[2 * t + 1];
-  x[s * XS] = xs;
-  x[e * XS] = xe;
+  x[2 * sp<float>(s)] = xs;
+  x[2 * sp<float>(e)] = xe;
   if (M > 2) {
 #pragma unroll
-    for (int i = 0; i < M - 2; ++i) x[(s + 1 + i) * XS] = y[i] + al[i] * xs + be[i] * xe;
+    for (int i = 0; i < M - 2; ++i) x[2 * sp<float>(s + 1 + i)] = y[i] + al[i] * xs + be[i] * xe;
   }
   __syncthreads();
 }

@@ -51,16 +51,21 @@ struct F32Plan {
 };
 
 // launch shapes (shared by kernels' __launch_bounds__ and the launchers)
-__host__ __device__ constexpr int col32_radix(int nx) { return nx <= 8 ? nx : (nx <= 2048 ? 8 : 16); }
+// column tiles: radix 8 up to nx = 1024, radix 16 above; S column pairs per
+// CTA, at least 4 (32-byte row segments) but at most 512 threads, so that a
+// thread keeps up to 128 registers
+__host__ __device__ constexpr int col32_radix(int nx) { return nx <= 8 ? nx : (nx <= 1024 ? 8 : 16); }
+__host__ __device__ constexpr int col32_seqs_raw(int g) { return (256 / g) > 4 ? (256 / g) : 4; }
 __host__ __device__ constexpr int col32_seqs(int nx, int r) {
-  return ((nx / r) * ((256 / (nx / r)) > 4 ? (256 / (nx / r)) : 4) <= 1024)
-             ? ((256 / (nx / r)) > 4 ? (256 / (nx / r)) : 4)
-             : (1024 / (nx / r) > 1 ? 1024 / (nx / r) : 1);
+  return (nx / r) * col32_seqs_raw(nx / r) <= 512 ? col32_seqs_raw(nx / r)
+                                                   : (512 / (nx / r) > 1 ? 512 / (nx / r) : 1);
 }
 __host__ __device__ constexpr int row32_radix(int n) { return n <= 8 ? n : (n <= 4096 ? 8 : 16); }
 __host__ __device__ constexpr int row32_block(int n, int r) { return (n / r) >= 256 ? (n / r) : 256; }
+// per row-pair group: padded sequence (one pad per 16 complex floats), PCR
+// scratch of 4 x 2G floats, double-float reduction slots
 __host__ __device__ constexpr size_t row32_group_bytes(int n, int r) {
-  return (size_t)n * 8 + (size_t)8 * (n / r) * 4 + (size_t)((n / r) / 32 + 1) * 9 * 8;
+  return (size_t)(n + (n >> 4)) * 8 + 16 + (size_t)8 * (n / r) * 4 + (size_t)((n / r) / 32 + 1) * 9 * 8;
 }
 
 constexpr int F32_MAX_MODES = 4;

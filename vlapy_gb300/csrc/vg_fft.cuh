@@ -41,6 +41,17 @@ __host__ __device__ constexpr int col_seqs(int nx) {
        : (2 * fft_threads<T>(nx) <= 512 ? 2 : 1);
 }
 
+// Shared-memory layout of a sequence: one padding element after every 8
+// (complex double) or 16 (complex float) elements, so that the stride-r
+// Stockham writes and the contiguous per-thread chunks of the tridiagonal
+// solver fall in distinct banks.
+template <typename T>
+__host__ __device__ constexpr int pad_shift() { return sizeof(T) == 8 ? 3 : 4; }
+template <typename T>
+__device__ __forceinline__ int sp(int i) { return i + (i >> pad_shift<T>()); }
+template <typename T>
+__host__ __device__ constexpr int sp_len(int n) { return n + (n >> pad_shift<T>()); }
+
 // multiply by exp(-+2 pi i k / R), forward sign '-' unless INV
 template <typename T, int R, bool INV>
 __device__ __forceinline__ cx<T> rot_const(int k, cx<T> a) {
@@ -105,7 +116,7 @@ struct StockhamPass {
       const int j = t + b * G;
       const int k = j & (NS - 1);
 #pragma unroll
-      for (int m = 0; m < r; ++m) a[b][m] = s[j + m * NB];
+      for (int m = 0; m < r; ++m) a[b][m] = s[sp<T>(j + m * NB)];
       if (NS > 1) {
 #pragma unroll
         for (int m = 1; m < r; ++m) a[b][m] = cmul(a[b][m], twiddle(tw, m * k * TWS, INV));
@@ -119,7 +130,7 @@ struct StockhamPass {
       const int k = j & (NS - 1);
       const int base = (j - k) * r + k;
 #pragma unroll
-      for (int m = 0; m < r; ++m) s[base + m * NS] = a[b][m];
+      for (int m = 0; m < r; ++m) s[sp<T>(base + m * NS)] = a[b][m];
     }
     __syncthreads();
     StockhamPass<T, N, R, INV, NS * r>::run(s, t, tw);
@@ -157,17 +168,17 @@ __device__ __forceinline__ void two_real_rotate(cx<T>* s, int N, int t, int G, P
     }
     phase(k, ca, sa, cb, sb);
     if (2 * k == N) {
-      const cx<T> z = s[k];
-      s[k] = {z.x * ca, z.y * cb};
+      const cx<T> z = s[sp<T>(k)];
+      s[sp<T>(k)] = {z.x * ca, z.y * cb};
       continue;
     }
-    const cx<T> zk = s[k], zm = s[N - k];
+    const cx<T> zk = s[sp<T>(k)], zm = s[sp<T>(N - k)];
     const cx<T> fa = {(zk.x + zm.x) * T(0.5), (zk.y - zm.y) * T(0.5)};
     const cx<T> fb = {(zk.y + zm.y) * T(0.5), (zm.x - zk.x) * T(0.5)};
     const cx<T> ga = {ca * fa.x - sa * fa.y, ca * fa.y + sa * fa.x};
     const cx<T> gb = {cb * fb.x - sb * fb.y, cb * fb.y + sb * fb.x};
-    s[k] = {ga.x - gb.y, ga.y + gb.x};
-    s[N - k] = {ga.x + gb.y, gb.x - ga.y};
+    s[sp<T>(k)] = {ga.x - gb.y, ga.y + gb.x};
+    s[sp<T>(N - k)] = {ga.x + gb.y, gb.x - ga.y};
   }
 }
 

@@ -212,21 +212,21 @@ __global__ void __launch_bounds__(fft_threads<double>(NX)) k_poisson_fft_f64(
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cx<double>* s = reinterpret_cast<cx<double>*>(smem_raw);
   const int t = threadIdx.x;
-  for (int n = t; n < NX; n += G) s[n] = {is_density ? sub_rn(1.0, dens[n]) : dens[n], 0.0};
+  for (int n = t; n < NX; n += G) s[sp<double>(n)] = {is_density ? sub_rn(1.0, dens[n]) : dens[n], 0.0};
   __syncthreads();
   block_fft<double, NX, false>(s, t, tw);
   // (1j * inv_kx) * Z = (0 + i k)(zr + i zi) = (0*zr - k*zi) + i (0*zi + k*zr)
   for (int k = t; k < NX; k += G) {
-    const cx<double> z = s[k];
+    const cx<double> z = s[sp<double>(k)];
     const double ik = inv_kx[k];
-    s[k] = {sub_rn(mul_rn(0.0, z.x), mul_rn(ik, z.y)), add_rn(mul_rn(0.0, z.y), mul_rn(ik, z.x))};
+    s[sp<double>(k)] = {sub_rn(mul_rn(0.0, z.x), mul_rn(ik, z.y)), add_rn(mul_rn(0.0, z.y), mul_rn(ik, z.x))};
   }
   __syncthreads();
   block_fft<double, NX, true>(s, t, tw);
   const double tt = field_time(ft);
   const double sc = 1.0 / NX;
   for (int n = t; n < NX; n += G) {
-    const double self = s[n].x * sc;
+    const double self = s[sp<double>(n)].x * sc;
     e[n] = add_rn(driver_value(driver, use_pulses, P, np, tt, x, n), self);
   }
 }
@@ -273,7 +273,7 @@ template <int NX>
 cudaError_t poisson_n(const vg_plan& p, const double* dens, int is_density, const double* driver,
                       const FieldTime& ft, double* e, cudaStream_t s) {
   constexpr int G = fft_threads<double>(NX);
-  const size_t smem = (size_t)NX * sizeof(cx<double>);
+  const size_t smem = (size_t)sp_len<double>(NX) * sizeof(cx<double>);
   cudaError_t err = ensure_smem((const void*)k_poisson_fft_f64<NX>, smem);
   if (err != cudaSuccess) return err;
   k_poisson_fft_f64<NX><<<1, G, smem, s>>>(dens, is_density, p.inv_kx, driver, ft.use_pulses, p.pulses,

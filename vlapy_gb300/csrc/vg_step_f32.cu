@@ -27,7 +27,7 @@ __global__ void __launch_bounds__((NX / R) * col32_seqs(NX, R)) k_col_f32(
     float* __restrict__ g, int nv, int ntiles, int W, double phi_unit,
     const double* __restrict__ v, const cx<float>* __restrict__ tw, float2* __restrict__ dpart) {
   constexpr int G = NX / R;
-  constexpr int LD = NX + COL32_PAD;
+  constexpr int LD = sp_len<float>(NX) + COL32_PAD;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int S = W / 2;
   cx<float>* s = reinterpret_cast<cx<float>*>(smem_raw);
@@ -42,7 +42,7 @@ __global__ void __launch_bounds__((NX / R) * col32_seqs(NX, R)) k_col_f32(
     const int total = NX * W;
     for (int q = threadIdx.x; q < total; q += blockDim.x) {
       const int x = q / W, c = q - x * W;
-      sf[2 * ((c >> 1) * LD + x) + (c & 1)] = g[(size_t)x * nv + c0 + c];
+      sf[2 * ((c >> 1) * LD + sp<float>(x)) + (c & 1)] = g[(size_t)x * nv + c0 + c];
     }
     __syncthreads();
     block_fft<float, NX, false, R>(sg, t, tw);
@@ -65,13 +65,13 @@ __global__ void __launch_bounds__((NX / R) * col32_seqs(NX, R)) k_col_f32(
       for (int c = 0; c < W; ++c) {
         const int col = c0 + c;
         const float w = (col == 0 || col == nv - 1) ? 0.5f : 1.f;
-        acc = fmaf(w, sf[2 * ((c >> 1) * LD + x) + (c & 1)], acc);
+        acc = fmaf(w, sf[2 * ((c >> 1) * LD + sp<float>(x)) + (c & 1)], acc);
       }
       dacc[x] = df_add(dacc[x], {acc, 0.f});
     }
     for (int q = threadIdx.x; q < total; q += blockDim.x) {
       const int x = q / W, c = q - x * W;
-      g[(size_t)x * nv + c0 + c] = sf[2 * ((c >> 1) * LD + x) + (c & 1)];
+      g[(size_t)x * nv + c0 + c] = sf[2 * ((c >> 1) * LD + sp<float>(x)) + (c & 1)];
     }
     __syncthreads();
   }
@@ -127,14 +127,14 @@ __global__ void __launch_bounds__(fft_threads<float>(NX)) k_field_f32(
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cx<float>* s = reinterpret_cast<cx<float>*>(smem_raw);
   const int t = threadIdx.x;
-  for (int n = t; n < NX; n += G) s[n] = {(float)rho[n], 0.f};
+  for (int n = t; n < NX; n += G) s[sp<float>(n)] = {(float)rho[n], 0.f};
   __syncthreads();
   block_fft<float, NX, false>(s, t, tw);
   const float sc = 1.f / NX;
   for (int k = t; k < NX; k += G) {
-    const cx<float> z = s[k];
+    const cx<float> z = s[sp<float>(k)];
     const float ik = (float)inv_kx[k] * sc;
-    s[k] = {-ik * z.y, ik * z.x};
+    s[sp<float>(k)] = {-ik * z.y, ik * z.x};
   }
   __syncthreads();
   block_fft<float, NX, true>(s, t, tw);
@@ -145,7 +145,7 @@ __global__ void __launch_bounds__(fft_threads<float>(NX)) k_field_f32(
     float drv = 0.f;
     if (driver) drv = (float)driver[n];
     else if (use_pulses) drv = pulse_sum_f32(P, np, tt, x[n]);
-    e[n] = (double)(drv + s[n].x);
+    e[n] = (double)(drv + s[sp<float>(n)].x);
   }
 }
 
@@ -168,20 +168,20 @@ __device__ __forceinline__ void kick_rotate(cx<float>* s, int t, int G, Ang ha, 
     const float pb_m1r = -2.f * sb * sb, pb_i = 2.f * sb * cb, pb_r = 1.f + pb_m1r;
     const cx<float> f0 = F0[k];
     if (k == 0 || 2 * k == N) {
-      const cx<float> z = s[k];
+      const cx<float> z = s[sp<float>(k)];
       // real bins: only Re(P) survives
-      s[k] = {(pa_r * z.x + pa_m1r * f0.x) * sc, (pb_r * z.y + pb_m1r * f0.x) * sc};
+      s[sp<float>(k)] = {(pa_r * z.x + pa_m1r * f0.x) * sc, (pb_r * z.y + pb_m1r * f0.x) * sc};
       continue;
     }
-    const cx<float> zk = s[k], zm = s[N - k];
+    const cx<float> zk = s[sp<float>(k)], zm = s[sp<float>(N - k)];
     const cx<float> fa = {(zk.x + zm.x) * 0.5f, (zk.y - zm.y) * 0.5f};
     const cx<float> fb = {(zk.y + zm.y) * 0.5f, (zm.x - zk.x) * 0.5f};
     const cx<float> ga = {(pa_r * fa.x - pa_i * fa.y + pa_m1r * f0.x - pa_i * f0.y) * sc,
                           (pa_r * fa.y + pa_i * fa.x + pa_m1r * f0.y + pa_i * f0.x) * sc};
     const cx<float> gb = {(pb_r * fb.x - pb_i * fb.y + pb_m1r * f0.x - pb_i * f0.y) * sc,
                           (pb_r * fb.y + pb_i * fb.x + pb_m1r * f0.y + pb_i * f0.x) * sc};
-    s[k] = {ga.x - gb.y, ga.y + gb.x};
-    s[N - k] = {ga.x + gb.y, gb.x - ga.y};
+    s[sp<float>(k)] = {ga.x - gb.y, ga.y + gb.x};
+    s[sp<float>(N - k)] = {ga.x + gb.y, gb.x - ga.y};
   }
 }
 
@@ -211,7 +211,7 @@ __device__ __forceinline__ void collide_row(float* x, int t, const RowConsts& rc
     for (int i = 0; i < R; ++i) {
       const int j = t * R + i;
       const float w = (j == 0 || j == N - 1) ? 0.5f : 1.f;
-      const float gv = w * x[2 * j];
+      const float gv = w * x[2 * sp<float>(j)];
       const float vj = rc.v[j];
       a0 += gv;
       a1 = fmaf(gv, vj, a1);
@@ -239,12 +239,12 @@ __device__ __forceinline__ void collide_row(float* x, int t, const RowConsts& rc
 #pragma unroll
   for (int i = 0; i < R; ++i) {
     const int j = t * R + i;
-    x[2 * j] -= -cs * rc.S[j] + cm * rc.Mv[j] - cd * rc.D[j];
+    x[2 * sp<float>(j)] -= -cs * rc.S[j] + cm * rc.Mv[j] - cd * rc.D[j];
   }
   __syncthreads();
   auto lf = [&](int j) { return nu * (Af + (rc.v[j - 1] - vb) * i2dv); };
   auto uf = [&](int j) { return nu * (Af - (rc.v[j + 1] - vb) * i2dv); };
-  partition_solve<R>(x, 2, t, G, bdiag, lf, uf, pcr);
+  partition_solve<R>(x, t, G, bdiag, lf, uf, pcr);
 }
 
 template <int N, int R>
@@ -257,8 +257,9 @@ __global__ void __launch_bounds__(row32_block(N, R)) k_row_f32(RowArgs a) {
   const size_t grp_bytes = row32_group_bytes(N, R);
   unsigned char* gb = smem_raw + (size_t)grp * grp_bytes;
   cx<float>* s = reinterpret_cast<cx<float>*>(gb);
-  float* pcr = reinterpret_cast<float*>(gb + (size_t)N * sizeof(cx<float>));
-  df32* red = reinterpret_cast<df32*>(gb + (size_t)N * sizeof(cx<float>) + 8 * G * sizeof(float));
+  const size_t seq_bytes = (size_t)sp_len<float>(N) * sizeof(cx<float>) + 16;
+  float* pcr = reinterpret_cast<float*>(gb + seq_bytes);
+  df32* red = reinterpret_cast<df32*>(gb + seq_bytes + 8 * G * sizeof(float));
   cx<float>* macc = reinterpret_cast<cx<float>*>(smem_raw + (size_t)P * grp_bytes);  // [n_modes][N]
   const int nm = a.n_modes;
   for (int q = threadIdx.x; q < nm * N; q += blockDim.x) macc[q] = {0.f, 0.f};
@@ -273,7 +274,7 @@ __global__ void __launch_bounds__(row32_block(N, R)) k_row_f32(RowArgs a) {
 #pragma unroll
     for (int i = 0; i < R; ++i) {
       const int n = t + i * G;
-      s[n] = {va ? ga[n] : 0.f, vb ? gbp[n] : 0.f};
+      s[sp<float>(n)] = {va ? ga[n] : 0.f, vb ? gbp[n] : 0.f};
     }
     __syncthreads();
     const bool kicks = a.dt1 != 0.0 || a.dt2 != 0.0;
@@ -293,7 +294,7 @@ __global__ void __launch_bounds__(row32_block(N, R)) k_row_f32(RowArgs a) {
         const int j = t * R + i;
         const float w = (j == 0 || j == N - 1) ? 0.5f : 1.f;
         const float vj = a.rc.v[j], f0j = a.rc.f0[j];
-        const cx<float> z = s[j];
+        const cx<float> z = s[sp<float>(j)];
         float pa = w * z.x, pb = w * z.y;
 #pragma unroll
         for (int p = 0; p < 6; ++p) {
@@ -341,7 +342,7 @@ __global__ void __launch_bounds__(row32_block(N, R)) k_row_f32(RowArgs a) {
             if (!vb) cwb = swb = 0.f;
             for (int i = 0; i < R; ++i) {
               const int n = t + i * G;
-              const cx<float> z = s[n];
+              const cx<float> z = s[sp<float>(n)];
               cx<float>& acc = macc[(size_t)mq * N + n];
               acc.x += z.x * cwa + z.y * cwb;
               acc.y += z.x * swa + z.y * swb;
@@ -355,7 +356,7 @@ __global__ void __launch_bounds__(row32_block(N, R)) k_row_f32(RowArgs a) {
 #pragma unroll
     for (int i = 0; i < R; ++i) {
       const int n = t + i * G;
-      const cx<float> z = s[n];
+      const cx<float> z = s[sp<float>(n)];
       if (va) ga[n] = z.x;
       if (vb) gbp[n] = z.y;
     }
@@ -430,7 +431,7 @@ cudaError_t col_n(const vg_plan& p, float* g, double dt, cudaStream_t s) {
   if (2 * S > p.nv) S = p.nv / 2;
   const int W = 2 * S;
   const int ntiles = p.nv / W;
-  const size_t smem = (size_t)S * (NX + COL32_PAD) * sizeof(cx<float>) + (size_t)NX * sizeof(df32);
+  const size_t smem = (size_t)S * (sp_len<float>(NX) + COL32_PAD) * sizeof(cx<float>) + (size_t)NX * sizeof(df32);
   cudaError_t err = ensure_smem((const void*)k_col_f32<NX, R>, smem);
   if (err != cudaSuccess) return err;
   int occ = 1;
@@ -446,7 +447,7 @@ cudaError_t col_n(const vg_plan& p, float* g, double dt, cudaStream_t s) {
 template <int NX>
 cudaError_t field_n(const vg_plan& p, const double* driver, const FieldTime& ft, double* e, cudaStream_t s) {
   constexpr int G = fft_threads<float>(NX);
-  const size_t smem = (size_t)NX * sizeof(cx<float>);
+  const size_t smem = (size_t)sp_len<float>(NX) * sizeof(cx<float>);
   cudaError_t err = ensure_smem((const void*)k_field_f32<NX>, smem);
   if (err != cudaSuccess) return err;
   k_field_f32<NX><<<1, G, smem, s>>>(p.rho, p.inv_kx, driver, ft.use_pulses, p.pulses, p.n_pulses, p.x, ft.t_ptr,

@@ -22,59 +22,68 @@ namespace vg {
 
 constexpr int COL32_PAD = 1;
 
+// One column tile [NX x W] at column c0: x-drift by exp(i m (-dkx dt) v_col)
+// and the tile's trapz-weighted density partials added into dacc[x].
+// smem: W/2 padded sequences of NX complex floats.
+template <int NX, int R>
+__device__ __forceinline__ void col_tile(float* __restrict__ g, int nv, int c0, int W, double phi_unit,
+                                         const double* __restrict__ v, const cx<float>* __restrict__ tw,
+                                         unsigned char* smem, df32* dacc) {
+  constexpr int G = NX / R;
+  constexpr int LD = sp_len<float>(NX) + COL32_PAD;
+  cx<float>* s = reinterpret_cast<cx<float>*>(smem);
+  float* sf = reinterpret_cast<float*>(smem);
+  const int grp = threadIdx.x / G, t = threadIdx.x - grp * G;
+  cx<float>* sg = s + (size_t)grp * LD;
+  const float scale = 1.f / NX;
+  const int total = NX * W;
+  for (int q = threadIdx.x; q < total; q += blockDim.x) {
+    const int x = q / W, c = q - x * W;
+    sf[2 * ((c >> 1) * LD + sp<float>(x)) + (c & 1)] = g[(size_t)x * nv + c0 + c];
+  }
+  __syncthreads();
+  block_fft<float, NX, false, R>(sg, t, tw);
+  // theta(m) = m * (-dkx dt v_col): kx = m dkx on the bins m <= NX/2
+  const Ang aa = split_angle(phi_unit * v[c0 + 2 * grp]);
+  const Ang ab = split_angle(phi_unit * v[c0 + 2 * grp + 1]);
+  two_real_rotate<float>(sg, NX, t, G, [&](int m, float& ca, float& sa, float& cb, float& sb) {
+    sincos_m((float)m, aa, sa, ca);
+    sincos_m((float)m, ab, sb, cb);
+    ca *= scale;
+    sa *= scale;
+    cb *= scale;
+    sb *= scale;
+  });
+  __syncthreads();
+  block_fft<float, NX, true, R>(sg, t, tw);
+  // density partial sums (trapz weights: 1/2 at the two v end points)
+  for (int x = threadIdx.x; x < NX; x += blockDim.x) {
+    float acc = 0.f;
+    for (int c = 0; c < W; ++c) {
+      const int col = c0 + c;
+      const float w = (col == 0 || col == nv - 1) ? 0.5f : 1.f;
+      acc = fmaf(w, sf[2 * ((c >> 1) * LD + sp<float>(x)) + (c & 1)], acc);
+    }
+    dacc[x] = df_add(dacc[x], {acc, 0.f});
+  }
+  for (int q = threadIdx.x; q < total; q += blockDim.x) {
+    const int x = q / W, c = q - x * W;
+    g[(size_t)x * nv + c0 + c] = sf[2 * ((c >> 1) * LD + sp<float>(x)) + (c & 1)];
+  }
+  __syncthreads();
+}
+
 template <int NX, int R>
 __global__ void __launch_bounds__((NX / R) * col32_seqs(NX, R)) k_col_f32(
     float* __restrict__ g, int nv, int ntiles, int W, double phi_unit,
     const double* __restrict__ v, const cx<float>* __restrict__ tw, float2* __restrict__ dpart) {
-  constexpr int G = NX / R;
   constexpr int LD = sp_len<float>(NX) + COL32_PAD;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int S = W / 2;
-  cx<float>* s = reinterpret_cast<cx<float>*>(smem_raw);
-  float* sf = reinterpret_cast<float*>(smem_raw);
   df32* dacc = reinterpret_cast<df32*>(smem_raw + (size_t)S * LD * sizeof(cx<float>));
   for (int x = threadIdx.x; x < NX; x += blockDim.x) dacc[x] = {0.f, 0.f};
-  const int grp = threadIdx.x / G, t = threadIdx.x - grp * G;
-  cx<float>* sg = s + (size_t)grp * LD;
-  const float scale = 1.f / NX;
-  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const int c0 = tile * W;
-    const int total = NX * W;
-    for (int q = threadIdx.x; q < total; q += blockDim.x) {
-      const int x = q / W, c = q - x * W;
-      sf[2 * ((c >> 1) * LD + sp<float>(x)) + (c & 1)] = g[(size_t)x * nv + c0 + c];
-    }
-    __syncthreads();
-    block_fft<float, NX, false, R>(sg, t, tw);
-    // theta(m) = m * (-dkx dt v_col): kx = m dkx on the bins m <= NX/2
-    const Ang aa = split_angle(phi_unit * v[c0 + 2 * grp]);
-    const Ang ab = split_angle(phi_unit * v[c0 + 2 * grp + 1]);
-    two_real_rotate<float>(sg, NX, t, G, [&](int m, float& ca, float& sa, float& cb, float& sb) {
-      sincos_m((float)m, aa, sa, ca);
-      sincos_m((float)m, ab, sb, cb);
-      ca *= scale;
-      sa *= scale;
-      cb *= scale;
-      sb *= scale;
-    });
-    __syncthreads();
-    block_fft<float, NX, true, R>(sg, t, tw);
-    // density partial sums (trapz weights: 1/2 at the two v end points)
-    for (int x = threadIdx.x; x < NX; x += blockDim.x) {
-      float acc = 0.f;
-      for (int c = 0; c < W; ++c) {
-        const int col = c0 + c;
-        const float w = (col == 0 || col == nv - 1) ? 0.5f : 1.f;
-        acc = fmaf(w, sf[2 * ((c >> 1) * LD + sp<float>(x)) + (c & 1)], acc);
-      }
-      dacc[x] = df_add(dacc[x], {acc, 0.f});
-    }
-    for (int q = threadIdx.x; q < total; q += blockDim.x) {
-      const int x = q / W, c = q - x * W;
-      g[(size_t)x * nv + c0 + c] = sf[2 * ((c >> 1) * LD + sp<float>(x)) + (c & 1)];
-    }
-    __syncthreads();
-  }
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x)
+    col_tile<NX, R>(g, nv, tile * W, W, phi_unit, v, tw, smem_raw, dacc);
   for (int x = threadIdx.x; x < NX; x += blockDim.x)
     dpart[(size_t)blockIdx.x * NX + x] = make_float2(dacc[x].hi, dacc[x].lo);
 }
@@ -247,99 +256,90 @@ __device__ __forceinline__ void collide_row(float* x, int t, const RowConsts& rc
   partition_solve<R>(x, t, G, bdiag, lf, uf, pcr);
 }
 
+// One row-pair group of the row pass: load, [kick dt1], [collide], [moments
+// and x-mode partials], [kick dt2], store.  grp_base: this group's shared
+// memory (row32_group_bytes); macc: the CTA's mode accumulators [n_modes][N].
 template <int N, int R>
-__global__ void __launch_bounds__(row32_block(N, R)) k_row_f32(RowArgs a) {
+__device__ __forceinline__ void row_pair(const RowArgs& a, int pair, unsigned char* grp_base, cx<float>* macc,
+                                         int P, int grp, int t) {
   constexpr int G = N / R;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int P = blockDim.x / G;
-  const int grp = threadIdx.x / G, t = threadIdx.x - grp * G;
-  // per group: row pair [N] cx<float>, PCR scratch [8G] floats, df reduction [G/32+1][9]
-  const size_t grp_bytes = row32_group_bytes(N, R);
-  unsigned char* gb = smem_raw + (size_t)grp * grp_bytes;
-  cx<float>* s = reinterpret_cast<cx<float>*>(gb);
+  cx<float>* s = reinterpret_cast<cx<float>*>(grp_base);
   const size_t seq_bytes = (size_t)sp_len<float>(N) * sizeof(cx<float>) + 16;
-  float* pcr = reinterpret_cast<float*>(gb + seq_bytes);
-  df32* red = reinterpret_cast<df32*>(gb + seq_bytes + 8 * G * sizeof(float));
-  cx<float>* macc = reinterpret_cast<cx<float>*>(smem_raw + (size_t)P * grp_bytes);  // [n_modes][N]
+  float* pcr = reinterpret_cast<float*>(grp_base + seq_bytes);
+  df32* red = reinterpret_cast<df32*>(grp_base + seq_bytes + 8 * G * sizeof(float));
   const int nm = a.n_modes;
-  for (int q = threadIdx.x; q < nm * N; q += blockDim.x) macc[q] = {0.f, 0.f};
-  const int npairs = (a.nx + 1) / 2;
-  const int ngroups = (npairs + P - 1) / P;
-  for (int pg = blockIdx.x; pg < ngroups; pg += gridDim.x) {
-    const int pair = pg * P + grp;
-    const int ra = 2 * pair, rb = ra + 1;
-    const bool va = ra < a.nx, vb = rb < a.nx;
-    float* ga = a.g + (size_t)ra * N;
-    float* gbp = a.g + (size_t)rb * N;
+  const int ra = 2 * pair, rb = ra + 1;
+  const bool va = ra < a.nx, vb = rb < a.nx;
+  float* ga = a.g + (size_t)ra * N;
+  float* gbp = a.g + (size_t)rb * N;
+#pragma unroll
+  for (int i = 0; i < R; ++i) {
+    const int n = t + i * G;
+    s[sp<float>(n)] = {va ? ga[n] : 0.f, vb ? gbp[n] : 0.f};
+  }
+  __syncthreads();
+  const bool kicks = a.dt1 != 0.0 || a.dt2 != 0.0;
+  const double ea = (kicks && va) ? a.e[ra] : 0.0, eb = (kicks && vb) ? a.e[rb] : 0.0;
+  if (a.dt1 != 0.0) kick<N, R>(s, t, a.rc.dkv, a.dt1, ea, eb, a.F0, a.tw);
+  float* sx = reinterpret_cast<float*>(s);
+  if (a.fp) {
+    collide_row<N, R>(sx, t, a.rc, a.nudt, a.dougherty, red, pcr);
+    collide_row<N, R>(sx + 1, t, a.rc, a.nudt, a.dougherty, red, pcr);
+  }
+  if (a.want_mom) {
+    // n, j, T, q, fv4, vN (sums of w g v^p), sum w g^2, sum w g f0, sum w f log f
+    df32 mv[9], mw[9];
+    float sa[9] = {0}, sb[9] = {0};
 #pragma unroll
     for (int i = 0; i < R; ++i) {
-      const int n = t + i * G;
-      s[sp<float>(n)] = {va ? ga[n] : 0.f, vb ? gbp[n] : 0.f};
+      const int j = t * R + i;
+      const float w = (j == 0 || j == N - 1) ? 0.5f : 1.f;
+      const float vj = a.rc.v[j], f0j = a.rc.f0[j];
+      const cx<float> z = s[sp<float>(j)];
+      float pa = w * z.x, pb = w * z.y;
+#pragma unroll
+      for (int p = 0; p < 6; ++p) {
+        sa[p] += pa;
+        sb[p] += pb;
+        pa *= vj;
+        pb *= vj;
+      }
+      sa[6] = fmaf(w * z.x, z.x, sa[6]);
+      sb[6] = fmaf(w * z.y, z.y, sb[6]);
+      sa[7] = fmaf(w * z.x, f0j, sa[7]);
+      sb[7] = fmaf(w * z.y, f0j, sb[7]);
+      const float fa = z.x + f0j, fb = z.y + f0j;
+      sa[8] = fmaf(w * fa, logf(fa), sa[8]);
+      sb[8] = fmaf(w * fb, logf(fb), sb[8]);
     }
-    __syncthreads();
-    const bool kicks = a.dt1 != 0.0 || a.dt2 != 0.0;
-    const double ea = (kicks && va) ? a.e[ra] : 0.0, eb = (kicks && vb) ? a.e[rb] : 0.0;
-    if (a.dt1 != 0.0) kick<N, R>(s, t, a.rc.dkv, a.dt1, ea, eb, a.F0, a.tw);
-    float* sx = reinterpret_cast<float*>(s);
-    if (a.fp) {
-      collide_row<N, R>(sx, t, a.rc, a.nudt, a.dougherty, red, pcr);
-      collide_row<N, R>(sx + 1, t, a.rc, a.nudt, a.dougherty, red, pcr);
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+      mv[q] = {sa[q], 0.f};
+      mw[q] = {sb[q], 0.f};
     }
-    if (a.want_mom) {
-      // n, j, T, q, fv4, vN (sums of w g v^p), sum w g^2, sum w g f0, sum w f log f
-      df32 mv[9], mw[9];
-      float sa[9] = {0}, sb[9] = {0};
-#pragma unroll
-      for (int i = 0; i < R; ++i) {
-        const int j = t * R + i;
-        const float w = (j == 0 || j == N - 1) ? 0.5f : 1.f;
-        const float vj = a.rc.v[j], f0j = a.rc.f0[j];
-        const cx<float> z = s[sp<float>(j)];
-        float pa = w * z.x, pb = w * z.y;
-#pragma unroll
-        for (int p = 0; p < 6; ++p) {
-          sa[p] += pa;
-          sb[p] += pb;
-          pa *= vj;
-          pb *= vj;
-        }
-        sa[6] = fmaf(w * z.x, z.x, sa[6]);
-        sb[6] = fmaf(w * z.y, z.y, sb[6]);
-        sa[7] = fmaf(w * z.x, f0j, sa[7]);
-        sb[7] = fmaf(w * z.y, f0j, sb[7]);
-        const float fa = z.x + f0j, fb = z.y + f0j;
-        sa[8] = fmaf(w * fa, logf(fa), sa[8]);
-        sb[8] = fmaf(w * fb, logf(fb), sb[8]);
+    group_df_sum<9>(mv, red, G, t);
+    group_df_sum<9>(mw, red, G, t);
+    if (t == 0) {
+      for (int r = 0; r < 2; ++r) {
+        const int row = r ? rb : ra;
+        if (!(r ? vb : va)) continue;
+        const df32* m = r ? mw : mv;
+        double* out = a.mom + (size_t)row * MOM_STRIDE;
+        for (int p = 0; p < 6; ++p) out[p] = a.rc.dv * df_to_double(m[p]) + a.rc.f0m[p];
+        out[6] = a.rc.dv * (df_to_double(m[6]) + 2.0 * df_to_double(m[7])) + a.rc.f0m[6];
+        out[7] = a.rc.dv * df_to_double(m[8]);
       }
-#pragma unroll
-      for (int q = 0; q < 9; ++q) {
-        mv[q] = {sa[q], 0.f};
-        mw[q] = {sb[q], 0.f};
-      }
-      group_df_sum<9>(mv, red, G, t);
-      group_df_sum<9>(mw, red, G, t);
-      if (t == 0) {
-        for (int r = 0; r < 2; ++r) {
-          const int row = r ? rb : ra;
-          if (!(r ? vb : va)) continue;
-          const df32* m = r ? mw : mv;
-          double* out = a.mom + (size_t)row * MOM_STRIDE;
-          for (int p = 0; p < 6; ++p) out[p] = a.rc.dv * df_to_double(m[p]) + a.rc.f0m[p];
-          out[6] = a.rc.dv * (df_to_double(m[6]) + 2.0 * df_to_double(m[7])) + a.rc.f0m[6];
-          out[7] = a.rc.dv * df_to_double(m[8]);
-        }
-      }
-      // x-Fourier modes of f (the f0 part of mode 0 is added in the reduction);
-      // the groups of a CTA hold different rows but add into the same bins,
-      // so they take turns
+    }
+    // x-Fourier modes of f (the f0 part of mode 0 is added in the reduction);
+    // the groups of a CTA hold different rows but add into the same bins,
+    // so they take turns
+    if (nm > 0) {
       for (int gq = 0; gq < P; ++gq) {
         if (gq == grp) {
           for (int mq = 0; mq < nm; ++mq) {
-            float swa, cwa, swb, cwb;
-            sincospif(-2.f * (float)((mq * ra) % a.nx) / (float)a.nx, &swa, &cwa);
-            sincospif(-2.f * (float)((mq * rb) % a.nx) / (float)a.nx, &swb, &cwb);
-            if (!va) cwa = swa = 0.f;
-            if (!vb) cwb = swb = 0.f;
+            float swa = 0.f, cwa = 0.f, swb = 0.f, cwb = 0.f;
+            if (va) sincospif(-2.f * (float)((mq * ra) % a.nx) / (float)a.nx, &swa, &cwa);
+            if (vb) sincospif(-2.f * (float)((mq * rb) % a.nx) / (float)a.nx, &swb, &cwb);
             for (int i = 0; i < R; ++i) {
               const int n = t + i * G;
               const cx<float> z = s[sp<float>(n)];
@@ -352,17 +352,34 @@ __global__ void __launch_bounds__(row32_block(N, R)) k_row_f32(RowArgs a) {
         __syncthreads();
       }
     }
-    if (a.dt2 != 0.0) kick<N, R>(s, t, a.rc.dkv, a.dt2, ea, eb, a.F0, a.tw);
-#pragma unroll
-    for (int i = 0; i < R; ++i) {
-      const int n = t + i * G;
-      const cx<float> z = s[sp<float>(n)];
-      if (va) ga[n] = z.x;
-      if (vb) gbp[n] = z.y;
-    }
-    __syncthreads();
   }
-  if (a.want_mom && nm > 0) {
+  if (a.dt2 != 0.0) kick<N, R>(s, t, a.rc.dkv, a.dt2, ea, eb, a.F0, a.tw);
+#pragma unroll
+  for (int i = 0; i < R; ++i) {
+    const int n = t + i * G;
+    const cx<float> z = s[sp<float>(n)];
+    if (va) ga[n] = z.x;
+    if (vb) gbp[n] = z.y;
+  }
+  __syncthreads();
+}
+
+template <int N, int R>
+__global__ void __launch_bounds__(row32_block(N, R)) k_row_f32(RowArgs a) {
+  constexpr int G = N / R;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int P = blockDim.x / G;
+  const int grp = threadIdx.x / G, t = threadIdx.x - grp * G;
+  const size_t grp_bytes = row32_group_bytes(N, R);
+  cx<float>* macc = reinterpret_cast<cx<float>*>(smem_raw + (size_t)P * grp_bytes);  // [n_modes][N]
+  const int nm = a.want_mom ? a.n_modes : 0;
+  for (int q = threadIdx.x; q < nm * N; q += blockDim.x) macc[q] = {0.f, 0.f};
+  const int npairs = (a.nx + 1) / 2;
+  const int ngroups = (npairs + P - 1) / P;
+  for (int pg = blockIdx.x; pg < ngroups; pg += gridDim.x)
+    row_pair<N, R>(a, pg * P + grp, smem_raw + (size_t)grp * grp_bytes, macc, P, grp, t);
+  if (nm > 0) {
+    __syncthreads();
     for (int q = threadIdx.x; q < nm * N; q += blockDim.x)
       a.mpart[(size_t)blockIdx.x * nm * N + q] = macc[q];
   }

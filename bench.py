@@ -11,6 +11,9 @@ bytes per launch over its CUDA-event launch time in a profiled pass.
 reference path) on the host cores instead.
 
 Workloads (synthetic inputs of the reference's shapes; no datasets involved):
+  sweep   4096 independent runs (seeded: nx in {32,64,128}, nv in {256,512,1024},
+          k ~ U[0.25,0.45], amplitude 10^U[-6,-2], nu 10^U[-5,-2] with 25% zero,
+          DG collisions, vmax=6.4, dt=0.1), all advanced by every launch
   large   nx=4096, nv=8192, xmax=2pi/0.3, vmax=8, two-stream f, nu=1e-4 DG, dt=0.05
   driven  nx=64, nv=1024, k=0.3, vmax=6.4, sin^2-enveloped driver, nu=1e-3 DG, dt=0.1
   landau  nx=32, nv=512, k=0.3, vmax=6.4, A=1e-4, nu=0, dt=0.1
@@ -31,7 +34,10 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+SWEEP_STEPS = 2000  # steps of one sweep run (the workload's run length)
+
 WORKLOADS = {
+    "sweep": dict(kind="sweep", n_runs=4096, seed=20261203, vmax=6.4, dt=0.1),
     "large": dict(nx=4096, nv=8192, k=0.3, vmax=8.0, dt=0.05, nu=1e-4, op="dg", kind="two-stream"),
     "driven": dict(nx=64, nv=1024, k=0.3, vmax=6.4, dt=0.1, nu=1e-3, op="dg", kind="driven"),
     "landau": dict(nx=32, nv=512, k=0.3, vmax=6.4, dt=0.1, nu=0.0, op="dg", kind="landau"),
@@ -227,6 +233,146 @@ def run_e2e(plan, f, e, storage, hist, tb_host, drv_host, W, K, stream, torch):
     return (t1 - t0), h2d, d2h
 
 
+def run_sweep_gpu(args, w, rank, world):
+    import torch
+    from vlapy_gb300 import _lib
+    from vlapy_gb300.sweep import Sweep, sweep_config
+
+    torch.cuda.set_device(rank % max(1, torch.cuda.device_count()))
+    _lib.load()
+    runs = sweep_config(w["n_runs"], w["seed"])
+    sw = Sweep(runs, vmax=w["vmax"], dt=w["dt"])
+    K, W = args.steps, args.warmup
+    eh, sh = sw.history(K)
+    stream = torch.cuda.Stream()
+    with torch.cuda.stream(stream):
+        sw.reset(stream)
+        sw.run_steps(W, use_graph=False, stream=stream)
+        sw.run_steps(K, eh, sh, use_graph=True, stream=stream)  # capture
+        sw.reset(stream)
+        sw.run_steps(W, use_graph=False, stream=stream)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    with torch.cuda.stream(stream):
+        sw.run_steps(K, eh, sh, use_graph=True, stream=stream)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    clk = clocks.stop()
+    if not torch.isfinite(eh).all():
+        raise RuntimeError("non-finite field in the sweep history")
+    sw.profile(True)
+    with torch.cuda.stream(stream):
+        sw.run_steps(args.prof_steps, eh, sh, use_graph=False, stream=stream)
+    prof = sw.profile_read()
+    sw.profile(False)
+    # e2e: one C-ABI call per step, the step's e row and series read back to pinned memory
+    out_e = torch.empty(sw.x_points, dtype=torch.float64).pin_memory()
+    out_s = torch.empty((sw.n_runs, 7), dtype=torch.float64).pin_memory()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    with torch.cuda.stream(stream):
+        for i in range(K):
+            sw.run_steps(1, eh, sh, row0=0, use_graph=False, stream=stream)
+            out_e.copy_(eh[0], non_blocking=True)
+            out_s.copy_(sh[0], non_blocking=True)
+            stream.synchronize()
+    e2e_sec = time.perf_counter() - t0
+    d2h = out_e.numel() * 8 + out_s.numel() * 8
+    return ms, prof, clk, (e2e_sec, 0, d2h), sw
+
+
+def fp64_plain_sweep(w, steps=3):
+    """Plain FP64 GPU step (the parity mode, one run at a time) timed on one
+    sampled run of each shape class and extrapolated to the sweep."""
+    import torch
+    from vlapy_gb300 import initializers as I
+    from vlapy_gb300.plan import Plan
+    from vlapy_gb300.sweep import sweep_config
+    runs = sweep_config(w["n_runs"], w["seed"])
+    classes = {}
+    for r in runs:
+        classes.setdefault((r["nx"], r["nv"]), []).append(r)
+    total_ms = 0.0
+    per = {}
+    for (nx, nv), rs in sorted(classes.items()):
+        r = next((q for q in rs if q["nu"] > 0), rs[0])
+        dx, x, kx, inv = I.initialize_spatial_quantities(0.0, 2 * np.pi / r["k"], nx)
+        dv, v, kv = I.initialize_velocity_quantities(w["vmax"], nv)
+        p = Plan(nx, nv, x, v, kx, kv, inv, dx, dv, dt=w["dt"], nu=r["nu"], collision="dg" if r["nu"] > 0 else "none")
+        f = torch.as_tensor(I.initialize_distribution(nx, nv, w["vmax"]) * (1 + r["amplitude"] * np.cos(r["k"] * x))[:, None],
+                            device="cuda")
+        e = torch.zeros(nx, dtype=torch.float64, device="cuda")
+        tb = torch.as_tensor(w["dt"] * np.arange(steps + 2), device="cuda")
+        p.run_steps(f, e, None, tb, None, 0, 2, use_graph=False)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        p.run_steps(f, e, None, tb, None, 0, steps, use_graph=False)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        per["%dx%d" % (nx, nv)] = ms
+        total_ms += ms * len(rs)
+        p.close()
+    runs_per_s = len(runs) / (total_ms / 1e3 * SWEEP_STEPS)
+    return runs_per_s, per
+
+
+def _oracle_sweep_sample(args):
+    """One pool task: oracle steps of one sampled sweep run (host cores)."""
+    r, steps, vmax, dt = args
+    import numpy as np
+    from oracle import vlapy_oracle as vo
+    nx, nv, k = r["nx"], r["nv"], r["k"]
+    run = vo.OracleRun(nx, nv, 2 * np.pi / k, vmax, dt, nu=r["nu"], operator="dg", n_modes=2)
+    dx, x, kx, inv = vo.spatial_axis(0.0, 2 * np.pi / k, nx)
+    f = vo.maxwellian(nx, nv, vmax) * (1.0 + r["amplitude"] * np.cos(k * x))[:, None]
+    st = vo.new_storage(f, np.zeros(nx), steps, 2)
+    st["time_batch"] = dt * np.arange(steps)
+    st["driver_array_batch"] = np.zeros((steps, nx))
+    t0 = time.perf_counter()
+    for i in range(steps):
+        run.timestep(st, i)
+    return nx * nv * steps, time.perf_counter() - t0
+
+
+def cpu_baseline_sweep(w, n_sample=36, steps=10, cores=None):
+    """Reference step (CPU oracle) on a stratified sample of sweep runs, one
+    process per host core; aggregate cell-updates/s and extrapolated runs/s."""
+    import multiprocessing as mp
+    from vlapy_gb300.sweep import sweep_config
+    runs = sweep_config(w["n_runs"], w["seed"])
+    classes = {}
+    for r in runs:
+        classes.setdefault((r["nx"], r["nv"]), []).append(r)
+    per_class = max(1, n_sample // len(classes))
+    sample = []
+    for key in sorted(classes):
+        sample += classes[key][:per_class]
+    cores = cores or os.cpu_count() or 1
+    with mp.get_context("spawn").Pool(min(cores, len(sample))) as pool:
+        # warm the workers (imports, first FFT plans) before timing
+        pool.map(_oracle_sweep_sample, [(r, 1, w["vmax"], w["dt"]) for r in sample])
+        t0 = time.perf_counter()
+        res = pool.map(_oracle_sweep_sample, [(r, steps, w["vmax"], w["dt"]) for r in sample])
+        wall = time.perf_counter() - t0
+    cells = sum(c for c, _ in res)
+    # seconds per step per class (single core), then the whole sweep on `cores` cores
+    sec_class = {}
+    for r, (c, sec) in zip(sample, res):
+        sec_class.setdefault((r["nx"], r["nv"]), []).append(sec / steps)
+    core_sec = sum(np.mean(sec_class[key]) * len(classes[key]) for key in classes) * SWEEP_STEPS
+    runs_per_s = len(runs) / (core_sec / min(cores, len(sample)))
+    value = cells / wall
+    return value, runs_per_s, min(cores, len(sample)), len(sample), steps, wall
+
+
 def cpu_baseline(w, steps, reps_cap=3):
     """Oracle (NumPy restatement of the reference step) on the host cores."""
     from oracle import vlapy_oracle as vo
@@ -256,7 +402,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="large", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="sweep", choices=sorted(WORKLOADS))
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32-deltaf"])
     ap.add_argument("--prof-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -266,6 +412,8 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     w = WORKLOADS[args.workload]
+    if w["kind"] == "sweep":
+        return main_sweep(args, w, rank, world)
     cells = w["nx"] * w["nv"]
     metric = "cell-updates/s"
     cfg = {"workload": args.workload, "nx": w["nx"], "nv": w["nv"], "dt": w["dt"], "nu": w["nu"],
@@ -332,6 +480,78 @@ def main():
         "gpu_launches": int(round(launches_per_step * args.steps)),
         "clocks": clk,
         "cpu_baseline": cpu,
+    }
+    print(json.dumps(line))
+
+
+def main_sweep(args, w, rank, world):
+    cfg = {"workload": "sweep", "n_runs": w["n_runs"], "seed": w["seed"], "nx": [32, 64, 128],
+           "nv": [256, 512, 1024], "vmax": w["vmax"], "dt": w["dt"], "collision": "dg (25% of runs nu=0)",
+           "integrator": "leapfrog", "precision": "fp32-deltaf (FP64 moment/zero-mode reductions)",
+           "storage": "per run and step: field e[nx] + 7 series", "run_steps": SWEEP_STEPS}
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        val, rps, cores, n, steps, wall = cpu_baseline_sweep(w, n_sample=max(36, args.steps), steps=60)
+        line = {"metric": "cell-updates/s", "value": val, "unit": "cell-updates/s", "n_gpus": args.gpus,
+                "steps": steps, "warmup": 0, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg, "impl": "reference",
+                "runs_per_s": rps,
+                "cpu_baseline": {"value": val, "unit": "cell-updates/s", "cores": cores, "kind": "port",
+                                 "sample": "%d sweep runs (stratified over the 9 shapes) x %d full oracle steps, "
+                                           "one process per core, %.1f s wall; runs/s extrapolated to 4096 "
+                                           "runs x 2000 steps" % (n, steps, wall)},
+                "e2e": {"value": val, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+    import torch
+    if world > 1:
+        torch.distributed.init_process_group("nccl")
+    ms, prof, clk, e2e, sw = run_sweep_gpu(args, w, int(os.environ.get("LOCAL_RANK", rank)), world)
+    t_max = ms
+    if world > 1:
+        tt = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_max = float(tt.item())
+    cells = sw.cells
+    value = world * cells * args.steps / (t_max / 1e3)
+    runs_per_s = world * sw.n_runs / (t_max / args.steps / 1e3 * SWEEP_STEPS)
+    e2e_sec, h2d, d2h = e2e
+    dom_name, dom = max(prof.items(), key=lambda kv: kv[1]["total_ms"])
+    avg_ms = dom["total_ms"] / dom["launches"]
+    peak, peak_kind = peaks()
+    achieved = dom["bytes_per_launch"] / (avg_ms / 1e3) / 1e9
+    launches_per_step = 0.0
+    for k, d in prof.items():
+        launches_per_step += d["launches"] / args.prof_steps
+    if rank != 0:
+        return
+    fp64_rps, fp64_per = fp64_plain_sweep(w)
+    cpu = None
+    if not args.no_cpu_baseline:
+        cval, crps, cores, n, steps, wall = cpu_baseline_sweep(w, n_sample=36, steps=60)
+        cpu = {"value": cval, "unit": "cell-updates/s", "cores": cores, "kind": "port", "runs_per_s": crps,
+               "sample": "%d sweep runs (stratified over the 9 shapes) x %d full oracle steps, one process per "
+                         "core, %.1f s wall" % (n, steps, wall)}
+    line = {
+        "metric": "cell-updates/s", "value": value, "unit": "cell-updates/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": cfg,
+        "runs_per_s": runs_per_s,
+        "fp64_plain_gpu": {"runs_per_s": fp64_rps, "ms_per_step_by_shape": fp64_per,
+                           "how": "FP64 parity step, one run at a time, timed on one run per shape and "
+                                  "weighted by the shape counts"},
+        "e2e": {"value": world * cells * args.steps / e2e_sec, "unit": "cell-updates/s",
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "kernel": dom_name, "peak_source": peak_kind, "kernel_ms": avg_ms,
+                     "bytes_per_launch": dom["bytes_per_launch"]},
+        "kernels": {k: {"launches": d["launches"], "avg_ms": d["total_ms"] / d["launches"]} for k, d in prof.items()},
+        "gpu_launches": int(round(launches_per_step * args.steps)),
+        "clocks": clk,
+        "cpu_baseline": cpu,
+        "state_bytes": cells * 4,
+        "l2": "state %.0f MB, larger than L2 (129 MB)" % (cells * 4 / 1e6),
     }
     print(json.dumps(line))
 

@@ -89,6 +89,14 @@ typedef struct vg_history {
   void* stored_f;
 } vg_history;
 
+/* one line of a per-kernel timing record (vg_profile_read, vg_sweep_profile_read) */
+typedef struct vg_prof_entry {
+  char name[32];
+  int64_t launches;
+  double total_ms;
+  double bytes_per_launch;
+} vg_prof_entry;
+
 /* ---- plan lifetime ---------------------------------------------------- */
 /* Builds the per-run constants (grids, FFT twiddles, NumPy summation trees)
  * and allocates the plan's scratch with cudaMalloc on the current device.
@@ -138,6 +146,50 @@ int vg_run_steps(vg_plan* plan, void* f, double* e, const vg_history* hist,
                  const double* time_batch, const double* driver_batch,
                  int32_t i0, int32_t nsteps, int32_t use_graph, vg_stream stream);
 
+/* ---- batched sweep ----------------------------------------------------- */
+/* Thousands of independent runs of uneven shape advanced together in the
+ * FP32 delta-f mode: every kernel launch of a step covers all runs (work
+ * lists of (run, column tile) and (run, row-pair group) items dispatched by
+ * shape inside the kernel).  Each run is the reference's leapfrog step with
+ * exponential advection, spectral Poisson and, for nu > 0, the chosen
+ * collision operator (vlapy/core/step.py:286-328 applied per run), started
+ * from f = M(v) (1 + A cos(k x)) on x in [0, 2 pi / k), v in [-vmax, vmax).
+ * The sweep owns the run states; per step it stores each run's field e[nx]
+ * and its seven series.  No reference counterpart: the reference runs one
+ * simulation per process (vlapy/manager.py:35-177). */
+typedef struct vg_sweep vg_sweep;
+typedef struct vg_sweep_run {
+  int32_t nx, nv;    /* powers of two; nx in [8, 256], nv in [64, 2048] */
+  double k;          /* fundamental wavenumber (box length 2 pi / k) */
+  double amplitude;  /* density perturbation of the initial state */
+  double nu;         /* collision frequency; 0 = collisionless */
+} vg_sweep_run;
+typedef struct vg_sweep_desc {
+  int32_t n_runs;
+  int32_t collision;  /* VG_COLL_DG or VG_COLL_LB for the runs with nu > 0 */
+  double vmax, dt;
+  const vg_sweep_run* runs;  /* host [n_runs] */
+} vg_sweep_desc;
+int vg_sweep_create(const vg_sweep_desc* desc, vg_sweep** out);
+int vg_sweep_destroy(vg_sweep* sweep);
+/* total phase-space cells and total x points (the e-history row length) */
+int vg_sweep_sizes(const vg_sweep* sweep, int64_t* cells, int64_t* x_points);
+/* x offset of each run's field in an e-history row (host [n_runs]) */
+int vg_sweep_x_offsets(const vg_sweep* sweep, int64_t* out);
+/* every run back to its initial state, e = 0, t = 0 */
+int vg_sweep_reset(vg_sweep* sweep, vg_stream stream);
+/* nsteps leapfrog steps of every run.  If e_hist/series_hist are non-NULL,
+ * step i of this call is stored at row (hist_row0 + i) of e_hist
+ * [rows][x_points] and series_hist [rows][n_runs][7] (mean n, j, T, e^2,
+ * driver^2, f^2, f log f), for rows < hist_rows. */
+int vg_sweep_run_steps(vg_sweep* sweep, int32_t nsteps, double* e_hist, double* series_hist,
+                       int32_t hist_rows, int32_t hist_row0, int32_t use_graph, vg_stream stream);
+/* f = g + f0 of one run as float64 [nx][nv] and its e[nx] (DEVICE pointers) */
+int vg_sweep_read_run(vg_sweep* sweep, int32_t run, double* f_out, double* e_out, vg_stream stream);
+/* per-kernel timing of vg_sweep_run_steps (same contract as vg_profile_*) */
+int vg_sweep_profile_enable(vg_sweep* sweep, int32_t enable);
+int vg_sweep_profile_read(vg_sweep* sweep, vg_prof_entry* out, int32_t max, int32_t* n_out);
+
 /* ---- measurement ----------------------------------------------------- */
 /* Per-kernel device timing of vg_run_steps: while enabled, every kernel of
  * the step sequence is bracketed by CUDA events on the plan's stream and the
@@ -146,12 +198,6 @@ int vg_run_steps(vg_plan* plan, void* f, double* e, const vg_history* hist,
  * algorithmic DRAM bytes per launch) and clears the record.  No reference
  * counterpart (the reference only logs wall-clock per step,
  * vlapy/manager.py:144-146). */
-typedef struct vg_prof_entry {
-  char name[32];
-  int64_t launches;
-  double total_ms;
-  double bytes_per_launch;
-} vg_prof_entry;
 int vg_profile_enable(vg_plan* plan, int32_t enable);
 int vg_profile_read(vg_plan* plan, vg_prof_entry* out, int32_t max, int32_t* n_out);
 

@@ -1,0 +1,129 @@
+"""Batched sweep (vg_sweep_*) against the FP64 oracle, run by run."""
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from oracle import vlapy_oracle as vo  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib_loaded():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from vlapy_gb300 import _lib
+    _lib.load()
+
+
+def mixed_runs():
+    """All nine shape classes of the sweep workload plus a collisionless run."""
+    runs = []
+    rng = np.random.default_rng(7)
+    for nx in (32, 64, 128):
+        for nv in (256, 512, 1024):
+            runs.append(dict(nx=nx, nv=nv, k=float(rng.uniform(0.25, 0.45)),
+                             amplitude=float(10 ** rng.uniform(-4, -2)),
+                             nu=float(10 ** rng.uniform(-5, -2))))
+    runs[4]["nu"] = 0.0
+    runs.append(dict(nx=32, nv=256, k=0.3, amplitude=1e-6, nu=0.0))
+    return runs
+
+
+def oracle_run(r, nsteps, vmax=6.4, dt=0.1):
+    nx, nv, k = r["nx"], r["nv"], r["k"]
+    run = vo.OracleRun(nx, nv, 2 * np.pi / k, vmax, dt, nu=r["nu"], operator="dg")
+    dx, x, kx, inv = vo.spatial_axis(0.0, 2 * np.pi / k, nx)
+    f = vo.maxwellian(nx, nv, vmax) * (1.0 + r["amplitude"] * np.cos(k * x))[:, None]
+    f0 = vo.maxwellian(1, nv, vmax)[0]
+    e = np.zeros(nx)
+    es = []
+    for i in range(nsteps):
+        e, f = run.step(e, f, dt * i)
+        es.append(e)
+    return f, np.array(es), f0
+
+
+def test_sweep_runs_match_oracle():
+    from vlapy_gb300.sweep import Sweep
+    runs = mixed_runs()
+    sw = Sweep(runs)
+    sw.reset()
+    nsteps = 20
+    eh, sh = sw.history(nsteps)
+    sw.run_steps(nsteps, eh, sh)
+    torch.cuda.synchronize()
+    for i, r in enumerate(runs):
+        f_ref, e_ref, f0 = oracle_run(r, nsteps)
+        f, e = sw.read_run(i)
+        f = f.cpu().numpy()
+        dev = np.linalg.norm(f - f_ref) / np.linalg.norm(f_ref - f0[None, :])
+        assert dev <= 1e-4, (i, r, dev)
+        e_hist = sw.e_of(eh, i).cpu().numpy()
+        assert np.linalg.norm(e_hist - e_ref) / np.linalg.norm(e_ref) <= 1e-4, (i, r)
+        # series: mean density and field energy of the last step
+        s_last = sh[-1, i].cpu().numpy()
+        np.testing.assert_allclose(s_last[3], np.mean(e_ref[-1] ** 2), rtol=2e-4)
+        dv = 2 * 6.4 / r["nv"]
+        np.testing.assert_allclose(s_last[0], np.mean(vo.trapz(f_ref, dv, 1)), rtol=1e-9)
+
+
+def test_sweep_graph_equals_direct():
+    from vlapy_gb300.sweep import Sweep
+    runs = mixed_runs()
+    a, b = Sweep(runs), Sweep(runs)
+    a.reset()
+    b.reset()
+    ea, sa = a.history(8)
+    eb, sb = b.history(8)
+    a.run_steps(8, ea, sa)
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        b.run_steps(8, eb, sb, use_graph=True, stream=s)
+    torch.cuda.synchronize()
+    assert torch.equal(ea, eb) and torch.equal(sa, sb)
+    for i in range(len(runs)):
+        assert torch.equal(a.read_run(i)[0], b.read_run(i)[0])
+
+
+def test_sweep_config_distribution():
+    from vlapy_gb300.sweep import sweep_config
+    runs = sweep_config(4096)
+    nx = np.array([r["nx"] for r in runs])
+    nu = np.array([r["nu"] for r in runs])
+    assert set(nx) == {32, 64, 128}
+    assert 0.2 < np.mean(nu == 0.0) < 0.3
+    assert all(0.25 <= r["k"] <= 0.45 for r in runs)
+    assert all(1e-6 <= r["amplitude"] <= 1e-2 for r in runs)
+
+
+def test_sweep_landau_rates():
+    """Collisionless runs of the sweep damp at the oracle's rate (within 1%)."""
+    from vlapy_gb300.sweep import Sweep
+    ks = (0.3, 0.35, 0.4)
+    runs = [dict(nx=32, nv=512, k=k, amplitude=1e-4, nu=0.0) for k in ks]
+    sw = Sweep(runs)
+    sw.reset()
+    nsteps = 600
+    eh, sh = sw.history(nsteps)
+    sw.run_steps(nsteps, eh, sh)
+    torch.cuda.synchronize()
+    t = 0.1 * np.arange(1, nsteps + 1)
+    for i, r in enumerate(runs):
+        _, e_ref, _ = oracle_run(r, nsteps)
+        a_gpu = vo.mode_amplitude(sw.e_of(eh, i).cpu().numpy())
+        a_ref = vo.mode_amplitude(e_ref)
+        rg, wg = vo.envelope_fit(t, a_gpu, t_min=5.0)
+        rr, wr = vo.envelope_fit(t, a_ref, t_min=5.0)
+        assert abs(rg - rr) <= 0.01 * abs(rr), (r, rg, rr)
+        assert abs(wg - wr) <= 0.01 * abs(wr), (r, wg, wr)
+
+
+def test_sweep_rejects_unsupported_shapes():
+    from vlapy_gb300.sweep import Sweep
+    with pytest.raises(NotImplementedError):
+        Sweep([dict(nx=48, nv=256, k=0.3, amplitude=1e-3, nu=0.0)])
+    with pytest.raises(NotImplementedError):
+        Sweep([dict(nx=8, nv=64, k=0.3, amplitude=1e-3, nu=0.0)])

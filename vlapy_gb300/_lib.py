@@ -51,6 +51,16 @@ class VgHistory(C.Structure):
                 ("stored_f", C.c_void_p)]
 
 
+class VgSweepRun(C.Structure):
+    _fields_ = [("nx", C.c_int32), ("nv", C.c_int32), ("k", C.c_double), ("amplitude", C.c_double),
+                ("nu", C.c_double)]
+
+
+class VgSweepDesc(C.Structure):
+    _fields_ = [("n_runs", C.c_int32), ("collision", C.c_int32), ("vmax", C.c_double), ("dt", C.c_double),
+                ("runs", C.POINTER(VgSweepRun))]
+
+
 class VgProfEntry(C.Structure):
     _fields_ = [("name", C.c_char * 32), ("launches", C.c_int64), ("total_ms", C.c_double),
                 ("bytes_per_launch", C.c_double)]
@@ -74,6 +84,16 @@ EXPORTS = {
     "vg_run_steps": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(VgHistory),
                                C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32,
                                C.c_void_p]),
+    "vg_sweep_create": (C.c_int, [C.POINTER(VgSweepDesc), C.POINTER(C.c_void_p)]),
+    "vg_sweep_destroy": (C.c_int, [C.c_void_p]),
+    "vg_sweep_sizes": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    "vg_sweep_x_offsets": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
+    "vg_sweep_reset": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "vg_sweep_run_steps": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32,
+                                     C.c_int32, C.c_void_p]),
+    "vg_sweep_read_run": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "vg_sweep_profile_enable": (C.c_int, [C.c_void_p, C.c_int32]),
+    "vg_sweep_profile_read": (C.c_int, [C.c_void_p, C.POINTER(VgProfEntry), C.c_int32, C.POINTER(C.c_int32)]),
     "vg_profile_enable": (C.c_int, [C.c_void_p, C.c_int32]),
     "vg_profile_read": (C.c_int, [C.c_void_p, C.POINTER(VgProfEntry), C.c_int32,
                                   C.POINTER(C.c_int32)]),

@@ -22,6 +22,35 @@ int cuda_status(cudaError_t err, const char* what) {
   return VG_ERR_CUDA;
 }
 
+int prof_collect(ProfState* ps, int n_kinds, const char* const* names, const double* bytes_per_launch,
+                 vg_prof_entry* out, int max, int* n_out) {
+  std::vector<double> ms(n_kinds, 0.0);
+  std::vector<long long> cnt(n_kinds, 0);
+  for (auto& r : ps->recs) {
+    cudaError_t err = cudaEventSynchronize(r.e);
+    if (err != cudaSuccess) return cuda_status(err, "profile sync");
+    float t = 0.f;
+    err = cudaEventElapsedTime(&t, r.b, r.e);
+    if (err != cudaSuccess) return cuda_status(err, "profile elapsed");
+    ms[r.kind] += t;
+    cnt[r.kind] += 1;
+  }
+  ps->recs.clear();
+  ps->used = 0;
+  int n = 0;
+  for (int k = 0; k < n_kinds; ++k) {
+    if (!cnt[k] || n >= max) continue;
+    std::memset(&out[n], 0, sizeof(vg_prof_entry));
+    std::snprintf(out[n].name, sizeof(out[n].name), "%s", names[k]);
+    out[n].launches = cnt[k];
+    out[n].total_ms = ms[k];
+    out[n].bytes_per_launch = bytes_per_launch[k];
+    ++n;
+  }
+  *n_out = n;
+  return VG_OK;
+}
+
 cudaError_t ensure_smem(const void* kernel, size_t bytes) {
   static std::mutex mu;
   static std::map<std::pair<const void*, int>, size_t> done;
@@ -86,25 +115,6 @@ enum ProfKind {
 static const char* kProfNames[PK_COUNT] = {"edfdv", "vdfdx", "density", "poisson", "fp_moments", "fp_solve",
                                             "storage", "x_drift_f32", "field_f32", "row_pass_f32", "kick_f32",
                                             "store_f32"};
-
-struct ProfState {
-  bool enabled = false;
-  std::vector<cudaEvent_t> pool;
-  size_t used = 0;
-  struct Rec { int kind; cudaEvent_t b, e; };
-  std::vector<Rec> recs;
-  ~ProfState() {
-    for (cudaEvent_t ev : pool) cudaEventDestroy(ev);
-  }
-  cudaEvent_t next() {
-    if (used == pool.size()) {
-      cudaEvent_t ev;
-      if (cudaEventCreate(&ev) != cudaSuccess) return nullptr;
-      pool.push_back(ev);
-    }
-    return pool[used++];
-  }
-};
 
 // algorithmic DRAM bytes of one launch of each kind: the f traffic the
 // operation cannot avoid (read + write of f for in-place transforms, one
@@ -201,20 +211,9 @@ int require_fft_x(const vg_plan* p) {
   return VG_OK;
 }
 
-// Run one launcher, bracketed by events when profiling is on.
 template <typename Fn>
 cudaError_t prof_run(vg_plan* p, int kind, cudaStream_t s, Fn fn) {
-  auto* ps = static_cast<ProfState*>(p->prof);
-  if (!ps || !ps->enabled) return fn();
-  cudaEvent_t b = ps->next(), e = ps->next();
-  if (!b || !e) return cudaErrorMemoryAllocation;
-  cudaError_t err = cudaEventRecord(b, s);
-  if (err != cudaSuccess) return err;
-  err = fn();
-  if (err != cudaSuccess) return err;
-  err = cudaEventRecord(e, s);
-  ps->recs.push_back({kind, b, e});
-  return err;
+  return prof_call(static_cast<ProfState*>(p->prof), kind, s, fn);
 }
 
 // One FP step: moments of the operator, then the tridiagonal solve.
@@ -832,31 +831,11 @@ int vg_profile_read(vg_plan* p, vg_prof_entry* out, int32_t max, int32_t* n_out)
     set_error("null output");
     return VG_ERR_ARG;
   }
-  auto* ps = static_cast<ProfState*>(p->prof);
-  double ms[PK_COUNT] = {0};
-  int64_t cnt[PK_COUNT] = {0};
-  for (auto& r : ps->recs) {
-    VG_CHECK(cuda_status(cudaEventSynchronize(r.e), "profile sync"));
-    float t = 0.f;
-    VG_CHECK(cuda_status(cudaEventElapsedTime(&t, r.b, r.e), "profile elapsed"));
-    ms[r.kind] += t;
-    cnt[r.kind] += 1;
-  }
-  ps->recs.clear();
-  ps->used = 0;
+  double bytes[PK_COUNT];
+  for (int k = 0; k < PK_COUNT; ++k) bytes[k] = prof_bytes(p, k);
   int n = 0;
-  for (int k = 0; k < PK_COUNT; ++k) {
-    if (!cnt[k]) continue;
-    if (n < max) {
-      std::memset(&out[n], 0, sizeof(vg_prof_entry));
-      std::snprintf(out[n].name, sizeof(out[n].name), "%s", kProfNames[k]);
-      out[n].launches = cnt[k];
-      out[n].total_ms = ms[k];
-      out[n].bytes_per_launch = prof_bytes(p, k);
-    }
-    ++n;
-  }
-  *n_out = n < max ? n : max;
+  VG_CHECK(prof_collect(static_cast<ProfState*>(p->prof), PK_COUNT, kProfNames, bytes, out, max, &n));
+  *n_out = n;
   return VG_OK;
 }
 

@@ -2,6 +2,7 @@
 #pragma once
 
 #include <string>
+#include <vector>
 
 #include "vg_common.cuh"
 #include "vg_f32_plan.cuh"
@@ -51,6 +52,48 @@ struct MomSpec {
   int kind[MOM_STRIDE];
   int arg[MOM_STRIDE];  // MOM_W: row of v_pow; MOM_DG2: index of the vbar moment
 };
+
+// Per-kernel event timing shared by plans and sweeps: while enabled, each
+// launcher call is bracketed by two events on its stream.
+struct ProfState {
+  bool enabled = false;
+  std::vector<cudaEvent_t> pool;
+  size_t used = 0;
+  struct Rec {
+    int kind;
+    cudaEvent_t b, e;
+  };
+  std::vector<Rec> recs;
+  ~ProfState() {
+    for (cudaEvent_t ev : pool) cudaEventDestroy(ev);
+  }
+  cudaEvent_t next() {
+    if (used == pool.size()) {
+      cudaEvent_t ev;
+      if (cudaEventCreate(&ev) != cudaSuccess) return nullptr;
+      pool.push_back(ev);
+    }
+    return pool[used++];
+  }
+};
+
+template <typename Fn>
+cudaError_t prof_call(ProfState* ps, int kind, cudaStream_t s, Fn fn) {
+  if (!ps || !ps->enabled) return fn();
+  cudaEvent_t b = ps->next(), e = ps->next();
+  if (!b || !e) return cudaErrorMemoryAllocation;
+  cudaError_t err = cudaEventRecord(b, s);
+  if (err != cudaSuccess) return err;
+  err = fn();
+  if (err != cudaSuccess) return err;
+  err = cudaEventRecord(e, s);
+  ps->recs.push_back({kind, b, e});
+  return err;
+}
+
+// Sum the recorded launches per kind into vg_prof_entry lines (clears the record).
+int prof_collect(ProfState* ps, int n_kinds, const char* const* names, const double* bytes_per_launch,
+                 vg_prof_entry* out, int max, int* n_out);
 
 void set_error(const std::string& msg);
 int cuda_status(cudaError_t err, const char* what);

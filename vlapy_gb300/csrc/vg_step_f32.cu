@@ -10,68 +10,14 @@
 // The first half kick of a batch runs once as a row pass of its own; the
 // last step of a batch skips the trailing kick, so the state handed back is
 // the reference's f after its collision step.
-#include "vg_f32.cuh"
+#include "vg_f32_body.cuh"
 #include "vg_internal.cuh"
-#include "vg_f32_plan.cuh"
 
 namespace vg {
 
 // ---------------------------------------------------------------------------
 // x-drift of column tiles
 // ---------------------------------------------------------------------------
-
-constexpr int COL32_PAD = 1;
-
-// One column tile [NX x W] at column c0: x-drift by exp(i m (-dkx dt) v_col)
-// and the tile's trapz-weighted density partials added into dacc[x].
-// smem: W/2 padded sequences of NX complex floats.
-template <int NX, int R>
-__device__ __forceinline__ void col_tile(float* __restrict__ g, int nv, int c0, int W, double phi_unit,
-                                         const double* __restrict__ v, const cx<float>* __restrict__ tw,
-                                         unsigned char* smem, df32* dacc) {
-  constexpr int G = NX / R;
-  constexpr int LD = sp_len<float>(NX) + COL32_PAD;
-  cx<float>* s = reinterpret_cast<cx<float>*>(smem);
-  float* sf = reinterpret_cast<float*>(smem);
-  const int grp = threadIdx.x / G, t = threadIdx.x - grp * G;
-  cx<float>* sg = s + (size_t)grp * LD;
-  const float scale = 1.f / NX;
-  const int total = NX * W;
-  for (int q = threadIdx.x; q < total; q += blockDim.x) {
-    const int x = q / W, c = q - x * W;
-    sf[2 * ((c >> 1) * LD + sp<float>(x)) + (c & 1)] = g[(size_t)x * nv + c0 + c];
-  }
-  __syncthreads();
-  block_fft<float, NX, false, R>(sg, t, tw);
-  // theta(m) = m * (-dkx dt v_col): kx = m dkx on the bins m <= NX/2
-  const Ang aa = split_angle(phi_unit * v[c0 + 2 * grp]);
-  const Ang ab = split_angle(phi_unit * v[c0 + 2 * grp + 1]);
-  two_real_rotate<float>(sg, NX, t, G, [&](int m, float& ca, float& sa, float& cb, float& sb) {
-    sincos_m((float)m, aa, sa, ca);
-    sincos_m((float)m, ab, sb, cb);
-    ca *= scale;
-    sa *= scale;
-    cb *= scale;
-    sb *= scale;
-  });
-  __syncthreads();
-  block_fft<float, NX, true, R>(sg, t, tw);
-  // density partial sums (trapz weights: 1/2 at the two v end points)
-  for (int x = threadIdx.x; x < NX; x += blockDim.x) {
-    float acc = 0.f;
-    for (int c = 0; c < W; ++c) {
-      const int col = c0 + c;
-      const float w = (col == 0 || col == nv - 1) ? 0.5f : 1.f;
-      acc = fmaf(w, sf[2 * ((c >> 1) * LD + sp<float>(x)) + (c & 1)], acc);
-    }
-    dacc[x] = df_add(dacc[x], {acc, 0.f});
-  }
-  for (int q = threadIdx.x; q < total; q += blockDim.x) {
-    const int x = q / W, c = q - x * W;
-    g[(size_t)x * nv + c0 + c] = sf[2 * ((c >> 1) * LD + sp<float>(x)) + (c & 1)];
-  }
-  __syncthreads();
-}
 
 template <int NX, int R>
 __global__ void __launch_bounds__((NX / R) * col32_seqs(NX, R)) k_col_f32(
@@ -161,208 +107,6 @@ __global__ void __launch_bounds__(fft_threads<float>(NX)) k_field_f32(
 // ---------------------------------------------------------------------------
 // row pass: kick / collide / measure / kick
 // ---------------------------------------------------------------------------
-
-// rotation of one packed row pair with the delta-f background term; the 1/N of
-// the inverse transform is folded in.  ha/hb: half-angle per kv index.
-template <int N>
-__device__ __forceinline__ void kick_rotate(cx<float>* s, int t, int G, Ang ha, Ang hb,
-                                            const cx<float>* __restrict__ F0) {
-  const float sc = 1.f / N;
-  for (int k = t; k <= N / 2; k += G) {
-    float sa, ca, sb, cb;
-    sincos_m((float)k, ha, sa, ca);
-    sincos_m((float)k, hb, sb, cb);
-    // P = (1 - 2 sin^2, 2 sin cos) of the half angle; P - 1 = (-2 sin^2, 2 sin cos)
-    const float pa_m1r = -2.f * sa * sa, pa_i = 2.f * sa * ca, pa_r = 1.f + pa_m1r;
-    const float pb_m1r = -2.f * sb * sb, pb_i = 2.f * sb * cb, pb_r = 1.f + pb_m1r;
-    const cx<float> f0 = F0[k];
-    if (k == 0 || 2 * k == N) {
-      const cx<float> z = s[sp<float>(k)];
-      // real bins: only Re(P) survives
-      s[sp<float>(k)] = {(pa_r * z.x + pa_m1r * f0.x) * sc, (pb_r * z.y + pb_m1r * f0.x) * sc};
-      continue;
-    }
-    const cx<float> zk = s[sp<float>(k)], zm = s[sp<float>(N - k)];
-    const cx<float> fa = {(zk.x + zm.x) * 0.5f, (zk.y - zm.y) * 0.5f};
-    const cx<float> fb = {(zk.y + zm.y) * 0.5f, (zm.x - zk.x) * 0.5f};
-    const cx<float> ga = {(pa_r * fa.x - pa_i * fa.y + pa_m1r * f0.x - pa_i * f0.y) * sc,
-                          (pa_r * fa.y + pa_i * fa.x + pa_m1r * f0.y + pa_i * f0.x) * sc};
-    const cx<float> gb = {(pb_r * fb.x - pb_i * fb.y + pb_m1r * f0.x - pb_i * f0.y) * sc,
-                          (pb_r * fb.y + pb_i * fb.x + pb_m1r * f0.y + pb_i * f0.x) * sc};
-    s[sp<float>(k)] = {ga.x - gb.y, ga.y + gb.x};
-    s[sp<float>(N - k)] = {ga.x + gb.y, gb.x - ga.y};
-  }
-}
-
-template <int N, int R>
-__device__ __forceinline__ void kick(cx<float>* s, int t, double dkv, double dt, double ea, double eb,
-                                     const cx<float>* __restrict__ F0, const cx<float>* __restrict__ tw) {
-  constexpr int G = N / R;
-  block_fft<float, N, false, R>(s, t, tw);
-  // theta(k) = -kv_k dt e = k * (-dkv dt e); half angle for P - 1
-  const Ang ha = split_angle(-0.5 * dkv * dt * ea);
-  const Ang hb = split_angle(-0.5 * dkv * dt * eb);
-  kick_rotate<N>(s, t, G, ha, hb, F0);
-  __syncthreads();
-  block_fft<float, N, true, R>(s, t, tw);
-}
-
-// Fokker-Planck step of one row stored at x (stride 2 floats) in delta-f form.
-template <int N, int R>
-__device__ __forceinline__ void collide_row(float* x, int t, const RowConsts& rc, double nudt, int dougherty,
-                                            df32* red, float* pcr) {
-  constexpr int G = N / R;
-  // moments of g over the thread's chunk: sum w g, sum w g v, sum w g v^2
-  df32 mv[3];
-  {
-    float a0 = 0.f, a1 = 0.f, a2 = 0.f;
-#pragma unroll
-    for (int i = 0; i < R; ++i) {
-      const int j = t * R + i;
-      const float w = (j == 0 || j == N - 1) ? 0.5f : 1.f;
-      const float gv = w * x[2 * sp<float>(j)];
-      const float vj = rc.v[j];
-      a0 += gv;
-      a1 = fmaf(gv, vj, a1);
-      a2 = fmaf(gv * vj, vj, a2);
-    }
-    mv[0] = {a0, 0.f};
-    mv[1] = {a1, 0.f};
-    mv[2] = {a2, 0.f};
-  }
-  group_df_sum<3>(mv, red, G, t);
-  const double M0 = rc.dv * df_to_double(mv[0]) + rc.f0m[0];
-  const double M1 = rc.dv * df_to_double(mv[1]) + rc.f0m[1];
-  const double M2 = rc.dv * df_to_double(mv[2]) + rc.f0m[2];
-  // DG: vbar = trapz(f v), v0t^2 = trapz(f (v - vbar)^2) = M2 + vbar^2 (M0 - 2)
-  // LB: v0t^2 = trapz(f v^2), no drift
-  const double vbar = dougherty ? M1 : 0.0;
-  const double vth = dougherty ? M2 + vbar * vbar * (M0 - 2.0) : M2;
-  const float Af = (float)(-vth / rc.dv_sq);
-  const float bdiag = (float)(1.0 + nudt * (2.0 * vth / rc.dv_sq));
-  const float nu = (float)nudt;
-  const float vb = (float)vbar;
-  const float i2dv = (float)(0.5 / rc.dv);
-  // right-hand side: g - (A - I) f0 with (A - I) f0 = nudt (-vth S + Mv - vbar D)
-  const float cs = (float)(nudt * vth), cm = nu, cd = (float)(nudt * vbar);
-#pragma unroll
-  for (int i = 0; i < R; ++i) {
-    const int j = t * R + i;
-    x[2 * sp<float>(j)] -= -cs * rc.S[j] + cm * rc.Mv[j] - cd * rc.D[j];
-  }
-  __syncthreads();
-  auto lf = [&](int j) { return nu * (Af + (rc.v[j - 1] - vb) * i2dv); };
-  auto uf = [&](int j) { return nu * (Af - (rc.v[j + 1] - vb) * i2dv); };
-  partition_solve<R>(x, t, G, bdiag, lf, uf, pcr);
-}
-
-// One row-pair group of the row pass: load, [kick dt1], [collide], [moments
-// and x-mode partials], [kick dt2], store.  grp_base: this group's shared
-// memory (row32_group_bytes); macc: the CTA's mode accumulators [n_modes][N].
-template <int N, int R>
-__device__ __forceinline__ void row_pair(const RowArgs& a, int pair, unsigned char* grp_base, cx<float>* macc,
-                                         int P, int grp, int t) {
-  constexpr int G = N / R;
-  cx<float>* s = reinterpret_cast<cx<float>*>(grp_base);
-  const size_t seq_bytes = (size_t)sp_len<float>(N) * sizeof(cx<float>) + 16;
-  float* pcr = reinterpret_cast<float*>(grp_base + seq_bytes);
-  df32* red = reinterpret_cast<df32*>(grp_base + seq_bytes + 8 * G * sizeof(float));
-  const int nm = a.n_modes;
-  const int ra = 2 * pair, rb = ra + 1;
-  const bool va = ra < a.nx, vb = rb < a.nx;
-  float* ga = a.g + (size_t)ra * N;
-  float* gbp = a.g + (size_t)rb * N;
-#pragma unroll
-  for (int i = 0; i < R; ++i) {
-    const int n = t + i * G;
-    s[sp<float>(n)] = {va ? ga[n] : 0.f, vb ? gbp[n] : 0.f};
-  }
-  __syncthreads();
-  const bool kicks = a.dt1 != 0.0 || a.dt2 != 0.0;
-  const double ea = (kicks && va) ? a.e[ra] : 0.0, eb = (kicks && vb) ? a.e[rb] : 0.0;
-  if (a.dt1 != 0.0) kick<N, R>(s, t, a.rc.dkv, a.dt1, ea, eb, a.F0, a.tw);
-  float* sx = reinterpret_cast<float*>(s);
-  if (a.fp) {
-    collide_row<N, R>(sx, t, a.rc, a.nudt, a.dougherty, red, pcr);
-    collide_row<N, R>(sx + 1, t, a.rc, a.nudt, a.dougherty, red, pcr);
-  }
-  if (a.want_mom) {
-    // n, j, T, q, fv4, vN (sums of w g v^p), sum w g^2, sum w g f0, sum w f log f
-    df32 mv[9], mw[9];
-    float sa[9] = {0}, sb[9] = {0};
-#pragma unroll
-    for (int i = 0; i < R; ++i) {
-      const int j = t * R + i;
-      const float w = (j == 0 || j == N - 1) ? 0.5f : 1.f;
-      const float vj = a.rc.v[j], f0j = a.rc.f0[j];
-      const cx<float> z = s[sp<float>(j)];
-      float pa = w * z.x, pb = w * z.y;
-#pragma unroll
-      for (int p = 0; p < 6; ++p) {
-        sa[p] += pa;
-        sb[p] += pb;
-        pa *= vj;
-        pb *= vj;
-      }
-      sa[6] = fmaf(w * z.x, z.x, sa[6]);
-      sb[6] = fmaf(w * z.y, z.y, sb[6]);
-      sa[7] = fmaf(w * z.x, f0j, sa[7]);
-      sb[7] = fmaf(w * z.y, f0j, sb[7]);
-      const float fa = z.x + f0j, fb = z.y + f0j;
-      sa[8] = fmaf(w * fa, logf(fa), sa[8]);
-      sb[8] = fmaf(w * fb, logf(fb), sb[8]);
-    }
-#pragma unroll
-    for (int q = 0; q < 9; ++q) {
-      mv[q] = {sa[q], 0.f};
-      mw[q] = {sb[q], 0.f};
-    }
-    group_df_sum<9>(mv, red, G, t);
-    group_df_sum<9>(mw, red, G, t);
-    if (t == 0) {
-      for (int r = 0; r < 2; ++r) {
-        const int row = r ? rb : ra;
-        if (!(r ? vb : va)) continue;
-        const df32* m = r ? mw : mv;
-        double* out = a.mom + (size_t)row * MOM_STRIDE;
-        for (int p = 0; p < 6; ++p) out[p] = a.rc.dv * df_to_double(m[p]) + a.rc.f0m[p];
-        out[6] = a.rc.dv * (df_to_double(m[6]) + 2.0 * df_to_double(m[7])) + a.rc.f0m[6];
-        out[7] = a.rc.dv * df_to_double(m[8]);
-      }
-    }
-    // x-Fourier modes of f (the f0 part of mode 0 is added in the reduction);
-    // the groups of a CTA hold different rows but add into the same bins,
-    // so they take turns
-    if (nm > 0) {
-      for (int gq = 0; gq < P; ++gq) {
-        if (gq == grp) {
-          for (int mq = 0; mq < nm; ++mq) {
-            float swa = 0.f, cwa = 0.f, swb = 0.f, cwb = 0.f;
-            if (va) sincospif(-2.f * (float)((mq * ra) % a.nx) / (float)a.nx, &swa, &cwa);
-            if (vb) sincospif(-2.f * (float)((mq * rb) % a.nx) / (float)a.nx, &swb, &cwb);
-            for (int i = 0; i < R; ++i) {
-              const int n = t + i * G;
-              const cx<float> z = s[sp<float>(n)];
-              cx<float>& acc = macc[(size_t)mq * N + n];
-              acc.x += z.x * cwa + z.y * cwb;
-              acc.y += z.x * swa + z.y * swb;
-            }
-          }
-        }
-        __syncthreads();
-      }
-    }
-  }
-  if (a.dt2 != 0.0) kick<N, R>(s, t, a.rc.dkv, a.dt2, ea, eb, a.F0, a.tw);
-#pragma unroll
-  for (int i = 0; i < R; ++i) {
-    const int n = t + i * G;
-    const cx<float> z = s[sp<float>(n)];
-    if (va) ga[n] = z.x;
-    if (vb) gbp[n] = z.y;
-  }
-  __syncthreads();
-}
 
 template <int N, int R>
 __global__ void __launch_bounds__(row32_block(N, R)) k_row_f32(RowArgs a) {

@@ -1,0 +1,701 @@
+// Batched sweep: many independent FP32 delta-f runs of uneven shape advanced
+// together, every launch covering all runs.
+//
+// Layout in HBM: one FP32 buffer holds every run's g[nx][nv] back to back
+// (runs in their input order); fields e, 1 - n and the row moments are
+// packed the same way along x.  Runs share per-nv constants (v grid, the
+// Maxwellian background f0, its stencils and spectrum); per run only k, nu
+// and the offsets differ.  A step is four launches -- x-drift over (run,
+// tile) items, field solve over groups of runs of one nx, the fused row pass
+// over (run, row-pair group) items, and the storage of e and the series --
+// preceded once per call by the first half kick.  Kernels dispatch on the
+// item's shape to the same device bodies as the single-run path.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <vector>
+
+#include "vg_f32_body.cuh"
+#include "vg_internal.cuh"
+
+namespace vg {
+
+struct SweepRunDev {
+  int nx, nv, cls;     // cls: index of the run's nv class
+  int ntiles, W;       // column tiles of the x-drift
+  int fp;              // collide this run
+  long long g_off;     // cells before this run
+  int x_off;           // x points before this run
+  long long dp_off;    // density-partial elements (float2) before this run
+  double k, nudt;
+};
+
+constexpr int SWEEP_BLOCK = 256;
+constexpr int SWEEP_FIELD_BLOCK = 128;
+constexpr int SWEEP_MAX_CLASSES = 6;  // nv in {64, ..., 2048}
+
+__host__ __device__ constexpr int sweep_col_w(int nx) { return 2 * (SWEEP_BLOCK / (nx / col32_radix(nx))); }
+
+struct SweepConsts {
+  RowConsts rc[SWEEP_MAX_CLASSES];
+  const cx<float>* F0[SWEEP_MAX_CLASSES];
+  const double* v64[SWEEP_MAX_CLASSES];
+  double c0[SWEEP_MAX_CLASSES];
+};
+
+// ---------------------------------------------------------------------------
+// kernels
+// ---------------------------------------------------------------------------
+
+template <int NX>
+__device__ __forceinline__ void sweep_col_item(const SweepRunDev& r, int tile, float* g, const SweepConsts& sc,
+                                               double dt, const cx<float>* tw, float2* dpart, unsigned char* smem) {
+  constexpr int R = col32_radix(NX);
+  constexpr int W = sweep_col_w(NX);
+  constexpr int LD = sp_len<float>(NX) + COL32_PAD;
+  df32* dacc = reinterpret_cast<df32*>(smem + (size_t)(W / 2) * LD * sizeof(cx<float>));
+  for (int x = threadIdx.x; x < NX; x += blockDim.x) dacc[x] = {0.f, 0.f};
+  __syncthreads();
+  col_tile<NX, R>(g + r.g_off, r.nv, tile * W, W, -r.k * dt, sc.v64[r.cls], tw, smem, dacc);
+  float2* out = dpart + r.dp_off + (size_t)tile * NX;
+  for (int x = threadIdx.x; x < NX; x += blockDim.x) out[x] = make_float2(dacc[x].hi, dacc[x].lo);
+}
+
+__global__ void __launch_bounds__(SWEEP_BLOCK) k_sweep_col(const SweepRunDev* __restrict__ runs,
+                                                           const int2* __restrict__ items, float* g,
+                                                           const SweepConsts* __restrict__ scp, double dt,
+                                                           const cx<float>* __restrict__ tw, float2* dpart) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int2 it = items[blockIdx.x];
+  const SweepRunDev r = runs[it.x];
+  const SweepConsts& sc = *scp;
+  switch (r.nx) {
+    case 8: sweep_col_item<8>(r, it.y, g, sc, dt, tw, dpart, smem_raw); break;
+    case 16: sweep_col_item<16>(r, it.y, g, sc, dt, tw, dpart, smem_raw); break;
+    case 32: sweep_col_item<32>(r, it.y, g, sc, dt, tw, dpart, smem_raw); break;
+    case 64: sweep_col_item<64>(r, it.y, g, sc, dt, tw, dpart, smem_raw); break;
+    case 128: sweep_col_item<128>(r, it.y, g, sc, dt, tw, dpart, smem_raw); break;
+    default: sweep_col_item<256>(r, it.y, g, sc, dt, tw, dpart, smem_raw); break;
+  }
+}
+
+// field solve of up to SWEEP_FIELD_BLOCK/G runs of one nx per CTA
+template <int NX>
+__device__ __forceinline__ void sweep_field_runs(const SweepRunDev* __restrict__ runs, int first, int count,
+                                                 const SweepConsts& sc, const float2* __restrict__ dpart,
+                                                 const cx<float>* __restrict__ tw, double* __restrict__ e,
+                                                 unsigned char* smem) {
+  constexpr int G = fft_threads<float>(NX);
+  const int grp = threadIdx.x / G, t = threadIdx.x - grp * G;
+  cx<float>* s = reinterpret_cast<cx<float>*>(smem) + (size_t)grp * sp_len<float>(NX);
+  const bool valid = grp < count;
+  const SweepRunDev r = runs[valid ? first + grp : first];
+  const double dv = sc.rc[r.cls].dv, c0 = sc.c0[r.cls];
+  for (int x = t; x < NX; x += G) {
+    df32 acc = {0.f, 0.f};
+    if (valid)
+      for (int p = 0; p < r.ntiles; ++p) {
+        const float2 q = dpart[r.dp_off + (size_t)p * NX + x];
+        acc = df_add(acc, {q.x, q.y});
+      }
+    s[sp<float>(x)] = {valid ? (float)(-(dv * df_to_double(acc)) - c0) : 0.f, 0.f};
+  }
+  __syncthreads();
+  block_fft<float, NX, false>(s, t, tw);
+  const float scale = 1.f / NX;
+  for (int m = t; m < NX; m += G) {
+    // 1 / kx with kx = 2 pi fftfreq(nx, dx) = m' k, the zero mode removed
+    const int mm = (m < NX / 2) ? m : m - NX;
+    const float ik = (m == 0) ? 0.f : (float)(1.0 / ((double)mm * r.k)) * scale;
+    const cx<float> z = s[sp<float>(m)];
+    s[sp<float>(m)] = {-ik * z.y, ik * z.x};
+  }
+  __syncthreads();
+  block_fft<float, NX, true>(s, t, tw);
+  if (valid)
+    for (int x = t; x < NX; x += G) e[r.x_off + x] = (double)s[sp<float>(x)].x;
+}
+
+__global__ void __launch_bounds__(SWEEP_FIELD_BLOCK) k_sweep_field(const SweepRunDev* __restrict__ runs,
+                                                                   const int4* __restrict__ items,
+                                                                   const SweepConsts* __restrict__ scp,
+                                                                   const float2* __restrict__ dpart,
+                                                                   const cx<float>* __restrict__ tw,
+                                                                   double* __restrict__ e) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int4 it = items[blockIdx.x];  // (nx, first run, count, -)
+  const SweepConsts& sc = *scp;
+  switch (it.x) {
+    case 8: sweep_field_runs<8>(runs, it.y, it.z, sc, dpart, tw, e, smem_raw); break;
+    case 16: sweep_field_runs<16>(runs, it.y, it.z, sc, dpart, tw, e, smem_raw); break;
+    case 32: sweep_field_runs<32>(runs, it.y, it.z, sc, dpart, tw, e, smem_raw); break;
+    case 64: sweep_field_runs<64>(runs, it.y, it.z, sc, dpart, tw, e, smem_raw); break;
+    case 128: sweep_field_runs<128>(runs, it.y, it.z, sc, dpart, tw, e, smem_raw); break;
+    default: sweep_field_runs<256>(runs, it.y, it.z, sc, dpart, tw, e, smem_raw); break;
+  }
+}
+
+struct SweepRowArgs {
+  float* g;
+  const double* e;
+  double* mom;
+  double dt1, dt2;
+  int fp, want_mom, dougherty;
+  const cx<float>* tw;
+};
+
+template <int N>
+__device__ __forceinline__ void sweep_row_item(const SweepRunDev& r, int pg, const SweepRowArgs& sa,
+                                               const SweepConsts& sc, unsigned char* smem) {
+  constexpr int R = row32_radix(N);
+  constexpr int G = N / R;
+  constexpr int P = SWEEP_BLOCK / G;
+  const int grp = threadIdx.x / G, t = threadIdx.x - grp * G;
+  RowArgs a;
+  a.g = sa.g + r.g_off;
+  a.nx = r.nx;
+  a.e = sa.e + r.x_off;
+  a.dt1 = sa.dt1;
+  a.dt2 = sa.dt2;
+  a.fp = sa.fp && r.fp;
+  a.dougherty = sa.dougherty;
+  a.nudt = r.nudt;
+  a.want_mom = sa.want_mom;
+  a.mom = sa.mom + (size_t)r.x_off * MOM_STRIDE;
+  a.n_modes = 0;
+  a.mpart = nullptr;
+  a.F0 = sc.F0[r.cls];
+  a.tw = sa.tw;
+  a.rc = sc.rc[r.cls];
+  row_pair<N, R>(a, pg * P + grp, smem + (size_t)grp * row32_group_bytes(N, R), nullptr, P, grp, t);
+}
+
+__global__ void __launch_bounds__(SWEEP_BLOCK) k_sweep_row(const SweepRunDev* __restrict__ runs,
+                                                           const int2* __restrict__ items, SweepRowArgs sa,
+                                                           const SweepConsts* __restrict__ scp) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int2 it = items[blockIdx.x];
+  const SweepRunDev r = runs[it.x];
+  const SweepConsts& sc = *scp;
+  switch (r.nv) {
+    case 64: sweep_row_item<64>(r, it.y, sa, sc, smem_raw); break;
+    case 128: sweep_row_item<128>(r, it.y, sa, sc, smem_raw); break;
+    case 256: sweep_row_item<256>(r, it.y, sa, sc, smem_raw); break;
+    case 512: sweep_row_item<512>(r, it.y, sa, sc, smem_raw); break;
+    case 1024: sweep_row_item<1024>(r, it.y, sa, sc, smem_raw); break;
+    default: sweep_row_item<2048>(r, it.y, sa, sc, smem_raw); break;
+  }
+}
+
+// e history row and the seven series of every run (one CTA per run)
+__global__ void __launch_bounds__(128) k_sweep_store(const SweepRunDev* __restrict__ runs, int n_runs,
+                                                     const double* __restrict__ mom, const double* __restrict__ e,
+                                                     double* __restrict__ e_row, double* __restrict__ s_row) {
+  __shared__ df32 red[4 * 7];
+  const SweepRunDev r = runs[blockIdx.x];
+  df32 acc[7];
+  for (int q = 0; q < 7; ++q) acc[q] = {0.f, 0.f};
+  for (int x = threadIdx.x; x < r.nx; x += blockDim.x) {
+    const double ex = e[r.x_off + x];
+    if (e_row) e_row[r.x_off + x] = ex;
+    const double* m = mom + (size_t)(r.x_off + x) * MOM_STRIDE;
+    const double src[7] = {m[0], m[1], m[2], ex * ex, 0.0, m[6], m[7]};
+    for (int q = 0; q < 7; ++q) {
+      const float hi = (float)src[q];
+      acc[q] = df_add(acc[q], {hi, (float)(src[q] - (double)hi)});
+    }
+  }
+  block_df_sum<7>(acc, red);
+  if (s_row && threadIdx.x < 7) s_row[(size_t)blockIdx.x * 7 + threadIdx.x] = df_to_double(acc[threadIdx.x]) / r.nx;
+}
+
+// initial state g = A cos(k x_j) M(v) (the x-mean of f = M (1 + A cos k x) is M)
+__global__ void k_sweep_init(const SweepRunDev* __restrict__ runs, const double* __restrict__ amp,
+                             const SweepConsts* __restrict__ scp, float* __restrict__ g, double* __restrict__ e) {
+  const SweepRunDev r = runs[blockIdx.x];
+  const double A = amp[blockIdx.x];
+  const float* f0 = scp->rc[r.cls].f0;
+  const size_t n = (size_t)r.nx * r.nv;
+  for (size_t q = threadIdx.x; q < n; q += blockDim.x) {
+    const int x = (int)(q / r.nv), vj = (int)(q % r.nv);
+    // k x_j = pi (2 j + 1) / nx on the cell-centred grid of [0, 2 pi / k)
+    const double c = cospi((2.0 * x + 1.0) / (double)r.nx);
+    g[r.g_off + q] = (float)(A * c * (double)f0[vj]);
+  }
+  for (int x = threadIdx.x; x < r.nx; x += blockDim.x) e[r.x_off + x] = 0.0;
+}
+
+__global__ void k_sweep_read(const SweepRunDev* __restrict__ runs, int run, const SweepConsts* __restrict__ scp,
+                             const float* __restrict__ g, const double* __restrict__ f0d, const double* __restrict__ e,
+                             double* __restrict__ f_out, double* __restrict__ e_out) {
+  const SweepRunDev r = runs[run];
+  const size_t n = (size_t)r.nx * r.nv;
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x)
+    if (f_out) f_out[q] = (double)g[r.g_off + q] + f0d[q % r.nv];
+  if (e_out && blockIdx.x == 0)
+    for (int x = threadIdx.x; x < r.nx; x += blockDim.x) e_out[x] = e[r.x_off + x];
+}
+
+}  // namespace vg
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+
+using namespace vg;
+
+struct vg_sweep {
+  int n_runs, collision;
+  double vmax, dt;
+  long long cells;
+  int x_points;
+  std::vector<SweepRunDev> runs_h;
+  std::vector<double> amp_h;
+  std::vector<int> nv_of_class;
+  std::vector<void*> owned;  // device allocations freed at destroy
+  // device
+  SweepRunDev* runs;
+  SweepRunDev* field_runs;  // runs ordered as the field items address them
+  double* amp;
+  SweepConsts consts_h;
+  SweepConsts* consts;
+  float* g;
+  double* e;
+  double* mom;
+  float2* dpart;
+  cx<float>* tw32;
+  cx<double>* tw64;
+  std::vector<double*> f0d;  // per nv class: FP64 background
+  int2* col_items;
+  int n_col;
+  int4* field_items;
+  int n_field;
+  int2* row_items;
+  int n_row;
+  size_t col_smem, field_smem, row_smem;
+  std::map<std::tuple<int, const void*, const void*, int, int, cudaStream_t>, cudaGraphExec_t> graphs;
+  ProfState prof;
+};
+
+namespace {
+
+#define SW_CHECK(expr)            \
+  do {                            \
+    int _st = (expr);             \
+    if (_st != VG_OK) return _st; \
+  } while (0)
+
+template <typename T>
+int sw_alloc(vg_sweep* s, T** dst, size_t n, const void* src, const char* what) {
+  *dst = nullptr;
+  cudaError_t err = cudaMalloc(reinterpret_cast<void**>(dst), std::max<size_t>(n, 1) * sizeof(T));
+  if (err != cudaSuccess) return cuda_status(err, what);
+  s->owned.push_back(*dst);
+  if (src) err = cudaMemcpy(*dst, src, n * sizeof(T), cudaMemcpyHostToDevice);
+  else err = cudaMemset(*dst, 0, std::max<size_t>(n, 1) * sizeof(T));
+  return cuda_status(err, what);
+}
+
+void host_fft_sw(std::vector<double>& re, std::vector<double>& im) {
+  const size_t n = re.size();
+  for (size_t i = 1, j = 0; i < n; ++i) {
+    size_t bit = n >> 1;
+    for (; j & bit; bit >>= 1) j ^= bit;
+    j ^= bit;
+    if (i < j) {
+      std::swap(re[i], re[j]);
+      std::swap(im[i], im[j]);
+    }
+  }
+  for (size_t len = 2; len <= n; len <<= 1) {
+    const double ang = -2.0 * M_PI / (double)len;
+    for (size_t i = 0; i < n; i += len)
+      for (size_t k = 0; k < len / 2; ++k) {
+        const double c = std::cos(ang * k), sn = std::sin(ang * k);
+        const double ur = re[i + k], ui = im[i + k];
+        const double vr = re[i + k + len / 2] * c - im[i + k + len / 2] * sn;
+        const double vi = re[i + k + len / 2] * sn + im[i + k + len / 2] * c;
+        re[i + k] = ur + vr;
+        im[i + k] = ui + vi;
+        re[i + k + len / 2] = ur - vr;
+        im[i + k + len / 2] = ui - vi;
+      }
+  }
+}
+
+// Per-nv constants: the reference's cell-centred grid (linspace of
+// vlapy/initializers.py:66), the trapz-normalised Maxwellian background, its
+// collision stencils, spectrum and moments.
+int sweep_class(vg_sweep* s, int cls, int nv) {
+  const double vmax = s->vmax;
+  const double dv = 2.0 * vmax / nv;
+  std::vector<double> v(nv), f0(nv);
+  const double lo = -vmax + dv / 2.0, hi = vmax - dv / 2.0, step = (hi - lo) / (nv - 1);
+  for (int j = 0; j < nv; ++j) v[j] = lo + j * step;
+  v[nv - 1] = hi;
+  double norm = 0.0;
+  for (int j = 0; j < nv; ++j) {
+    f0[j] = std::exp(-(v[j] * v[j]) / 2.0);
+    norm += ((j == 0 || j == nv - 1) ? 0.5 : 1.0) * f0[j];
+  }
+  norm *= dv;
+  for (int j = 0; j < nv; ++j) f0[j] /= norm;
+  const double dv2 = dv * dv;
+  std::vector<float> v32(nv), f32v(nv), S(nv), Mv(nv), D(nv);
+  double mom[7] = {0, 0, 0, 0, 0, 0, 0};
+  for (int j = 0; j < nv; ++j) {
+    const double fm = j > 0 ? f0[j - 1] : 0.0, fp = j < nv - 1 ? f0[j + 1] : 0.0;
+    const double vm = j > 0 ? v[j - 1] : 0.0, vp = j < nv - 1 ? v[j + 1] : 0.0;
+    S[j] = (float)((fm - 2.0 * f0[j] + fp) / dv2);
+    Mv[j] = (float)((vm * fm - vp * fp) / (2.0 * dv));
+    D[j] = (float)((fm - fp) / (2.0 * dv));
+    v32[j] = (float)v[j];
+    f32v[j] = (float)f0[j];
+    const double w = (j == 0 || j == nv - 1) ? 0.5 : 1.0;
+    double p = 1.0;
+    for (int k = 0; k < 6; ++k) {
+      mom[k] += w * f0[j] * p;
+      p *= v[j];
+    }
+    mom[6] += w * f0[j] * f0[j];
+  }
+  for (int k = 0; k < 7; ++k) mom[k] *= dv;
+  std::vector<double> re(f0), im(nv, 0.0);
+  host_fft_sw(re, im);
+  std::vector<cx<float>> F0(nv / 2 + 1);
+  for (int k = 0; k <= nv / 2; ++k) F0[k] = {(float)re[k], (float)im[k]};
+  float *dv32, *df0, *dS, *dM, *dD;
+  cx<float>* dF0;
+  double *dv64, *df064;
+  SW_CHECK(sw_alloc(s, &dv32, nv, v32.data(), "sweep constants"));
+  SW_CHECK(sw_alloc(s, &df0, nv, f32v.data(), "sweep constants"));
+  SW_CHECK(sw_alloc(s, &dS, nv, S.data(), "sweep constants"));
+  SW_CHECK(sw_alloc(s, &dM, nv, Mv.data(), "sweep constants"));
+  SW_CHECK(sw_alloc(s, &dD, nv, D.data(), "sweep constants"));
+  SW_CHECK(sw_alloc(s, &dF0, F0.size(), F0.data(), "sweep constants"));
+  SW_CHECK(sw_alloc(s, &dv64, nv, v.data(), "sweep constants"));
+  SW_CHECK(sw_alloc(s, &df064, nv, f0.data(), "sweep constants"));
+  RowConsts& rc = s->consts_h.rc[cls];
+  rc.v = dv32;
+  rc.f0 = df0;
+  rc.S = dS;
+  rc.Mv = dM;
+  rc.D = dD;
+  rc.dv = dv;
+  rc.dv_sq = dv2;
+  rc.dkv = 2.0 * M_PI / (nv * dv);
+  for (int k = 0; k < 7; ++k) rc.f0m[k] = mom[k];
+  s->consts_h.F0[cls] = dF0;
+  s->consts_h.v64[cls] = dv64;
+  s->consts_h.c0[cls] = mom[0] - 1.0;
+  s->f0d[cls] = df064;
+  return VG_OK;
+}
+
+void free_sweep(vg_sweep* s) {
+  if (!s) return;
+  for (auto& kv : s->graphs) cudaGraphExecDestroy(kv.second);
+  for (void* p : s->owned)
+    if (p) cudaFree(p);
+  delete s;
+}
+
+enum SweepProfKind { SK_KICK = 0, SK_X_DRIFT, SK_FIELD, SK_ROW, SK_STORE, SK_COUNT };
+const char* const kSweepNames[SK_COUNT] = {"sweep_kick", "sweep_x_drift", "sweep_field", "sweep_row_pass",
+                                          "sweep_store"};
+
+int sweep_sequence(vg_sweep* s, int nsteps, double* e_hist, double* s_hist, int rows, int row0,
+                   cudaStream_t st) {
+  const double dt = s->dt;
+  const int dg = s->collision == VG_COLL_DG;
+  auto row = [&](double dt1, double dt2, int fp, int mom, int kind) {
+    SweepRowArgs a;
+    a.g = s->g;
+    a.e = s->e;
+    a.mom = s->mom;
+    a.dt1 = dt1;
+    a.dt2 = dt2;
+    a.fp = fp;
+    a.want_mom = mom;
+    a.dougherty = dg;
+    a.tw = s->tw32;
+    return cuda_status(prof_call(&s->prof, kind, st, [&] {
+                         k_sweep_row<<<s->n_row, SWEEP_BLOCK, s->row_smem, st>>>(s->row_items ? s->runs : nullptr,
+                                                                                  s->row_items, a, s->consts);
+                         return cudaGetLastError();
+                       }),
+                       "sweep row pass");
+  };
+  SW_CHECK(row(0.5 * dt, 0.0, 0, 0, SK_KICK));
+  for (int k = 0; k < nsteps; ++k) {
+    SW_CHECK(cuda_status(prof_call(&s->prof, SK_X_DRIFT, st, [&] {
+                           k_sweep_col<<<s->n_col, SWEEP_BLOCK, s->col_smem, st>>>(s->runs, s->col_items, s->g,
+                                                                                    s->consts, dt, s->tw32,
+                                                                                    s->dpart);
+                           return cudaGetLastError();
+                         }),
+                         "sweep x drift"));
+    SW_CHECK(cuda_status(prof_call(&s->prof, SK_FIELD, st, [&] {
+                           k_sweep_field<<<s->n_field, SWEEP_FIELD_BLOCK, s->field_smem, st>>>(
+                               s->field_runs, s->field_items, s->consts, s->dpart, s->tw32, s->e);
+                           return cudaGetLastError();
+                         }),
+                         "sweep field"));
+    const int r = row0 + k;
+    const bool store = (e_hist || s_hist) && r >= 0 && r < rows;
+    SW_CHECK(row(0.5 * dt, (k + 1 < nsteps) ? 0.5 * dt : 0.0, 1, store ? 1 : 0, SK_ROW));
+    if (store) {
+      double* er = e_hist ? e_hist + (size_t)r * s->x_points : nullptr;
+      double* sr = s_hist ? s_hist + (size_t)r * s->n_runs * 7 : nullptr;
+      SW_CHECK(cuda_status(prof_call(&s->prof, SK_STORE, st, [&] {
+                             k_sweep_store<<<s->n_runs, 128, 0, st>>>(s->runs, s->n_runs, s->mom, s->e, er, sr);
+                             return cudaGetLastError();
+                           }),
+                           "sweep store"));
+    }
+  }
+  return VG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int vg_sweep_create(const vg_sweep_desc* d, vg_sweep** out) {
+  if (!d || !out || d->n_runs <= 0 || !d->runs || !(d->vmax > 0.0)) {
+    set_error("bad sweep descriptor");
+    return VG_ERR_ARG;
+  }
+  if (d->collision != VG_COLL_DG && d->collision != VG_COLL_LB) {
+    set_error("sweep collision operator must be VG_COLL_DG or VG_COLL_LB");
+    return VG_ERR_ARG;
+  }
+  *out = nullptr;
+  vg_sweep* s = new vg_sweep();
+  s->n_runs = d->n_runs;
+  s->collision = d->collision;
+  s->vmax = d->vmax;
+  s->dt = d->dt;
+  std::memset(&s->consts_h, 0, sizeof(SweepConsts));
+  std::map<int, int> cls_of;
+  long long cells = 0, dp = 0;
+  int xoff = 0;
+  for (int i = 0; i < d->n_runs; ++i) {
+    const vg_sweep_run& q = d->runs[i];
+    if (!is_pow2(q.nx) || !is_pow2(q.nv) || q.nx < 8 || q.nx > 256 || q.nv < 64 || q.nv > 2048 ||
+        q.nv < sweep_col_w(q.nx) || !(q.k > 0.0) || !(q.nu >= 0.0)) {
+      set_error("sweep run " + std::to_string(i) + ": needs power-of-two nx in [8, 256], nv in [64, 2048], " +
+                "nv >= the column tile width 4096/nx, k > 0 and nu >= 0");
+      free_sweep(s);
+      return VG_ERR_UNSUPPORTED;
+    }
+    if (!cls_of.count(q.nv)) {
+      if ((int)cls_of.size() == SWEEP_MAX_CLASSES) {
+        set_error("too many distinct nv in one sweep");
+        free_sweep(s);
+        return VG_ERR_UNSUPPORTED;
+      }
+      const int c = (int)cls_of.size();
+      cls_of[q.nv] = c;
+      s->nv_of_class.push_back(q.nv);
+    }
+    SweepRunDev r;
+    r.nx = q.nx;
+    r.nv = q.nv;
+    r.cls = cls_of[q.nv];
+    r.W = sweep_col_w(q.nx);
+    r.ntiles = q.nv / r.W;
+    r.fp = q.nu > 0.0;
+    r.g_off = cells;
+    r.x_off = xoff;
+    r.dp_off = dp;
+    r.k = q.k;
+    r.nudt = q.nu * d->dt;
+    cells += (long long)q.nx * q.nv;
+    xoff += q.nx;
+    dp += (long long)r.ntiles * q.nx;
+    s->runs_h.push_back(r);
+    s->amp_h.push_back(q.amplitude);
+  }
+  s->cells = cells;
+  s->x_points = xoff;
+  s->f0d.resize(s->nv_of_class.size());
+  int st = VG_OK;
+#define SW_TRY(expr)   \
+  do {                 \
+    st = (expr);       \
+    if (st != VG_OK) { \
+      free_sweep(s);   \
+      return st;       \
+    }                  \
+  } while (0)
+  for (size_t c = 0; c < s->nv_of_class.size(); ++c) SW_TRY(sweep_class(s, (int)c, s->nv_of_class[c]));
+  SW_TRY(sw_alloc(s, &s->runs, s->runs_h.size(), s->runs_h.data(), "sweep runs"));
+  SW_TRY(sw_alloc(s, &s->amp, s->amp_h.size(), s->amp_h.data(), "sweep runs"));
+  SW_TRY(sw_alloc(s, &s->consts, 1, &s->consts_h, "sweep constants"));
+  SW_TRY(sw_alloc<float>(s, &s->g, (size_t)cells, nullptr, "sweep state"));
+  SW_TRY(sw_alloc<double>(s, &s->e, (size_t)xoff, nullptr, "sweep fields"));
+  SW_TRY(sw_alloc<double>(s, &s->mom, (size_t)xoff * MOM_STRIDE, nullptr, "sweep moments"));
+  SW_TRY(sw_alloc<float2>(s, &s->dpart, (size_t)dp, nullptr, "sweep density partials"));
+  SW_TRY(sw_alloc<cx<double>>(s, &s->tw64, FFT_NMAX, nullptr, "twiddles"));
+  SW_TRY(sw_alloc<cx<float>>(s, &s->tw32, FFT_NMAX, nullptr, "twiddles"));
+  {
+    vg_plan tmp;
+    std::memset(&tmp, 0, sizeof(tmp));
+    tmp.tw64 = s->tw64;
+    tmp.tw32 = s->tw32;
+    SW_TRY(cuda_status(launch_twiddles(tmp, 0), "twiddles"));
+  }
+  // work lists and shared-memory sizes
+  std::vector<int2> col, row;
+  std::vector<int4> field;
+  std::vector<SweepRunDev> field_runs;
+  size_t col_smem = 0, row_smem = 0, field_smem = 0;
+  std::map<int, std::vector<int>> by_nx;
+  for (int i = 0; i < s->n_runs; ++i) {
+    const SweepRunDev& r = s->runs_h[i];
+    for (int t = 0; t < r.ntiles; ++t) col.push_back(make_int2(i, t));
+    const int G = r.nv / row32_radix(r.nv);
+    const int P = SWEEP_BLOCK / G;
+    for (int pg = 0; pg * P < r.nx / 2; ++pg) row.push_back(make_int2(i, pg));
+    by_nx[r.nx].push_back(i);
+    col_smem = std::max(col_smem, (size_t)(r.W / 2) * (sp_len<float>(r.nx) + COL32_PAD) * sizeof(cx<float>) +
+                                      (size_t)r.nx * sizeof(df32));
+    row_smem = std::max(row_smem, (size_t)P * row32_group_bytes(r.nv, row32_radix(r.nv)));
+  }
+  for (auto& kv : by_nx) {
+    const int nx = kv.first;
+    const int per = SWEEP_FIELD_BLOCK / fft_threads<float>(nx);
+    field_smem = std::max(field_smem, (size_t)per * sp_len<float>(nx) * sizeof(cx<float>));
+    const auto& ids = kv.second;
+    for (size_t b = 0; b < ids.size(); b += per) {
+      const int cnt = (int)std::min<size_t>(per, ids.size() - b);
+      field.push_back(make_int4(nx, (int)field_runs.size(), cnt, 0));
+      for (int q = 0; q < cnt; ++q) field_runs.push_back(s->runs_h[ids[b + q]]);
+    }
+  }
+  SW_TRY(sw_alloc(s, &s->col_items, col.size(), col.data(), "sweep work list"));
+  SW_TRY(sw_alloc(s, &s->row_items, row.size(), row.data(), "sweep work list"));
+  SW_TRY(sw_alloc(s, &s->field_items, field.size(), field.data(), "sweep work list"));
+  SW_TRY(sw_alloc(s, &s->field_runs, field_runs.size(), field_runs.data(), "sweep work list"));
+  s->n_col = (int)col.size();
+  s->n_row = (int)row.size();
+  s->n_field = (int)field.size();
+  s->col_smem = col_smem;
+  s->row_smem = row_smem;
+  s->field_smem = field_smem;
+  SW_TRY(cuda_status(ensure_smem((const void*)k_sweep_col, col_smem), "sweep smem"));
+  SW_TRY(cuda_status(ensure_smem((const void*)k_sweep_row, row_smem), "sweep smem"));
+  SW_TRY(cuda_status(ensure_smem((const void*)k_sweep_field, field_smem), "sweep smem"));
+  SW_TRY(cuda_status(cudaDeviceSynchronize(), "sweep setup"));
+#undef SW_TRY
+  *out = s;
+  return VG_OK;
+}
+
+int vg_sweep_destroy(vg_sweep* s) {
+  if (!s) return VG_OK;
+  cudaDeviceSynchronize();
+  free_sweep(s);
+  return VG_OK;
+}
+
+int vg_sweep_sizes(const vg_sweep* s, int64_t* cells, int64_t* x_points) {
+  if (!s) {
+    set_error("null sweep");
+    return VG_ERR_ARG;
+  }
+  if (cells) *cells = s->cells;
+  if (x_points) *x_points = s->x_points;
+  return VG_OK;
+}
+
+int vg_sweep_x_offsets(const vg_sweep* s, int64_t* out) {
+  if (!s || !out) {
+    set_error("null sweep or output");
+    return VG_ERR_ARG;
+  }
+  for (int i = 0; i < s->n_runs; ++i) out[i] = s->runs_h[i].x_off;
+  return VG_OK;
+}
+
+int vg_sweep_reset(vg_sweep* s, vg_stream stream) {
+  if (!s) {
+    set_error("null sweep");
+    return VG_ERR_ARG;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  k_sweep_init<<<s->n_runs, 256, 0, st>>>(s->runs, s->amp, s->consts, s->g, s->e);
+  return cuda_status(cudaGetLastError(), "sweep reset");
+}
+
+int vg_sweep_run_steps(vg_sweep* s, int32_t nsteps, double* e_hist, double* series_hist, int32_t hist_rows,
+                       int32_t hist_row0, int32_t use_graph, vg_stream stream) {
+  if (!s || nsteps < 0 || hist_rows < 0) {
+    set_error("null sweep or negative counts");
+    return VG_ERR_ARG;
+  }
+  if (nsteps == 0) return VG_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (s->prof.enabled || !use_graph) return sweep_sequence(s, nsteps, e_hist, series_hist, hist_rows, hist_row0, st);
+  if (st == 0) {
+    set_error("graph mode needs a non-default stream");
+    return VG_ERR_ARG;
+  }
+  const auto key = std::make_tuple(nsteps, (const void*)e_hist, (const void*)series_hist, hist_rows, hist_row0, st);
+  auto it = s->graphs.find(key);
+  if (it == s->graphs.end()) {
+    SW_CHECK(cuda_status(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed), "begin capture"));
+    const int rc = sweep_sequence(s, nsteps, e_hist, series_hist, hist_rows, hist_row0, st);
+    cudaGraph_t graph = nullptr;
+    cudaError_t err = cudaStreamEndCapture(st, &graph);
+    if (rc != VG_OK) {
+      if (graph) cudaGraphDestroy(graph);
+      return rc;
+    }
+    SW_CHECK(cuda_status(err, "end capture"));
+    cudaGraphExec_t exec = nullptr;
+    err = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    SW_CHECK(cuda_status(err, "graph instantiate"));
+    it = s->graphs.emplace(key, exec).first;
+  }
+  return cuda_status(cudaGraphLaunch(it->second, st), "graph launch");
+}
+
+int vg_sweep_read_run(vg_sweep* s, int32_t run, double* f_out, double* e_out, vg_stream stream) {
+  if (!s || run < 0 || run >= s->n_runs) {
+    set_error("null sweep or run index out of range");
+    return VG_ERR_ARG;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  const SweepRunDev& r = s->runs_h[run];
+  k_sweep_read<<<64, 256, 0, st>>>(s->runs, run, s->consts, s->g, s->f0d[r.cls], s->e, f_out, e_out);
+  return cuda_status(cudaGetLastError(), "sweep read");
+}
+
+int vg_sweep_profile_enable(vg_sweep* s, int32_t enable) {
+  if (!s) {
+    set_error("null sweep");
+    return VG_ERR_ARG;
+  }
+  s->prof.enabled = enable != 0;
+  return VG_OK;
+}
+
+int vg_sweep_profile_read(vg_sweep* s, vg_prof_entry* out, int32_t max, int32_t* n_out) {
+  if (!s || !n_out || (max > 0 && !out)) {
+    set_error("null sweep or output");
+    return VG_ERR_ARG;
+  }
+  const double cells = (double)s->cells;
+  const double bytes[SK_COUNT] = {8.0 * cells, 8.0 * cells, 8.0 * 2.0 * s->x_points, 8.0 * cells,
+                                  8.0 * 9.0 * s->x_points};
+  int n = 0;
+  SW_CHECK(prof_collect(&s->prof, SK_COUNT, kSweepNames, bytes, out, max, &n));
+  *n_out = n;
+  return VG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,120 @@
+"""Batched parameter sweep: thousands of independent VlaPy runs on one GPU.
+
+Each run is the reference's leapfrog step (exponential advection in x and v,
+spectral Poisson, the Dougherty or Lenard-Bernstein collision step for nu > 0;
+vlapy/core/step.py:286-328) from f = M(v) (1 + A cos(k x)) on x in [0, 2 pi/k),
+v in [-vmax, vmax), in the FP32 delta-f arithmetic of the GB300 step.  The
+reference runs one simulation per process; here every kernel launch of a step
+covers all runs (libvlagpu vg_sweep_*), and a whole batch of steps replays as
+one CUDA graph.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import check
+from .plan import _prof_dict, ptr, require_cuda, stream_handle
+
+SERIES = ("mean_n", "mean_j", "mean_T", "mean_e2", "mean_de2", "mean_f2", "mean_flogf")
+
+
+def sweep_config(n_runs=4096, seed=20261203, nx_choices=(32, 64, 128), nv_choices=(256, 512, 1024),
+                 k_range=(0.25, 0.45), log_amp=(-6.0, -2.0), log_nu=(-5.0, -2.0), p_collisionless=0.25):
+    """Seeded run list of the batched-sweep workload: nx and nv uniform over
+    the choices, k ~ U[0.25, 0.45], amplitude and nu log-uniform, a quarter of
+    the runs collisionless."""
+    rng = np.random.default_rng(seed)
+    nx = rng.choice(np.asarray(nx_choices), n_runs)
+    nv = rng.choice(np.asarray(nv_choices), n_runs)
+    k = rng.uniform(k_range[0], k_range[1], n_runs)
+    amp = 10.0 ** rng.uniform(log_amp[0], log_amp[1], n_runs)
+    nu = 10.0 ** rng.uniform(log_nu[0], log_nu[1], n_runs)
+    nu[rng.random(n_runs) < p_collisionless] = 0.0
+    return [dict(nx=int(a), nv=int(b), k=float(c), amplitude=float(d), nu=float(e))
+            for a, b, c, d, e in zip(nx, nv, k, amp, nu)]
+
+
+class Sweep:
+    """Owns a vg_sweep; runs are advanced together on the current stream."""
+
+    def __init__(self, runs, vmax=6.4, dt=0.1, collision="dg"):
+        require_cuda()
+        self._lib = _lib.load()
+        self.runs = list(runs)
+        self.vmax, self.dt = float(vmax), float(dt)
+        arr = (_lib.VgSweepRun * len(self.runs))()
+        for i, r in enumerate(self.runs):
+            arr[i] = _lib.VgSweepRun(int(r["nx"]), int(r["nv"]), float(r["k"]), float(r["amplitude"]),
+                                     float(r["nu"]))
+        d = _lib.VgSweepDesc(len(self.runs), _lib.VG_COLL_DG if collision == "dg" else _lib.VG_COLL_LB,
+                             self.vmax, self.dt, arr)
+        h = C.c_void_p()
+        check(self._lib.vg_sweep_create(C.byref(d), C.byref(h)), "sweep create")
+        self._h = h
+        cells, xp = C.c_int64(), C.c_int64()
+        check(self._lib.vg_sweep_sizes(h, C.byref(cells), C.byref(xp)), "sweep sizes")
+        self.cells, self.x_points = int(cells.value), int(xp.value)
+        offs = (C.c_int64 * len(self.runs))()
+        check(self._lib.vg_sweep_x_offsets(h, offs), "sweep offsets")
+        self.x_offsets = np.array(offs[:], dtype=np.int64)
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._lib.vg_sweep_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def n_runs(self):
+        return len(self.runs)
+
+    def reset(self, stream=None):
+        check(self._lib.vg_sweep_reset(self._h, stream_handle(stream)), "sweep reset")
+
+    def history(self, rows):
+        """Device buffers for `rows` stored steps: e [rows][x_points] and
+        series [rows][n_runs][7]."""
+        dev = torch.device("cuda")
+        return (torch.zeros((rows, self.x_points), dtype=torch.float64, device=dev),
+                torch.zeros((rows, self.n_runs, 7), dtype=torch.float64, device=dev))
+
+    def run_steps(self, nsteps, e_hist=None, series_hist=None, row0=0, use_graph=False, stream=None):
+        rows = 0
+        if e_hist is not None:
+            rows = int(e_hist.shape[0])
+        elif series_hist is not None:
+            rows = int(series_hist.shape[0])
+        check(self._lib.vg_sweep_run_steps(self._h, int(nsteps), ptr(e_hist), ptr(series_hist), rows, int(row0),
+                                           int(bool(use_graph)), stream_handle(stream)), "sweep run steps")
+
+    def read_run(self, i, stream=None):
+        """(f [nx][nv] float64, e [nx] float64) of run i on the device."""
+        r = self.runs[i]
+        f = torch.empty((r["nx"], r["nv"]), dtype=torch.float64, device="cuda")
+        e = torch.empty(r["nx"], dtype=torch.float64, device="cuda")
+        check(self._lib.vg_sweep_read_run(self._h, int(i), ptr(f), ptr(e), stream_handle(stream)), "sweep read")
+        return f, e
+
+    def e_of(self, e_hist, i):
+        """e history [rows][nx] of run i from a sweep e-history buffer."""
+        o = int(self.x_offsets[i])
+        return e_hist[:, o:o + self.runs[i]["nx"]]
+
+    def profile(self, enable):
+        check(self._lib.vg_sweep_profile_enable(self._h, int(bool(enable))), "profile")
+
+    def profile_read(self):
+        buf = (_lib.VgProfEntry * 16)()
+        n = C.c_int32()
+        check(self._lib.vg_sweep_profile_read(self._h, buf, 16, C.byref(n)), "profile read")
+        return _prof_dict(buf, n.value)

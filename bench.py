@@ -167,6 +167,7 @@ def run_gpu(args, w, rank, world):
                                              "mean_f2", "mean_flogf")}}
     hist = history_struct(storage, nx, 2)
     stream = torch.cuda.Stream()
+    stream.wait_stream(torch.cuda.current_stream())
     with torch.cuda.stream(stream):
         plan.run_steps(f, e, hist, tb, db, 0, W, use_graph=False, stream=stream)
         # capture the K timed steps once, then replay it (a second capture
@@ -245,6 +246,7 @@ def run_sweep_gpu(args, w, rank, world):
     K, W = args.steps, args.warmup
     eh, sh = sw.history(K)
     stream = torch.cuda.Stream()
+    stream.wait_stream(torch.cuda.current_stream())
     with torch.cuda.stream(stream):
         sw.reset(stream)
         sw.run_steps(W, use_graph=False, stream=stream)
@@ -406,12 +408,16 @@ def main():
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32-deltaf"])
     ap.add_argument("--prof-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--runs", type=int, default=None, help="sweep size (default: the 4096-run workload)")
+    ap.add_argument("--no-fp64-compare", action="store_true", help="skip the plain FP64 GPU sweep estimate")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
-    w = WORKLOADS[args.workload]
+    w = dict(WORKLOADS[args.workload])
+    if args.runs:
+        w["n_runs"] = args.runs
     if w["kind"] == "sweep":
         return main_sweep(args, w, rank, world)
     cells = w["nx"] * w["nv"]
@@ -526,7 +532,12 @@ def main_sweep(args, w, rank, world):
         launches_per_step += d["launches"] / args.prof_steps
     if rank != 0:
         return
-    fp64_rps, fp64_per = fp64_plain_sweep(w)
+    fp64 = None
+    if not args.no_fp64_compare:
+        fp64_rps, fp64_per = fp64_plain_sweep(w)
+        fp64 = {"runs_per_s": fp64_rps, "ms_per_step_by_shape": fp64_per,
+                "how": "FP64 parity step, one run at a time, timed on one run per shape and "
+                       "weighted by the shape counts"}
     cpu = None
     if not args.no_cpu_baseline:
         cval, crps, cores, n, steps, wall = cpu_baseline_sweep(w, n_sample=36, steps=60)
@@ -538,9 +549,7 @@ def main_sweep(args, w, rank, world):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": cfg,
         "runs_per_s": runs_per_s,
-        "fp64_plain_gpu": {"runs_per_s": fp64_rps, "ms_per_step_by_shape": fp64_per,
-                           "how": "FP64 parity step, one run at a time, timed on one run per shape and "
-                                  "weighted by the shape counts"},
+        "fp64_plain_gpu": fp64,
         "e2e": {"value": world * cells * args.steps / e2e_sec, "unit": "cell-updates/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,

@@ -159,6 +159,7 @@ def test_fp32_graph_equals_direct():
     tb = torch.as_tensor(0.1 * np.arange(20), device="cuda")
     p.run_steps(g1, e1, None, tb, None, 0, 20, use_graph=False)
     s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())  # pool streams do not wait for the default stream
     with torch.cuda.stream(s):
         p.run_steps(g2, e2, None, tb, None, 0, 20, use_graph=True, stream=s)
     torch.cuda.synchronize()

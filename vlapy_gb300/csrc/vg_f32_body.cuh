@@ -101,9 +101,11 @@ __device__ __forceinline__ void kick(cx<float>* s, int t, double dkv, double dt,
                                      const cx<float>* __restrict__ F0, const cx<float>* __restrict__ tw) {
   constexpr int G = N / R;
   block_fft<float, N, false, R>(s, t, tw);
-  // theta(k) = -kv_k dt e = k * (-dkv dt e); half angle for P - 1
-  const Ang ha = split_angle(-0.5 * dkv * dt * ea);
-  const Ang hb = split_angle(-0.5 * dkv * dt * eb);
+  // theta(k) = -kv_k dt e = k * (-dkv dt e); half angle for P - 1.  The kick
+  // angle stays O(10) rad, so an FP32 product is accurate to ~1e-6 rad here
+  const float hk = (float)(-0.5 * dkv * dt);
+  const Ang ha = {hk * (float)ea, 0.f};
+  const Ang hb = {hk * (float)eb, 0.f};
   kick_rotate<N>(s, t, G, ha, hb, F0);
   __syncthreads();
   block_fft<float, N, true, R>(s, t, tw);
@@ -133,20 +135,30 @@ __device__ __forceinline__ void collide_row(float* x, int t, const RowConsts& rc
     mv[2] = {a2, 0.f};
   }
   group_df_sum<3>(mv, red, G, t);
-  const double M0 = rc.dv * df_to_double(mv[0]) + rc.f0m[0];
-  const double M1 = rc.dv * df_to_double(mv[1]) + rc.f0m[1];
-  const double M2 = rc.dv * df_to_double(mv[2]) + rc.f0m[2];
-  // DG: vbar = trapz(f v), v0t^2 = trapz(f (v - vbar)^2) = M2 + vbar^2 (M0 - 2)
-  // LB: v0t^2 = trapz(f v^2), no drift
-  const double vbar = dougherty ? M1 : 0.0;
-  const double vth = dougherty ? M2 + vbar * vbar * (M0 - 2.0) : M2;
-  const float Af = (float)(-vth / rc.dv_sq);
-  const float bdiag = (float)(1.0 + nudt * (2.0 * vth / rc.dv_sq));
+  // per-row FP64 scalars: one thread computes them (FP64 is scarce on this
+  // part), the group reads them back as FP32 coefficients
+  float* sc = reinterpret_cast<float*>(red);
+  if (t == 0) {
+    const double M0 = rc.dv * df_to_double(mv[0]) + rc.f0m[0];
+    const double M1 = rc.dv * df_to_double(mv[1]) + rc.f0m[1];
+    const double M2 = rc.dv * df_to_double(mv[2]) + rc.f0m[2];
+    // DG: vbar = trapz(f v), v0t^2 = trapz(f (v - vbar)^2) = M2 + vbar^2 (M0 - 2)
+    // LB: v0t^2 = trapz(f v^2), no drift
+    const double vbar = dougherty ? M1 : 0.0;
+    const double vth = dougherty ? M2 + vbar * vbar * (M0 - 2.0) : M2;
+    sc[0] = (float)(-vth / rc.dv_sq);
+    sc[1] = (float)(1.0 + nudt * (2.0 * vth / rc.dv_sq));
+    sc[2] = (float)vbar;
+    sc[3] = (float)(nudt * vth);
+    sc[4] = (float)(nudt * vbar);
+  }
+  __syncthreads();
+  const float Af = sc[0], bdiag = sc[1], vb = sc[2], cs = sc[3], cd = sc[4];
   const float nu = (float)nudt;
-  const float vb = (float)vbar;
+  const float cm = nu;
   const float i2dv = (float)(0.5 / rc.dv);
+  __syncthreads();
   // right-hand side: g - (A - I) f0 with (A - I) f0 = nudt (-vth S + Mv - vbar D)
-  const float cs = (float)(nudt * vth), cm = nu, cd = (float)(nudt * vbar);
 #pragma unroll
   for (int i = 0; i < R; ++i) {
     const int j = t * R + i;

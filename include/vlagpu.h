@@ -146,6 +146,23 @@ int vg_run_steps(vg_plan* plan, void* f, double* e, const vg_history* hist,
                  const double* time_batch, const double* driver_batch,
                  int32_t i0, int32_t nsteps, int32_t use_graph, vg_stream stream);
 
+/* ---- field solve without allocation ------------------------------------ */
+/* e = driver + Re IFFT(i/kx FFT(1 - trapz_v f)) for f[nx][nv] float64, the
+ * same FP64 arithmetic as vg_field_solve, but with no plan and no device
+ * allocation of any kind: for callers whose device memory is owned by
+ * another allocator (a framework's caching allocator, a fixed pool) or who
+ * cannot afford the device-wide synchronisation of cudaMalloc/cudaFree.  All
+ * scratch (density, FFT twiddles, summation table, DFT work area) lives in
+ * one static device array of about 580 KB that every GPU loading the library
+ * keeps until exit.  Limits: 2 <= nx <= 8192, 2 <= nv <= 16384; larger sizes
+ * return VG_ERR_ARG.  one_over_kx[nx], driver[nx] (may be NULL) and e[nx] are
+ * DEVICE arrays.  The first call on a device resolves the array's address
+ * and fills its twiddle table; make that call before any stream capture.
+ * Calls share the array: calls that overlap on the GPU race and must be
+ * ordered by the caller.  No counterpart in the reference. */
+int vg_field_solve_noalloc(const double* f, int32_t nx, int32_t nv, double dv, const double* one_over_kx,
+                           const double* driver, double* e, vg_stream stream);
+
 /* ---- batched sweep ----------------------------------------------------- */
 /* Thousands of independent runs of uneven shape advanced together in the
  * FP32 delta-f mode: every kernel launch of a step covers all runs (work

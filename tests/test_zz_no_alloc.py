@@ -1,0 +1,66 @@
+"""vg_field_solve_noalloc: the field solve for callers that cannot allocate
+device memory (their memory belongs to another allocator, or they cannot
+take the synchronisation of cudaMalloc/cudaFree).  It keeps its scratch in a
+static device array; this checks it against the plan-based vg_field_solve,
+called twice in a row through the C ABI.  Collected last on purpose."""
+
+import ctypes as C
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from oracle import vlapy_oracle as vo  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-12  # the FP64 parity tolerance of the other GPU tests
+
+
+@pytest.fixture(scope="module")
+def lib():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from vlapy_gb300 import _lib
+    return _lib.load()
+
+
+def _case(nx, nv, seed):
+    rng = np.random.default_rng(seed)
+    dx, x, kx, inv = vo.spatial_axis(0.0, 2 * np.pi / 0.3, nx)
+    dv, v, kv = vo.velocity_axis(6.4, nv)
+    f = vo.maxwellian(nx, nv, 6.4) * (1.0 + 1e-3 * np.cos(0.3 * x + rng.uniform(0, 6)))[:, None]
+    drv = 1e-3 * np.sin(0.3 * x)
+    return f, drv, (x, v, kx, kv, inv, dx, dv)
+
+
+@pytest.mark.parametrize("nx,nv", [(32, 512), (96, 256), (8192, 16), (64, 16384), (5, 9)])
+def test_noalloc_field_solve_matches_plan(lib, nx, nv):
+    from vlapy_gb300._lib import check
+    from vlapy_gb300.plan import Plan, ptr, stream_handle
+    f, drv, (x, v, kx, kv, inv, dx, dv) = _case(nx, nv, nx + nv)
+    plan = Plan(nx, nv, x, v, kx, kv, inv, dx, dv)
+    ft = torch.as_tensor(f, device="cuda")
+    dt_ = torch.as_tensor(drv, device="cuda")
+    inv_t = torch.as_tensor(inv, device="cuda")
+    for driver in (dt_, None):
+        ref = torch.empty(nx, dtype=torch.float64, device="cuda")
+        plan.field_solve(ft, driver, ref)
+        for _ in range(2):  # two calls in a row share (and overwrite) the static scratch
+            out = torch.full((nx,), float("nan"), dtype=torch.float64, device="cuda")
+            check(lib.vg_field_solve_noalloc(ptr(ft), nx, nv, C.c_double(dv), ptr(inv_t), ptr(driver), ptr(out),
+                                             stream_handle()), "field solve noalloc")
+            torch.cuda.synchronize()
+            a, b = out.cpu().numpy(), ref.cpu().numpy()
+            assert np.linalg.norm(a - b) <= TOL * np.linalg.norm(b)
+
+
+def test_noalloc_rejects_sizes_beyond_its_scratch(lib):
+    from vlapy_gb300._lib import VG_ERR_ARG
+    from vlapy_gb300.plan import ptr, stream_handle
+    f = torch.zeros((16384, 2), dtype=torch.float64, device="cuda")
+    inv = torch.zeros(16384, dtype=torch.float64, device="cuda")
+    e = torch.zeros(16384, dtype=torch.float64, device="cuda")
+    st = lib.vg_field_solve_noalloc(ptr(f), 16384, 2, C.c_double(0.1), ptr(inv), None, ptr(e), stream_handle())
+    assert st == VG_ERR_ARG
+    assert b"nx <= 8192" in lib.vg_last_error()

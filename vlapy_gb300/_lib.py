@@ -84,6 +84,8 @@ EXPORTS = {
     "vg_run_steps": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(VgHistory),
                                C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32,
                                C.c_void_p]),
+    "vg_field_solve_noalloc": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_double, C.c_void_p,
+                                         C.c_void_p, C.c_void_p, C.c_void_p]),
     "vg_sweep_create": (C.c_int, [C.POINTER(VgSweepDesc), C.POINTER(C.c_void_p)]),
     "vg_sweep_destroy": (C.c_int, [C.c_void_p]),
     "vg_sweep_sizes": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),

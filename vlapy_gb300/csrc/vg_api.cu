@@ -173,7 +173,7 @@ void free_plan(vg_plan* p) {
   delete static_cast<ProfState*>(p->prof);
   if (p->f32) {
     F32Plan* q = p->f32;
-    void* qp[] = {q->F0, q->v32, q->f0_32, q->S, q->Mv, q->D, q->dpart, q->mpart};
+    void* qp[] = {q->F0, q->v32, q->f0_32, q->S, q->Mv, q->D, q->dpart, q->mpart, q->vhl, q->e32};
     for (void* x : qp)
       if (x) cudaFree(x);
     delete q;
@@ -377,8 +377,10 @@ int setup_f32(vg_plan* p, const vg_run_desc* d) {
   const double* f0 = d->f_background;
   const double* v = d->v;
   std::vector<float> v32(nv), f32v(nv), S(nv), Mv(nv), D(nv);
+  std::vector<float2> vhl(nv);
   double mom[7] = {0, 0, 0, 0, 0, 0, 0};
   for (int j = 0; j < nv; ++j) {
+    vhl[j] = split_f2(v[j]);
     const double fm = j > 0 ? f0[j - 1] : 0.0, fp = j < nv - 1 ? f0[j + 1] : 0.0;
     const double vm = j > 0 ? v[j - 1] : 0.0, vp = j < nv - 1 ? v[j + 1] : 0.0;
     S[j] = (float)((fm - 2.0 * f0[j] + fp) / dv2);
@@ -405,6 +407,8 @@ int setup_f32(vg_plan* p, const vg_run_desc* d) {
   VG_CHECK(upload(&q->Mv, Mv, "f32 constants"));
   VG_CHECK(upload(&q->D, D, "f32 constants"));
   VG_CHECK(upload(&q->F0, F0, "f32 constants"));
+  VG_CHECK(upload(&q->vhl, vhl, "f32 constants"));
+  VG_CHECK(dev_copy<float>(&q->e32, nullptr, (size_t)nx, "f32 field"));
   q->dkx = nx > 1 ? d->kx[1] : 0.0;
   q->dkv = d->kv[1];
   q->c0 = mom[0] - 1.0;
@@ -413,6 +417,8 @@ int setup_f32(vg_plan* p, const vg_run_desc* d) {
   q->rc.S = q->S;
   q->rc.Mv = q->Mv;
   q->rc.D = q->D;
+  q->rc.vhl = q->vhl;
+  q->rc.i2dv = (float)(0.5 / dv);
   q->rc.dv = dv;
   q->rc.dv_sq = dv2;
   q->rc.dkv = q->dkv;
@@ -462,6 +468,7 @@ int step_sequence_f32(vg_plan* p, float* g, double* e, const vg_history* h, cons
     return cuda_status(prof_run(p, PK_STORE32, s, [&] { return launch_store_f32(*p, g, e, de, *h, i, nm, s); }),
                        "store");
   };
+  VG_CHECK(cuda_status(launch_e_to_f32(*p, e, s), "field copy"));
   if (p->integrator == VG_LEAPFROG) {
     VG_CHECK(K(0.5 * dt));
     for (int k = 0; k < nsteps; ++k) {
@@ -633,9 +640,11 @@ int vg_edfdv(vg_plan* p, void* f, const double* e, double dt, vg_stream stream) 
     set_error("null f or e");
     return VG_ERR_ARG;
   }
-  if (p->f32)
-    return cuda_status(launch_row_f32(*p, static_cast<float*>(f), e, dt, 0.0, 0, 0, 0, (cudaStream_t)stream),
-                       "edfdv");
+  if (p->f32) {
+    cudaStream_t s = (cudaStream_t)stream;
+    VG_CHECK(cuda_status(launch_e_to_f32(*p, e, s), "field copy"));
+    return cuda_status(launch_row_f32(*p, static_cast<float*>(f), e, dt, 0.0, 0, 0, 0, s), "edfdv");
+  }
   VG_CHECK(require_fft_v(p));
   return cuda_status(launch_edfdv_f64(*p, static_cast<double*>(f), e, dt, (cudaStream_t)stream), "edfdv");
 }

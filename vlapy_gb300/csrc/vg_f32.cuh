@@ -49,6 +49,13 @@ __device__ __forceinline__ Ang split_angle(double a) {
   const float h = (float)a;
   return {h, (float)(a - (double)h)};
 }
+// double-float product a * b of two (hi, lo) splits, as an angle per unit index
+__device__ __forceinline__ Ang mul_angle(float2 a, float2 b) {
+  const float p = a.x * b.x;
+  const float e = fmaf(a.x, b.x, -p) + fmaf(a.x, b.y, a.y * b.x);
+  const float h = p + e;
+  return {h, e - (h - p)};
+}
 // sin/cos of m * a to ~1e-7 absolute for |m a| up to ~1e4
 __device__ __forceinline__ void sincos_m(float m, Ang a, float& s, float& c) {
   const float p = m * a.hi;

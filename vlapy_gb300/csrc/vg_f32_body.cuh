@@ -16,8 +16,8 @@ constexpr int COL32_PAD = 1;
 // and the tile's trapz-weighted density partials added into dacc[x].
 // smem: W/2 padded sequences of NX complex floats.
 template <int NX, int R>
-__device__ __forceinline__ void col_tile(float* __restrict__ g, int nv, int c0, int W, double phi_unit,
-                                         const double* __restrict__ v, const cx<float>* __restrict__ tw,
+__device__ __forceinline__ void col_tile(float* __restrict__ g, int nv, int c0, int W, float2 kdt,
+                                         const float2* __restrict__ vhl, const cx<float>* __restrict__ tw,
                                          unsigned char* smem, df32* dacc) {
   constexpr int G = NX / R;
   constexpr int LD = sp_len<float>(NX) + COL32_PAD;
@@ -33,9 +33,10 @@ __device__ __forceinline__ void col_tile(float* __restrict__ g, int nv, int c0, 
   }
   __syncthreads();
   block_fft<float, NX, false, R>(sg, t, tw);
-  // theta(m) = m * (-dkx dt v_col): kx = m dkx on the bins m <= NX/2
-  const Ang aa = split_angle(phi_unit * v[c0 + 2 * grp]);
-  const Ang ab = split_angle(phi_unit * v[c0 + 2 * grp + 1]);
+  // theta(m) = m * (-dkx dt) v_col (kx = m dkx on the bins m <= NX/2); the angle
+  // per unit m is the double-float product of kdt = -dkx dt and v (both split)
+  const Ang aa = mul_angle(kdt, vhl[c0 + 2 * grp]);
+  const Ang ab = mul_angle(kdt, vhl[c0 + 2 * grp + 1]);
   two_real_rotate<float>(sg, NX, t, G, [&](int m, float& ca, float& sa, float& cb, float& sb) {
     sincos_m((float)m, aa, sa, ca);
     sincos_m((float)m, ab, sb, cb);
@@ -97,15 +98,15 @@ __device__ __forceinline__ void kick_rotate(cx<float>* s, int t, int G, Ang ha, 
 }
 
 template <int N, int R>
-__device__ __forceinline__ void kick(cx<float>* s, int t, double dkv, double dt, double ea, double eb,
+__device__ __forceinline__ void kick(cx<float>* s, int t, float hk, float ea, float eb,
                                      const cx<float>* __restrict__ F0, const cx<float>* __restrict__ tw) {
   constexpr int G = N / R;
   block_fft<float, N, false, R>(s, t, tw);
-  // theta(k) = -kv_k dt e = k * (-dkv dt e); half angle for P - 1.  The kick
-  // angle stays O(10) rad, so an FP32 product is accurate to ~1e-6 rad here
-  const float hk = (float)(-0.5 * dkv * dt);
-  const Ang ha = {hk * (float)ea, 0.f};
-  const Ang hb = {hk * (float)eb, 0.f};
+  // theta(k) = -kv_k dt e = k * (-dkv dt e); hk = -dkv dt / 2 gives the half
+  // angle for P - 1.  The kick angle stays O(10) rad, so an FP32 product is
+  // accurate to ~1e-6 rad here
+  const Ang ha = {hk * ea, 0.f};
+  const Ang hb = {hk * eb, 0.f};
   kick_rotate<N>(s, t, G, ha, hb, F0);
   __syncthreads();
   block_fft<float, N, true, R>(s, t, tw);
@@ -113,8 +114,8 @@ __device__ __forceinline__ void kick(cx<float>* s, int t, double dkv, double dt,
 
 // Fokker-Planck step of one row stored at x (stride 2 floats) in delta-f form.
 template <int N, int R>
-__device__ __forceinline__ void collide_row(float* x, int t, const RowConsts& rc, double nudt, int dougherty,
-                                            df32* red, float* pcr) {
+__device__ __forceinline__ void collide_row(float* x, int t, const RowConsts& rc, double nudt, float nudt_f,
+                                            int dougherty, df32* red, float* pcr) {
   constexpr int G = N / R;
   // moments of g over the thread's chunk: sum w g, sum w g v, sum w g v^2
   df32 mv[3];
@@ -154,9 +155,9 @@ __device__ __forceinline__ void collide_row(float* x, int t, const RowConsts& rc
   }
   __syncthreads();
   const float Af = sc[0], bdiag = sc[1], vb = sc[2], cs = sc[3], cd = sc[4];
-  const float nu = (float)nudt;
+  const float nu = nudt_f;
   const float cm = nu;
-  const float i2dv = (float)(0.5 / rc.dv);
+  const float i2dv = rc.i2dv;
   __syncthreads();
   // right-hand side: g - (A - I) f0 with (A - I) f0 = nudt (-vth S + Mv - vbar D)
 #pragma unroll
@@ -192,13 +193,13 @@ __device__ __forceinline__ void row_pair(const RowArgs& a, int pair, unsigned ch
     s[sp<float>(n)] = {va ? ga[n] : 0.f, vb ? gbp[n] : 0.f};
   }
   __syncthreads();
-  const bool kicks = a.dt1 != 0.0 || a.dt2 != 0.0;
-  const double ea = (kicks && va) ? a.e[ra] : 0.0, eb = (kicks && vb) ? a.e[rb] : 0.0;
-  if (a.dt1 != 0.0) kick<N, R>(s, t, a.rc.dkv, a.dt1, ea, eb, a.F0, a.tw);
+  const bool kicks = a.hk1 != 0.f || a.hk2 != 0.f;
+  const float ea = (kicks && va) ? a.e32[ra] : 0.f, eb = (kicks && vb) ? a.e32[rb] : 0.f;
+  if (a.hk1 != 0.f) kick<N, R>(s, t, a.hk1, ea, eb, a.F0, a.tw);
   float* sx = reinterpret_cast<float*>(s);
   if (a.fp) {
-    collide_row<N, R>(sx, t, a.rc, a.nudt, a.dougherty, red, pcr);
-    collide_row<N, R>(sx + 1, t, a.rc, a.nudt, a.dougherty, red, pcr);
+    collide_row<N, R>(sx, t, a.rc, a.nudt, a.nudt_f, a.dougherty, red, pcr);
+    collide_row<N, R>(sx + 1, t, a.rc, a.nudt, a.nudt_f, a.dougherty, red, pcr);
   }
   if (a.want_mom) {
     // n, j, T, q, fv4, vN (sums of w g v^p), sum w g^2, sum w g f0, sum w f log f
@@ -267,7 +268,7 @@ __device__ __forceinline__ void row_pair(const RowArgs& a, int pair, unsigned ch
       }
     }
   }
-  if (a.dt2 != 0.0) kick<N, R>(s, t, a.rc.dkv, a.dt2, ea, eb, a.F0, a.tw);
+  if (a.hk2 != 0.f) kick<N, R>(s, t, a.hk2, ea, eb, a.F0, a.tw);
 #pragma unroll
   for (int i = 0; i < R; ++i) {
     const int n = t + i * G;

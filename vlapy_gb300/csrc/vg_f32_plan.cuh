@@ -13,17 +13,21 @@ struct RowConsts {
   const float* S;   // [nv] (f0[j-1] - 2 f0[j] + f0[j+1]) / dv^2, truncated at the ends
   const float* Mv;  // [nv] (v[j-1] f0[j-1] - v[j+1] f0[j+1]) / (2 dv)
   const float* D;   // [nv] (f0[j-1] - f0[j+1]) / (2 dv)
+  const float2* vhl;  // [nv] v split into FP32 (hi, lo) for exact phase products
   double dv, dv_sq, dkv;
   double f0m[7];    // trapz(f0 v^p), p = 0..5, and trapz(f0^2)
+  float i2dv;       // 1 / (2 dv)
 };
 
 struct RowArgs {
   float* g;
   int nx;
-  const double* e;
-  double dt1, dt2;  // leading / trailing half-kick steps (0: skip)
+  const float* e32;  // field of the kicks, FP32 copy
+  double dt1, dt2;   // leading / trailing half-kick steps (0: skip)
+  float hk1, hk2;    // -dkv dt / 2 of each kick: half angle per kv index and unit field
   int fp, dougherty;
   double nudt;
+  float nudt_f;
   int want_mom;     // storage moments + x modes of the post-collision state
   double* mom;      // [nx][8]
   int n_modes;
@@ -42,6 +46,8 @@ struct F32Plan {
   float* Mv;
   float* D;
   RowConsts rc;
+  float2* vhl;         // [nv] v as FP32 (hi, lo)
+  float* e32;          // [nx] FP32 copy of the field
   float2* dpart;       // [max col grid][nx] density partials (hi, lo)
   int npart;
   cx<float>* mpart;    // [max row grid][4][nv]
@@ -69,5 +75,11 @@ __host__ __device__ constexpr size_t row32_group_bytes(int n, int r) {
 }
 
 constexpr int F32_MAX_MODES = 4;
+
+// (hi, lo) FP32 split of an FP64 value
+inline float2 split_f2(double a) {
+  const float h = (float)a;
+  return make_float2(h, (float)(a - (double)h));
+}
 
 }  // namespace vg

@@ -133,6 +133,8 @@ cudaError_t launch_poisson_only_f32(const vg_plan& p, const double* rho, const d
                                     const FieldTime& ft, double* e, cudaStream_t s);
 cudaError_t launch_row_f32(const vg_plan& p, float* g, const double* e, double dt1, double dt2, int fp, int mom,
                            int n_modes, cudaStream_t s);
+// FP32 copy of a caller-provided field for the kicks
+cudaError_t launch_e_to_f32(const vg_plan& p, const double* e, cudaStream_t s);
 cudaError_t launch_store_f32(const vg_plan& p, const float* g, const double* e, const double* de,
                              const vg_history& h, int i, int n_modes, cudaStream_t s);
 

@@ -21,15 +21,15 @@ namespace vg {
 
 template <int NX, int R>
 __global__ void __launch_bounds__((NX / R) * col32_seqs(NX, R)) k_col_f32(
-    float* __restrict__ g, int nv, int ntiles, int W, double phi_unit,
-    const double* __restrict__ v, const cx<float>* __restrict__ tw, float2* __restrict__ dpart) {
+    float* __restrict__ g, int nv, int ntiles, int W, float2 kdt,
+    const float2* __restrict__ vhl, const cx<float>* __restrict__ tw, float2* __restrict__ dpart) {
   constexpr int LD = sp_len<float>(NX) + COL32_PAD;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int S = W / 2;
   df32* dacc = reinterpret_cast<df32*>(smem_raw + (size_t)S * LD * sizeof(cx<float>));
   for (int x = threadIdx.x; x < NX; x += blockDim.x) dacc[x] = {0.f, 0.f};
   for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x)
-    col_tile<NX, R>(g, nv, tile * W, W, phi_unit, v, tw, smem_raw, dacc);
+    col_tile<NX, R>(g, nv, tile * W, W, kdt, vhl, tw, smem_raw, dacc);
   for (int x = threadIdx.x; x < NX; x += blockDim.x)
     dpart[(size_t)blockIdx.x * NX + x] = make_float2(dacc[x].hi, dacc[x].lo);
 }
@@ -77,7 +77,7 @@ __global__ void __launch_bounds__(fft_threads<float>(NX)) k_field_f32(
     const double* __restrict__ rho, const double* __restrict__ inv_kx, const double* __restrict__ driver,
     int use_pulses, const vg_pulse* __restrict__ P, int np, const double* __restrict__ x, const double* t_ptr,
     double t_host, int nadd, double a0, double a1, double a2, double a3, double a4,
-    const cx<float>* __restrict__ tw, double* __restrict__ e) {
+    const cx<float>* __restrict__ tw, double* __restrict__ e, float* __restrict__ e32) {
   constexpr int G = fft_threads<float>(NX);
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cx<float>* s = reinterpret_cast<cx<float>*>(smem_raw);
@@ -100,7 +100,9 @@ __global__ void __launch_bounds__(fft_threads<float>(NX)) k_field_f32(
     float drv = 0.f;
     if (driver) drv = (float)driver[n];
     else if (use_pulses) drv = pulse_sum_f32(P, np, tt, x[n]);
-    e[n] = (double)(drv + s[sp<float>(n)].x);
+    const float en = drv + s[sp<float>(n)].x;
+    e[n] = (double)en;
+    e32[n] = en;
   }
 }
 
@@ -200,7 +202,8 @@ cudaError_t col_n(const vg_plan& p, float* g, double dt, cudaStream_t s) {
   int grid = (occ > 0 ? occ : 1) * p.f32->n_sm;
   if (grid > p.f32->col_grid_max) grid = p.f32->col_grid_max;
   if (grid > ntiles) grid = ntiles;
-  k_col_f32<NX, R><<<grid, S * G, smem, s>>>(g, p.nv, ntiles, W, -p.f32->dkx * dt, p.v, p.tw32, p.f32->dpart);
+  k_col_f32<NX, R><<<grid, S * G, smem, s>>>(g, p.nv, ntiles, W, split_f2(-p.f32->dkx * dt), p.f32->vhl, p.tw32,
+                                             p.f32->dpart);
   p.f32->npart = grid;
   return cudaGetLastError();
 }
@@ -213,7 +216,7 @@ cudaError_t field_n(const vg_plan& p, const double* driver, const FieldTime& ft,
   if (err != cudaSuccess) return err;
   k_field_f32<NX><<<1, G, smem, s>>>(p.rho, p.inv_kx, driver, ft.use_pulses, p.pulses, p.n_pulses, p.x, ft.t_ptr,
                                      ft.t_host, ft.nadd, ft.add[0], ft.add[1], ft.add[2], ft.add[3], ft.add[4],
-                                     p.tw32, e);
+                                     p.tw32, e, p.f32->e32);
   return cudaGetLastError();
 }
 
@@ -298,6 +301,15 @@ cudaError_t launch_dens_rows_f32(const vg_plan& p, const float* g, double* out, 
   return cudaGetLastError();
 }
 
+__global__ void k_e_to_f32(const double* __restrict__ e, int nx, float* __restrict__ e32) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nx; i += gridDim.x * blockDim.x) e32[i] = (float)e[i];
+}
+
+cudaError_t launch_e_to_f32(const vg_plan& p, const double* e, cudaStream_t s) {
+  k_e_to_f32<<<div_up(p.nx, 256), 256, 0, s>>>(e, p.nx, p.f32->e32);
+  return cudaGetLastError();
+}
+
 // stored_f[i] = g + f0 as float64 (store-all rule)
 __global__ void k_store_all_f32(const float* __restrict__ g, const double* __restrict__ f0, int nx, int nv,
                                 double* __restrict__ out) {
@@ -308,15 +320,19 @@ __global__ void k_store_all_f32(const float* __restrict__ g, const double* __res
 
 cudaError_t launch_row_f32(const vg_plan& p, float* g, const double* e, double dt1, double dt2, int fp, int mom,
                            int n_modes, cudaStream_t s) {
+  (void)e;  // the kicks read the FP32 copy p.f32->e32 (written by the field solve or launch_e_to_f32)
   RowArgs a;
   a.g = g;
   a.nx = p.nx;
-  a.e = e;
+  a.e32 = p.f32->e32;
   a.dt1 = dt1;
   a.dt2 = dt2;
+  a.hk1 = (float)(-0.5 * p.f32->dkv * dt1);
+  a.hk2 = (float)(-0.5 * p.f32->dkv * dt2);
   a.fp = fp && p.collision != VG_COLL_NONE;
   a.dougherty = p.collision == VG_COLL_DG;
   a.nudt = p.nudt;
+  a.nudt_f = (float)p.nudt;
   a.want_mom = mom;
   a.mom = p.mom;
   a.n_modes = mom ? n_modes : 0;

@@ -29,6 +29,8 @@ struct SweepRunDev {
   int x_off;           // x points before this run
   long long dp_off;    // density-partial elements (float2) before this run
   double k, nudt;
+  float2 kdt;          // -k dt split into FP32 (hi, lo): the x-drift angle per unit m and v
+  float nudt_f;
 };
 
 constexpr int SWEEP_BLOCK = 256;
@@ -48,36 +50,25 @@ struct SweepConsts {
 // kernels
 // ---------------------------------------------------------------------------
 
+// x-drift of one (run, tile) item per CTA; one kernel per nx class keeps
+// each instantiation's code and registers small
 template <int NX>
-__device__ __forceinline__ void sweep_col_item(const SweepRunDev& r, int tile, float* g, const SweepConsts& sc,
-                                               double dt, const cx<float>* tw, float2* dpart, unsigned char* smem) {
+__global__ void __launch_bounds__(SWEEP_BLOCK, (NX <= 64 ? 3 : 4)) k_sweep_col(const SweepRunDev* __restrict__ runs,
+                                                              const int2* __restrict__ items, float* g,
+                                                              const SweepConsts* __restrict__ scp,
+                                                              const cx<float>* __restrict__ tw, float2* dpart) {
   constexpr int R = col32_radix(NX);
   constexpr int W = sweep_col_w(NX);
   constexpr int LD = sp_len<float>(NX) + COL32_PAD;
-  df32* dacc = reinterpret_cast<df32*>(smem + (size_t)(W / 2) * LD * sizeof(cx<float>));
-  for (int x = threadIdx.x; x < NX; x += blockDim.x) dacc[x] = {0.f, 0.f};
-  __syncthreads();
-  col_tile<NX, R>(g + r.g_off, r.nv, tile * W, W, -r.k * dt, sc.v64[r.cls], tw, smem, dacc);
-  float2* out = dpart + r.dp_off + (size_t)tile * NX;
-  for (int x = threadIdx.x; x < NX; x += blockDim.x) out[x] = make_float2(dacc[x].hi, dacc[x].lo);
-}
-
-__global__ void __launch_bounds__(SWEEP_BLOCK) k_sweep_col(const SweepRunDev* __restrict__ runs,
-                                                           const int2* __restrict__ items, float* g,
-                                                           const SweepConsts* __restrict__ scp, double dt,
-                                                           const cx<float>* __restrict__ tw, float2* dpart) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int2 it = items[blockIdx.x];
   const SweepRunDev r = runs[it.x];
-  const SweepConsts& sc = *scp;
-  switch (r.nx) {
-    case 8: sweep_col_item<8>(r, it.y, g, sc, dt, tw, dpart, smem_raw); break;
-    case 16: sweep_col_item<16>(r, it.y, g, sc, dt, tw, dpart, smem_raw); break;
-    case 32: sweep_col_item<32>(r, it.y, g, sc, dt, tw, dpart, smem_raw); break;
-    case 64: sweep_col_item<64>(r, it.y, g, sc, dt, tw, dpart, smem_raw); break;
-    case 128: sweep_col_item<128>(r, it.y, g, sc, dt, tw, dpart, smem_raw); break;
-    default: sweep_col_item<256>(r, it.y, g, sc, dt, tw, dpart, smem_raw); break;
-  }
+  df32* dacc = reinterpret_cast<df32*>(smem_raw + (size_t)(W / 2) * LD * sizeof(cx<float>));
+  for (int x = threadIdx.x; x < NX; x += blockDim.x) dacc[x] = {0.f, 0.f};
+  __syncthreads();
+  col_tile<NX, R>(g + r.g_off, r.nv, it.y * W, W, r.kdt, scp->rc[r.cls].vhl, tw, smem_raw, dacc);
+  float2* out = dpart + r.dp_off + (size_t)it.y * NX;
+  for (int x = threadIdx.x; x < NX; x += blockDim.x) out[x] = make_float2(dacc[x].hi, dacc[x].lo);
 }
 
 // field solve of up to SWEEP_FIELD_BLOCK/G runs of one nx per CTA
@@ -85,7 +76,7 @@ template <int NX>
 __device__ __forceinline__ void sweep_field_runs(const SweepRunDev* __restrict__ runs, int first, int count,
                                                  const SweepConsts& sc, const float2* __restrict__ dpart,
                                                  const cx<float>* __restrict__ tw, double* __restrict__ e,
-                                                 unsigned char* smem) {
+                                                 float* __restrict__ e32, unsigned char* smem) {
   constexpr int G = fft_threads<float>(NX);
   const int grp = threadIdx.x / G, t = threadIdx.x - grp * G;
   cx<float>* s = reinterpret_cast<cx<float>*>(smem) + (size_t)grp * sp_len<float>(NX);
@@ -114,7 +105,11 @@ __device__ __forceinline__ void sweep_field_runs(const SweepRunDev* __restrict__
   __syncthreads();
   block_fft<float, NX, true>(s, t, tw);
   if (valid)
-    for (int x = t; x < NX; x += G) e[r.x_off + x] = (double)s[sp<float>(x)].x;
+    for (int x = t; x < NX; x += G) {
+      const float ex = s[sp<float>(x)].x;
+      e[r.x_off + x] = (double)ex;
+      e32[r.x_off + x] = ex;
+    }
 }
 
 __global__ void __launch_bounds__(SWEEP_FIELD_BLOCK) k_sweep_field(const SweepRunDev* __restrict__ runs,
@@ -122,70 +117,62 @@ __global__ void __launch_bounds__(SWEEP_FIELD_BLOCK) k_sweep_field(const SweepRu
                                                                    const SweepConsts* __restrict__ scp,
                                                                    const float2* __restrict__ dpart,
                                                                    const cx<float>* __restrict__ tw,
-                                                                   double* __restrict__ e) {
+                                                                   double* __restrict__ e, float* __restrict__ e32) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int4 it = items[blockIdx.x];  // (nx, first run, count, -)
   const SweepConsts& sc = *scp;
   switch (it.x) {
-    case 8: sweep_field_runs<8>(runs, it.y, it.z, sc, dpart, tw, e, smem_raw); break;
-    case 16: sweep_field_runs<16>(runs, it.y, it.z, sc, dpart, tw, e, smem_raw); break;
-    case 32: sweep_field_runs<32>(runs, it.y, it.z, sc, dpart, tw, e, smem_raw); break;
-    case 64: sweep_field_runs<64>(runs, it.y, it.z, sc, dpart, tw, e, smem_raw); break;
-    case 128: sweep_field_runs<128>(runs, it.y, it.z, sc, dpart, tw, e, smem_raw); break;
-    default: sweep_field_runs<256>(runs, it.y, it.z, sc, dpart, tw, e, smem_raw); break;
+    case 8: sweep_field_runs<8>(runs, it.y, it.z, sc, dpart, tw, e, e32, smem_raw); break;
+    case 16: sweep_field_runs<16>(runs, it.y, it.z, sc, dpart, tw, e, e32, smem_raw); break;
+    case 32: sweep_field_runs<32>(runs, it.y, it.z, sc, dpart, tw, e, e32, smem_raw); break;
+    case 64: sweep_field_runs<64>(runs, it.y, it.z, sc, dpart, tw, e, e32, smem_raw); break;
+    case 128: sweep_field_runs<128>(runs, it.y, it.z, sc, dpart, tw, e, e32, smem_raw); break;
+    default: sweep_field_runs<256>(runs, it.y, it.z, sc, dpart, tw, e, e32, smem_raw); break;
   }
 }
 
 struct SweepRowArgs {
   float* g;
-  const double* e;
+  const float* e32;
   double* mom;
   double dt1, dt2;
+  float hk1[SWEEP_MAX_CLASSES], hk2[SWEEP_MAX_CLASSES];  // -dkv dt / 2 per nv class
   int fp, want_mom, dougherty;
   const cx<float>* tw;
 };
 
+// one (run, row-pair group) item per CTA; one kernel per nv class
 template <int N>
-__device__ __forceinline__ void sweep_row_item(const SweepRunDev& r, int pg, const SweepRowArgs& sa,
-                                               const SweepConsts& sc, unsigned char* smem) {
+__global__ void __launch_bounds__(SWEEP_BLOCK, 3) k_sweep_row(const SweepRunDev* __restrict__ runs,
+                                                              const int2* __restrict__ items, SweepRowArgs sa,
+                                                              const SweepConsts* __restrict__ scp) {
   constexpr int R = row32_radix(N);
   constexpr int G = N / R;
   constexpr int P = SWEEP_BLOCK / G;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int2 it = items[blockIdx.x];
+  const SweepRunDev r = runs[it.x];
   const int grp = threadIdx.x / G, t = threadIdx.x - grp * G;
   RowArgs a;
   a.g = sa.g + r.g_off;
   a.nx = r.nx;
-  a.e = sa.e + r.x_off;
+  a.e32 = sa.e32 + r.x_off;
   a.dt1 = sa.dt1;
   a.dt2 = sa.dt2;
+  a.hk1 = sa.hk1[r.cls];
+  a.hk2 = sa.hk2[r.cls];
   a.fp = sa.fp && r.fp;
   a.dougherty = sa.dougherty;
   a.nudt = r.nudt;
+  a.nudt_f = r.nudt_f;
   a.want_mom = sa.want_mom;
   a.mom = sa.mom + (size_t)r.x_off * MOM_STRIDE;
   a.n_modes = 0;
   a.mpart = nullptr;
-  a.F0 = sc.F0[r.cls];
+  a.F0 = scp->F0[r.cls];
   a.tw = sa.tw;
-  a.rc = sc.rc[r.cls];
-  row_pair<N, R>(a, pg * P + grp, smem + (size_t)grp * row32_group_bytes(N, R), nullptr, P, grp, t);
-}
-
-__global__ void __launch_bounds__(SWEEP_BLOCK) k_sweep_row(const SweepRunDev* __restrict__ runs,
-                                                           const int2* __restrict__ items, SweepRowArgs sa,
-                                                           const SweepConsts* __restrict__ scp) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int2 it = items[blockIdx.x];
-  const SweepRunDev r = runs[it.x];
-  const SweepConsts& sc = *scp;
-  switch (r.nv) {
-    case 64: sweep_row_item<64>(r, it.y, sa, sc, smem_raw); break;
-    case 128: sweep_row_item<128>(r, it.y, sa, sc, smem_raw); break;
-    case 256: sweep_row_item<256>(r, it.y, sa, sc, smem_raw); break;
-    case 512: sweep_row_item<512>(r, it.y, sa, sc, smem_raw); break;
-    case 1024: sweep_row_item<1024>(r, it.y, sa, sc, smem_raw); break;
-    default: sweep_row_item<2048>(r, it.y, sa, sc, smem_raw); break;
-  }
+  a.rc = scp->rc[r.cls];
+  row_pair<N, R>(a, it.y * P + grp, smem_raw + (size_t)grp * row32_group_bytes(N, R), nullptr, P, grp, t);
 }
 
 // e history row and the seven series of every run (one CTA per run)
@@ -263,17 +250,19 @@ struct vg_sweep {
   float* g;
   double* e;
   double* mom;
+  float* e32;
   float2* dpart;
   cx<float>* tw32;
   cx<double>* tw64;
   std::vector<double*> f0d;  // per nv class: FP64 background
+  // work lists, one per shape class (items of one class are contiguous)
   int2* col_items;
-  int n_col;
+  std::vector<int> col_nx, col_first, col_count;
   int4* field_items;
   int n_field;
   int2* row_items;
-  int n_row;
-  size_t col_smem, field_smem, row_smem;
+  std::vector<int> row_nv, row_first, row_count;
+  size_t field_smem;
   std::map<std::tuple<int, const void*, const void*, int, int, cudaStream_t>, cudaGraphExec_t> graphs;
   ProfState prof;
 };
@@ -343,8 +332,10 @@ int sweep_class(vg_sweep* s, int cls, int nv) {
   for (int j = 0; j < nv; ++j) f0[j] /= norm;
   const double dv2 = dv * dv;
   std::vector<float> v32(nv), f32v(nv), S(nv), Mv(nv), D(nv);
+  std::vector<float2> vhl(nv);
   double mom[7] = {0, 0, 0, 0, 0, 0, 0};
   for (int j = 0; j < nv; ++j) {
+    vhl[j] = split_f2(v[j]);
     const double fm = j > 0 ? f0[j - 1] : 0.0, fp = j < nv - 1 ? f0[j + 1] : 0.0;
     const double vm = j > 0 ? v[j - 1] : 0.0, vp = j < nv - 1 ? v[j + 1] : 0.0;
     S[j] = (float)((fm - 2.0 * f0[j] + fp) / dv2);
@@ -366,6 +357,7 @@ int sweep_class(vg_sweep* s, int cls, int nv) {
   std::vector<cx<float>> F0(nv / 2 + 1);
   for (int k = 0; k <= nv / 2; ++k) F0[k] = {(float)re[k], (float)im[k]};
   float *dv32, *df0, *dS, *dM, *dD;
+  float2* dvhl;
   cx<float>* dF0;
   double *dv64, *df064;
   SW_CHECK(sw_alloc(s, &dv32, nv, v32.data(), "sweep constants"));
@@ -374,6 +366,7 @@ int sweep_class(vg_sweep* s, int cls, int nv) {
   SW_CHECK(sw_alloc(s, &dM, nv, Mv.data(), "sweep constants"));
   SW_CHECK(sw_alloc(s, &dD, nv, D.data(), "sweep constants"));
   SW_CHECK(sw_alloc(s, &dF0, F0.size(), F0.data(), "sweep constants"));
+  SW_CHECK(sw_alloc(s, &dvhl, vhl.size(), vhl.data(), "sweep constants"));
   SW_CHECK(sw_alloc(s, &dv64, nv, v.data(), "sweep constants"));
   SW_CHECK(sw_alloc(s, &df064, nv, f0.data(), "sweep constants"));
   RowConsts& rc = s->consts_h.rc[cls];
@@ -382,6 +375,8 @@ int sweep_class(vg_sweep* s, int cls, int nv) {
   rc.S = dS;
   rc.Mv = dM;
   rc.D = dD;
+  rc.vhl = dvhl;
+  rc.i2dv = (float)(0.5 / dv);
   rc.dv = dv;
   rc.dv_sq = dv2;
   rc.dkv = 2.0 * M_PI / (nv * dv);
@@ -405,6 +400,27 @@ enum SweepProfKind { SK_KICK = 0, SK_X_DRIFT, SK_FIELD, SK_ROW, SK_STORE, SK_COU
 const char* const kSweepNames[SK_COUNT] = {"sweep_kick", "sweep_x_drift", "sweep_field", "sweep_row_pass",
                                           "sweep_store"};
 
+template <int NX>
+cudaError_t sweep_col_launch(vg_sweep* s, int c, cudaStream_t st) {
+  constexpr int W = sweep_col_w(NX);
+  const size_t smem = (size_t)(W / 2) * (sp_len<float>(NX) + COL32_PAD) * sizeof(cx<float>) + (size_t)NX * sizeof(df32);
+  cudaError_t err = ensure_smem((const void*)k_sweep_col<NX>, smem);
+  if (err != cudaSuccess) return err;
+  k_sweep_col<NX><<<s->col_count[c], SWEEP_BLOCK, smem, st>>>(s->runs, s->col_items + s->col_first[c], s->g,
+                                                              s->consts, s->tw32, s->dpart);
+  return cudaGetLastError();
+}
+
+template <int N>
+cudaError_t sweep_row_launch(vg_sweep* s, int c, const SweepRowArgs& a, cudaStream_t st) {
+  constexpr int R = row32_radix(N);
+  const size_t smem = (size_t)(SWEEP_BLOCK / (N / R)) * row32_group_bytes(N, R);
+  cudaError_t err = ensure_smem((const void*)k_sweep_row<N>, smem);
+  if (err != cudaSuccess) return err;
+  k_sweep_row<N><<<s->row_count[c], SWEEP_BLOCK, smem, st>>>(s->runs, s->row_items + s->row_first[c], a, s->consts);
+  return cudaGetLastError();
+}
+
 int sweep_sequence(vg_sweep* s, int nsteps, double* e_hist, double* s_hist, int rows, int row0,
                    cudaStream_t st) {
   const double dt = s->dt;
@@ -412,33 +428,57 @@ int sweep_sequence(vg_sweep* s, int nsteps, double* e_hist, double* s_hist, int 
   auto row = [&](double dt1, double dt2, int fp, int mom, int kind) {
     SweepRowArgs a;
     a.g = s->g;
-    a.e = s->e;
+    a.e32 = s->e32;
     a.mom = s->mom;
     a.dt1 = dt1;
     a.dt2 = dt2;
+    for (size_t c = 0; c < s->nv_of_class.size(); ++c) {
+      const double dkv = s->consts_h.rc[c].dkv;
+      a.hk1[c] = (float)(-0.5 * dkv * dt1);
+      a.hk2[c] = (float)(-0.5 * dkv * dt2);
+    }
     a.fp = fp;
     a.want_mom = mom;
     a.dougherty = dg;
     a.tw = s->tw32;
     return cuda_status(prof_call(&s->prof, kind, st, [&] {
-                         k_sweep_row<<<s->n_row, SWEEP_BLOCK, s->row_smem, st>>>(s->row_items ? s->runs : nullptr,
-                                                                                  s->row_items, a, s->consts);
-                         return cudaGetLastError();
+                         for (size_t c = 0; c < s->row_nv.size(); ++c) {
+                           cudaError_t err = cudaSuccess;
+                           switch (s->row_nv[c]) {
+                             case 64: err = sweep_row_launch<64>(s, (int)c, a, st); break;
+                             case 128: err = sweep_row_launch<128>(s, (int)c, a, st); break;
+                             case 256: err = sweep_row_launch<256>(s, (int)c, a, st); break;
+                             case 512: err = sweep_row_launch<512>(s, (int)c, a, st); break;
+                             case 1024: err = sweep_row_launch<1024>(s, (int)c, a, st); break;
+                             default: err = sweep_row_launch<2048>(s, (int)c, a, st); break;
+                           }
+                           if (err != cudaSuccess) return err;
+                         }
+                         return cudaSuccess;
                        }),
                        "sweep row pass");
   };
   SW_CHECK(row(0.5 * dt, 0.0, 0, 0, SK_KICK));
   for (int k = 0; k < nsteps; ++k) {
     SW_CHECK(cuda_status(prof_call(&s->prof, SK_X_DRIFT, st, [&] {
-                           k_sweep_col<<<s->n_col, SWEEP_BLOCK, s->col_smem, st>>>(s->runs, s->col_items, s->g,
-                                                                                    s->consts, dt, s->tw32,
-                                                                                    s->dpart);
-                           return cudaGetLastError();
+                           for (size_t c = 0; c < s->col_nx.size(); ++c) {
+                             cudaError_t err = cudaSuccess;
+                             switch (s->col_nx[c]) {
+                               case 8: err = sweep_col_launch<8>(s, (int)c, st); break;
+                               case 16: err = sweep_col_launch<16>(s, (int)c, st); break;
+                               case 32: err = sweep_col_launch<32>(s, (int)c, st); break;
+                               case 64: err = sweep_col_launch<64>(s, (int)c, st); break;
+                               case 128: err = sweep_col_launch<128>(s, (int)c, st); break;
+                               default: err = sweep_col_launch<256>(s, (int)c, st); break;
+                             }
+                             if (err != cudaSuccess) return err;
+                           }
+                           return cudaSuccess;
                          }),
                          "sweep x drift"));
     SW_CHECK(cuda_status(prof_call(&s->prof, SK_FIELD, st, [&] {
                            k_sweep_field<<<s->n_field, SWEEP_FIELD_BLOCK, s->field_smem, st>>>(
-                               s->field_runs, s->field_items, s->consts, s->dpart, s->tw32, s->e);
+                               s->field_runs, s->field_items, s->consts, s->dpart, s->tw32, s->e, s->e32);
                            return cudaGetLastError();
                          }),
                          "sweep field"));
@@ -512,6 +552,8 @@ int vg_sweep_create(const vg_sweep_desc* d, vg_sweep** out) {
     r.dp_off = dp;
     r.k = q.k;
     r.nudt = q.nu * d->dt;
+    r.kdt = split_f2(-q.k * d->dt);
+    r.nudt_f = (float)r.nudt;
     cells += (long long)q.nx * q.nv;
     xoff += q.nx;
     dp += (long long)r.ntiles * q.nx;
@@ -537,6 +579,7 @@ int vg_sweep_create(const vg_sweep_desc* d, vg_sweep** out) {
   SW_TRY(sw_alloc<float>(s, &s->g, (size_t)cells, nullptr, "sweep state"));
   SW_TRY(sw_alloc<double>(s, &s->e, (size_t)xoff, nullptr, "sweep fields"));
   SW_TRY(sw_alloc<double>(s, &s->mom, (size_t)xoff * MOM_STRIDE, nullptr, "sweep moments"));
+  SW_TRY(sw_alloc<float>(s, &s->e32, (size_t)xoff, nullptr, "sweep fields"));
   SW_TRY(sw_alloc<float2>(s, &s->dpart, (size_t)dp, nullptr, "sweep density partials"));
   SW_TRY(sw_alloc<cx<double>>(s, &s->tw64, FFT_NMAX, nullptr, "twiddles"));
   SW_TRY(sw_alloc<cx<float>>(s, &s->tw32, FFT_NMAX, nullptr, "twiddles"));
@@ -547,22 +590,33 @@ int vg_sweep_create(const vg_sweep_desc* d, vg_sweep** out) {
     tmp.tw32 = s->tw32;
     SW_TRY(cuda_status(launch_twiddles(tmp, 0), "twiddles"));
   }
-  // work lists and shared-memory sizes
-  std::vector<int2> col, row;
+  // work lists and shared-memory sizes: (run, tile) items grouped by nx,
+  // (run, row-pair group) items grouped by nv, field items by nx
+  std::map<int, std::vector<int2>> col_by, row_by;
   std::vector<int4> field;
   std::vector<SweepRunDev> field_runs;
-  size_t col_smem = 0, row_smem = 0, field_smem = 0;
+  size_t field_smem = 0;
   std::map<int, std::vector<int>> by_nx;
   for (int i = 0; i < s->n_runs; ++i) {
     const SweepRunDev& r = s->runs_h[i];
-    for (int t = 0; t < r.ntiles; ++t) col.push_back(make_int2(i, t));
+    for (int t = 0; t < r.ntiles; ++t) col_by[r.nx].push_back(make_int2(i, t));
     const int G = r.nv / row32_radix(r.nv);
     const int P = SWEEP_BLOCK / G;
-    for (int pg = 0; pg * P < r.nx / 2; ++pg) row.push_back(make_int2(i, pg));
+    for (int pg = 0; pg * P < r.nx / 2; ++pg) row_by[r.nv].push_back(make_int2(i, pg));
     by_nx[r.nx].push_back(i);
-    col_smem = std::max(col_smem, (size_t)(r.W / 2) * (sp_len<float>(r.nx) + COL32_PAD) * sizeof(cx<float>) +
-                                      (size_t)r.nx * sizeof(df32));
-    row_smem = std::max(row_smem, (size_t)P * row32_group_bytes(r.nv, row32_radix(r.nv)));
+  }
+  std::vector<int2> col, row;
+  for (auto& kv : col_by) {
+    s->col_nx.push_back(kv.first);
+    s->col_first.push_back((int)col.size());
+    s->col_count.push_back((int)kv.second.size());
+    col.insert(col.end(), kv.second.begin(), kv.second.end());
+  }
+  for (auto& kv : row_by) {
+    s->row_nv.push_back(kv.first);
+    s->row_first.push_back((int)row.size());
+    s->row_count.push_back((int)kv.second.size());
+    row.insert(row.end(), kv.second.begin(), kv.second.end());
   }
   for (auto& kv : by_nx) {
     const int nx = kv.first;
@@ -579,14 +633,8 @@ int vg_sweep_create(const vg_sweep_desc* d, vg_sweep** out) {
   SW_TRY(sw_alloc(s, &s->row_items, row.size(), row.data(), "sweep work list"));
   SW_TRY(sw_alloc(s, &s->field_items, field.size(), field.data(), "sweep work list"));
   SW_TRY(sw_alloc(s, &s->field_runs, field_runs.size(), field_runs.data(), "sweep work list"));
-  s->n_col = (int)col.size();
-  s->n_row = (int)row.size();
   s->n_field = (int)field.size();
-  s->col_smem = col_smem;
-  s->row_smem = row_smem;
   s->field_smem = field_smem;
-  SW_TRY(cuda_status(ensure_smem((const void*)k_sweep_col, col_smem), "sweep smem"));
-  SW_TRY(cuda_status(ensure_smem((const void*)k_sweep_row, row_smem), "sweep smem"));
   SW_TRY(cuda_status(ensure_smem((const void*)k_sweep_field, field_smem), "sweep smem"));
   SW_TRY(cuda_status(cudaDeviceSynchronize(), "sweep setup"));
 #undef SW_TRY

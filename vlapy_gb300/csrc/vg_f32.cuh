@@ -89,13 +89,20 @@ __device__ __forceinline__ void block_df_sum(df32 (&v)[NQ], df32* red) {
 }
 
 // Same, restricted to the G threads of one group (G a multiple of 32 or a
-// divisor of 32); red holds (G/32 rounded up) * NQ entries per group.
+// divisor of 32); red holds (G/32 rounded up) * NQ entries per group.  Within
+// a warp the partial sums are added in FP32 (a thread's partial covers a few
+// terms, the tree five levels: ~5e-7 relative), across warps in double-float.
 template <int NQ>
 __device__ __forceinline__ void group_df_sum(df32 (&v)[NQ], df32* red, int G, int t) {
   if (G >= 32) {
     const int lane = t & 31, wid = t >> 5, nw = G >> 5;
 #pragma unroll
-    for (int q = 0; q < NQ; ++q) v[q] = df_warp_sum(v[q]);
+    for (int q = 0; q < NQ; ++q) {
+      float x = v[q].hi + v[q].lo;
+#pragma unroll
+      for (int m = 16; m > 0; m >>= 1) x += __shfl_xor_sync(0xffffffffu, x, m);
+      v[q] = {x, 0.f};
+    }
     if (lane == 0) {
 #pragma unroll
       for (int q = 0; q < NQ; ++q) red[wid * NQ + q] = v[q];

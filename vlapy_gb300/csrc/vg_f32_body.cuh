@@ -37,14 +37,27 @@ __device__ __forceinline__ void col_tile(float* __restrict__ g, int nv, int c0, 
   // per unit m is the double-float product of kdt = -dkx dt and v (both split)
   const Ang aa = mul_angle(kdt, vhl[c0 + 2 * grp]);
   const Ang ab = mul_angle(kdt, vhl[c0 + 2 * grp + 1]);
-  two_real_rotate<float>(sg, NX, t, G, [&](int m, float& ca, float& sa, float& cb, float& sb) {
-    sincos_m((float)m, aa, sa, ca);
-    sincos_m((float)m, ab, sb, cb);
-    ca *= scale;
-    sa *= scale;
-    cb *= scale;
-    sb *= scale;
-  });
+  {
+    // phases exp(i m a) for this thread's bins m = t, t+G, ...: one sincos for
+    // the start, one for the step, complex products in between
+    float sa, ca, sb, cb, sga, cga, sgb, cgb;
+    sincos_m((float)t, aa, sa, ca);
+    sincos_m((float)t, ab, sb, cb);
+    sincos_m((float)G, aa, sga, cga);
+    sincos_m((float)G, ab, sgb, cgb);
+    two_real_rotate<float>(sg, NX, t, G, [&](int, float& pca, float& psa, float& pcb, float& psb) {
+      pca = ca * scale;
+      psa = sa * scale;
+      pcb = cb * scale;
+      psb = sb * scale;
+      const float na = sa * cga + ca * sga, nca = ca * cga - sa * sga;
+      const float nb = sb * cgb + cb * sgb, ncb = cb * cgb - sb * sgb;
+      sa = na;
+      ca = nca;
+      sb = nb;
+      cb = ncb;
+    });
+  }
   __syncthreads();
   block_fft<float, NX, true, R>(sg, t, tw);
   // density partial sums (trapz weights: 1/2 at the two v end points)
@@ -71,10 +84,14 @@ template <int N>
 __device__ __forceinline__ void kick_rotate(cx<float>* s, int t, int G, Ang ha, Ang hb,
                                             const cx<float>* __restrict__ F0) {
   const float sc = 1.f / N;
+  // half-angle rotations h(k) = exp(i k a / 2) for this thread's bins k = t, t+G, ...
+  // by one sincos for the start and one for the step, then complex products
+  float sa, ca, sb, cb, sga, cga, sgb, cgb;
+  sincos_m((float)t, ha, sa, ca);
+  sincos_m((float)t, hb, sb, cb);
+  sincos_m((float)G, ha, sga, cga);
+  sincos_m((float)G, hb, sgb, cgb);
   for (int k = t; k <= N / 2; k += G) {
-    float sa, ca, sb, cb;
-    sincos_m((float)k, ha, sa, ca);
-    sincos_m((float)k, hb, sb, cb);
     // P = (1 - 2 sin^2, 2 sin cos) of the half angle; P - 1 = (-2 sin^2, 2 sin cos)
     const float pa_m1r = -2.f * sa * sa, pa_i = 2.f * sa * ca, pa_r = 1.f + pa_m1r;
     const float pb_m1r = -2.f * sb * sb, pb_i = 2.f * sb * cb, pb_r = 1.f + pb_m1r;
@@ -83,17 +100,23 @@ __device__ __forceinline__ void kick_rotate(cx<float>* s, int t, int G, Ang ha, 
       const cx<float> z = s[sp<float>(k)];
       // real bins: only Re(P) survives
       s[sp<float>(k)] = {(pa_r * z.x + pa_m1r * f0.x) * sc, (pb_r * z.y + pb_m1r * f0.x) * sc};
-      continue;
+    } else {
+      const cx<float> zk = s[sp<float>(k)], zm = s[sp<float>(N - k)];
+      const cx<float> fa = {(zk.x + zm.x) * 0.5f, (zk.y - zm.y) * 0.5f};
+      const cx<float> fb = {(zk.y + zm.y) * 0.5f, (zm.x - zk.x) * 0.5f};
+      const cx<float> ga = {(pa_r * fa.x - pa_i * fa.y + pa_m1r * f0.x - pa_i * f0.y) * sc,
+                            (pa_r * fa.y + pa_i * fa.x + pa_m1r * f0.y + pa_i * f0.x) * sc};
+      const cx<float> gb = {(pb_r * fb.x - pb_i * fb.y + pb_m1r * f0.x - pb_i * f0.y) * sc,
+                            (pb_r * fb.y + pb_i * fb.x + pb_m1r * f0.y + pb_i * f0.x) * sc};
+      s[sp<float>(k)] = {ga.x - gb.y, ga.y + gb.x};
+      s[sp<float>(N - k)] = {ga.x + gb.y, gb.x - ga.y};
     }
-    const cx<float> zk = s[sp<float>(k)], zm = s[sp<float>(N - k)];
-    const cx<float> fa = {(zk.x + zm.x) * 0.5f, (zk.y - zm.y) * 0.5f};
-    const cx<float> fb = {(zk.y + zm.y) * 0.5f, (zm.x - zk.x) * 0.5f};
-    const cx<float> ga = {(pa_r * fa.x - pa_i * fa.y + pa_m1r * f0.x - pa_i * f0.y) * sc,
-                          (pa_r * fa.y + pa_i * fa.x + pa_m1r * f0.y + pa_i * f0.x) * sc};
-    const cx<float> gb = {(pb_r * fb.x - pb_i * fb.y + pb_m1r * f0.x - pb_i * f0.y) * sc,
-                          (pb_r * fb.y + pb_i * fb.x + pb_m1r * f0.y + pb_i * f0.x) * sc};
-    s[sp<float>(k)] = {ga.x - gb.y, ga.y + gb.x};
-    s[sp<float>(N - k)] = {ga.x + gb.y, gb.x - ga.y};
+    const float na = sa * cga + ca * sga, nca = ca * cga - sa * sga;
+    const float nb = sb * cgb + cb * sgb, ncb = cb * cgb - sb * sgb;
+    sa = na;
+    ca = nca;
+    sb = nb;
+    cb = ncb;
   }
 }
 

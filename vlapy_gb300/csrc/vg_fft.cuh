@@ -159,14 +159,15 @@ template <typename T, typename PhaseFn>
 __device__ __forceinline__ void two_real_rotate(cx<T>* s, int N, int t, int G, PhaseFn phase) {
   for (int k = t; k <= N / 2; k += G) {
     T ca, sa, cb, sb;
+    // one phase() call per visited bin, in increasing k (callers may step a
+    // recurrence inside it)
+    phase(k, ca, sa, cb, sb);
     if (k == 0) {
-      phase(0, ca, sa, cb, sb);
       const cx<T> z = s[0];
       // DC bins of both real sequences are real: only Re(P) survives
       s[0] = {z.x * ca, z.y * cb};
       continue;
     }
-    phase(k, ca, sa, cb, sb);
     if (2 * k == N) {
       const cx<T> z = s[sp<T>(k)];
       s[sp<T>(k)] = {z.x * ca, z.y * cb};

@@ -326,6 +326,143 @@ def fp64_plain_sweep(w, steps=3):
     return runs_per_s, per
 
 
+def _damping_errors(t, sw_ref, e_ref, sw, e_hist, t_max=60.0):
+    """Relative damping-rate error of each run against the reference runs
+    (one peak-envelope fit of |E_1|(t) on [5, t_max] for both)."""
+    from vlapy_gb300.diagnostics import damping_fit, mode_amplitude
+    out = []
+    for i in range(sw.n_runs):
+        rf, _ = damping_fit(t, mode_amplitude(sw_ref.e_of(e_ref, i).cpu().numpy()), t_min=5.0, t_max=t_max)
+        rg, _ = damping_fit(t, mode_amplitude(sw.e_of(e_hist, i).cpu().numpy()), t_min=5.0, t_max=t_max)
+        out.append(abs(rg - rf) / abs(rf) if np.isfinite(rf) and np.isfinite(rg) and rf != 0 else np.nan)
+    return np.array(out)
+
+
+def learned_path(args, w):
+    """The learned coarse-velocity path (runs of the sweep distribution at
+    nx = 64): train the corrector on pairs from fine (nv = 1024) runs, judge
+    the corrected coarse (nv = 128) runs against the fine runs on held-out
+    seeds, and time the corrected coarse step against the fine FP32 sweep
+    and the plain FP64 step of the same runs."""
+    import torch
+    from vlapy_gb300 import corrector as cm
+    from vlapy_gb300 import initializers as I
+    from vlapy_gb300.plan import Plan
+    from vlapy_gb300.sweep import Sweep
+    nsteps, nx = SWEEP_STEPS, 64
+    t0 = time.perf_counter()
+    data = cm.generate_pairs(cm.corrector_runs(args.learned_train, seed=5), n_steps=nsteps)
+    torch.cuda.synchronize()
+    gen_s = time.perf_counter() - t0
+    tau = cm.output_scale(data)
+    n_eval = 256
+    corr = cm.Corrector(max(128, n_eval) * nx, tau=tau)
+    t0 = time.perf_counter()
+    hist = cm.train(corr, data, epochs=4)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t0
+    del data
+    held = cm.generate_pairs(cm.corrector_runs(n_eval, seed=6), n_steps=nsteps)
+    zero = cm.Corrector(128 * nx, params=np.zeros(corr.n_params, np.float32), tau=tau)
+    base_loss = cm.evaluate(zero, held)  # zero output: the uncorrected coarse step
+    zero.close()
+    loss = cm.evaluate(corr, held)
+    del held
+    # held-out rollouts: fine FP32 sweep (the judge), coarse, corrected coarse
+    ev = cm.corrector_runs(n_eval, seed=6)
+    fine, coarse, corrected = (Sweep([dict(r, nv=nv) for r in ev]) for nv in (1024, cm.NV, cm.NV))
+    hists = []
+    for sw in (fine, coarse):
+        sw.reset()
+        eh, sh = sw.history(nsteps)
+        sw.run_steps(nsteps, eh, sh)
+        hists.append((eh, sh))
+    corrected.reset()
+    ek, sk = corrected.history(nsteps)
+    cm.run_corrected(corrected, corr, nsteps, ek, sk)
+    torch.cuda.synchronize()
+    t = w["dt"] * np.arange(1, nsteps + 1)
+    dr_c = _damping_errors(t, fine, hists[0][0], coarse, hists[1][0])
+    dr_k = _damping_errors(t, fine, hists[0][0], corrected, ek)
+    e2 = [h[1][:, :, 3].cpu().numpy() for h in hists] + [sk[:, :, 3].cpu().numpy()]
+    e2_err = [np.linalg.norm(e - e2[0], axis=0) / np.linalg.norm(e2[0], axis=0) for e in e2[1:]]
+
+    def stats(a):
+        a = a[np.isfinite(a)]
+        return {"median": float(np.median(a)), "max": float(a.max()), "frac_within_1pct": float(np.mean(a <= 0.01)),
+                "n": int(a.size)}
+
+    # throughput on 2048 runs: corrected coarse step vs fine FP32 sweep step
+    runs = cm.corrector_runs(2048, seed=7)
+    K = max(5, min(args.steps, 20))
+    out = {}
+    for name, nv in (("learned", cm.NV), ("fine_fp32", 1024)):
+        sw = Sweep([dict(r, nv=nv) for r in runs])
+        sw.reset()
+        big = cm.Corrector(sw.cells // cm.NV, params=corr.params, tau=tau) if name == "learned" else None
+        step = (lambda n: cm.run_corrected(sw, big, n)) if big else (lambda n: sw.run_steps(n))
+        step(3)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        step(K)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / K
+        out[name] = {"ms_per_step": ms, "runs_per_s": len(runs) / (ms / 1e3 * nsteps)}
+        if big:
+            # tensor roofline of the network alone: forward FLOPs of one apply over its time
+            g = sw.state_view().view(-1, cm.NV)
+            rows = g.shape[0]
+            flops = 2.0 * rows * cm.NV * 5 * (16 * 64 + 64 * 64 + 64 * 64 + 64 * 8)
+            prev = g.clone()
+            e0.record()
+            for _ in range(K):
+                big.apply(g, prev, None, out=prev, group_rows=nx)
+            e1.record()
+            torch.cuda.synchronize()
+            ams = e0.elapsed_time(e1) / K
+            pk = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["bf16_tflops"] if os.path.exists(
+                os.path.join(ROOT, "MEASURED_PEAKS.json")) else 1900.0
+            out[name]["corrector_ms"] = ams
+            out[name]["tensor_roofline"] = {"bound": "tensor", "achieved": flops / (ams / 1e3) / 1e12, "peak": pk,
+                                            "unit": "TFLOP/s", "frac": flops / (ams / 1e3) / 1e12 / pk,
+                                            "flops_per_apply": flops,
+                                            "note": "mma.sync m16n8k16 BF16 (FP32 accumulate); padded channels "
+                                                    "counted as issued"}
+            big.close()
+        sw.close()
+    # plain FP64 GPU step of one 64x1024 run of the distribution
+    r = runs[0]
+    dx, x, kx, inv = I.initialize_spatial_quantities(0.0, 2 * np.pi / r["k"], nx)
+    dv, v, kv = I.initialize_velocity_quantities(w["vmax"], 1024)
+    pl = Plan(nx, 1024, x, v, kx, kv, inv, dx, dv, dt=w["dt"], nu=max(r["nu"], 1e-4), collision="dg")
+    f = torch.as_tensor(I.initialize_distribution(nx, 1024, w["vmax"]) * (1 + r["amplitude"] * np.cos(r["k"] * x))[:, None],
+                        device="cuda")
+    e = torch.zeros(nx, dtype=torch.float64, device="cuda")
+    tb = torch.as_tensor(w["dt"] * np.arange(8), device="cuda")
+    pl.run_steps(f, e, None, tb, None, 0, 2, use_graph=False)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    pl.run_steps(f, e, None, tb, None, 0, 3, use_graph=False)
+    e1.record()
+    torch.cuda.synchronize()
+    fp64_ms = e0.elapsed_time(e1) / 3
+    pl.close()
+    out["plain_fp64"] = {"ms_per_run_step": fp64_ms, "runs_per_s": 1.0 / (fp64_ms / 1e3 * nsteps)}
+    return {
+        "workload": "%d training runs (seed 5) and %d held-out runs (seed 6) of the sweep distribution at nx=64; "
+                    "fine nv=1024, coarse nv=128, vmax=6.4, dt=0.1, %d steps" % (args.learned_train, n_eval, nsteps),
+        "pairs_s": gen_s, "train_s": train_s, "train_loss_by_epoch": hist, "tau": tau,
+        "heldout_one_step_loss": {"uncorrected": base_loss, "corrected": loss, "ratio": loss / base_loss},
+        "damping_rate_rel_err_vs_fine": {"coarse": stats(dr_c), "corrected": stats(dr_k)},
+        "field_energy_history_rel_err_vs_fine": {"coarse": stats(e2_err[0]), "corrected": stats(e2_err[1])},
+        "throughput_2048_runs": out,
+        "judge": "fine runs of the FP32 batched sweep (the GPU tests hold it to the FP64 oracle)",
+    }
+
+
 def _oracle_sweep_sample(args):
     """One pool task: oracle steps of one sampled sweep run (host cores)."""
     r, steps, vmax, dt = args
@@ -410,6 +547,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--runs", type=int, default=None, help="sweep size (default: the 4096-run workload)")
     ap.add_argument("--no-fp64-compare", action="store_true", help="skip the plain FP64 GPU sweep estimate")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned coarse-velocity path")
+    ap.add_argument("--learned-train", type=int, default=2048, help="fine training runs of the learned path")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -538,9 +677,10 @@ def main_sweep(args, w, rank, world):
         fp64 = {"runs_per_s": fp64_rps, "ms_per_step_by_shape": fp64_per,
                 "how": "FP64 parity step, one run at a time, timed on one run per shape and "
                        "weighted by the shape counts"}
+    learned = None if args.no_learned else learned_path(args, w)
     cpu = None
     if not args.no_cpu_baseline:
-        cval, crps, cores, n, steps, wall = cpu_baseline_sweep(w, n_sample=36, steps=60)
+        cval, crps, cores, n, steps, wall = cpu_baseline_sweep(w, n_sample=36, steps=360)
         cpu = {"value": cval, "unit": "cell-updates/s", "cores": cores, "kind": "port", "runs_per_s": crps,
                "sample": "%d sweep runs (stratified over the 9 shapes) x %d full oracle steps, one process per "
                          "core, %.1f s wall" % (n, steps, wall)}
@@ -550,6 +690,7 @@ def main_sweep(args, w, rank, world):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": cfg,
         "runs_per_s": runs_per_s,
         "fp64_plain_gpu": fp64,
+        "learned_path": learned,
         "e2e": {"value": world * cells * args.steps / e2e_sec, "unit": "cell-updates/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,

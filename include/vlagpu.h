@@ -203,6 +203,19 @@ int vg_sweep_run_steps(vg_sweep* sweep, int32_t nsteps, double* e_hist, double* 
                        int32_t hist_rows, int32_t hist_row0, int32_t use_graph, vg_stream stream);
 /* f = g + f0 of one run as float64 [nx][nv] and its e[nx] (DEVICE pointers) */
 int vg_sweep_read_run(vg_sweep* sweep, int32_t run, double* f_out, double* e_out, vg_stream stream);
+/* copy every run's FP32 deviation g = f - f0 (runs back to back, [nx][nv]
+ * each) and field e (packed like e_hist rows) to / from caller DEVICE
+ * buffers; either pointer may be NULL.  set_state also refreshes the FP32
+ * copy of e that the first half-kick of the next vg_sweep_run_steps reads.
+ * No reference counterpart: they let a caller checkpoint a sweep, or move
+ * states between sweeps of different grids (the coarse-grid corrector). */
+int vg_sweep_get_state(vg_sweep* sweep, float* g_out, double* e_out, vg_stream stream);
+int vg_sweep_set_state(vg_sweep* sweep, const float* g_in, const double* e_in, vg_stream stream);
+/* the sweep's own device buffers g [cells] and e [x_points] (valid for its
+ * lifetime); a caller may modify g in place between vg_sweep_run_steps
+ * calls on the same stream (the corrector does).  Writing e this way would
+ * bypass the FP32 copy the kicks read: use vg_sweep_set_state for e. */
+int vg_sweep_state_ptr(vg_sweep* sweep, float** g, double** e);
 /* per-kernel timing of vg_sweep_run_steps (same contract as vg_profile_*) */
 int vg_sweep_profile_enable(vg_sweep* sweep, int32_t enable);
 int vg_sweep_profile_read(vg_sweep* sweep, vg_prof_entry* out, int32_t max, int32_t* n_out);
@@ -217,6 +230,58 @@ int vg_sweep_profile_read(vg_sweep* sweep, vg_prof_entry* out, int32_t max, int3
  * vlapy/manager.py:144-146). */
 int vg_profile_enable(vg_plan* plan, int32_t enable);
 int vg_profile_read(vg_plan* plan, vg_prof_entry* out, int32_t max, int32_t* n_out);
+
+/* ---- learned coarse-velocity corrector -------------------------------- */
+/* No reference counterpart.  A 1-D conv net along v applied to each x row
+ * of a coarse run (nv = 128) after a coarse step:
+ *   c = P(s * tau * net(d / s, v / vmax, row_feat, d_prev / s)),
+ *   g <- m + (d - Pd) + (Pd + c) * min(1, |Pd| / |Pd + c|),
+ * m = the mean of the row's group of group_rows consecutive rows (the
+ * x-mean of a run when a group is one run's x rows; group_rows = 0: m = 0),
+ * d = g - m, d_prev the same of the row before the coarse step, s the RMS
+ * of d over the row, tau a global output scale, row_feat one scalar per row
+ * (the collision-rate channel), P the orthogonal projection that removes
+ * the v-Fourier modes |m| < protect_modes of the 128-point row (those
+ * modes, which carry the density and the field, are never corrected), and
+ * the min() cap keeps the corrected high part no longer in L2 norm than the
+ * coarse step left it.  Four conv1d layers, kernel 5, zero padding 2, 64
+ * channels, ReLU after the first three; BF16 tensor cores with FP32
+ * accumulation.  Parameters are FP32 in PyTorch conv1d order: W1
+ * [64][16][5] (input channels 4..15 unused), b1 [64], W2, b2, W3, b3
+ * [64][64][5], [64], W4 [1][64][5], b4 [1] (vg_corr_num_params() = 46593
+ * floats).  Loss = mean over cells of (P(net - want))^2 with want =
+ * ((target - its group mean) - d) / (s tau). */
+typedef struct vg_corrector vg_corrector;
+#define VG_CORR_NV 128
+/* One batch of rows; all DEVICE pointers, FP32, [rows][128] unless noted. */
+typedef struct vg_corr_batch {
+  const float* g;         /* state after the coarse step */
+  const float* g_prev;    /* state before it; NULL: a zero channel */
+  const float* row_feat;  /* [rows]; NULL: a zero channel */
+  const float* target;    /* loss, gradients and training only */
+  int32_t rows;           /* <= max_rows */
+  int32_t group_rows;     /* 0, or a divisor of rows */
+} vg_corr_batch;
+int vg_corr_num_params(void);
+int vg_corr_create(int32_t max_rows, int32_t protect_modes, float vmax, float tau, const float* params_host,
+                   vg_corrector** out);
+int vg_corr_destroy(vg_corrector* corr);
+int vg_corr_set_tau(vg_corrector* corr, float tau);
+int vg_corr_get_params(vg_corrector* corr, float* host_out);
+/* also clears the optimiser state */
+int vg_corr_set_params(vg_corrector* corr, const float* host_in);
+/* g_out may alias batch->g (in-place correction) */
+int vg_corr_apply(vg_corrector* corr, const vg_corr_batch* batch, float* g_out, vg_stream stream);
+/* loss only (synchronises the stream) */
+int vg_corr_loss(vg_corrector* corr, const vg_corr_batch* batch, double* loss_out, vg_stream stream);
+/* loss and its gradient w.r.t. all parameters (HOST grad_host, PyTorch
+ * order; NULL to keep it on the device); synchronises the stream */
+int vg_corr_gradients(vg_corrector* corr, const vg_corr_batch* batch, float* grad_host, double* loss_out,
+                      vg_stream stream);
+/* one Adam step (beta 0.9, 0.999, eps 1e-8) on the loss of this batch;
+ * loss_out may be NULL (then nothing synchronises) */
+int vg_corr_train_step(vg_corrector* corr, const vg_corr_batch* batch, float lr, double* loss_out,
+                       vg_stream stream);
 
 #ifdef __cplusplus
 }

@@ -64,7 +64,10 @@ def test_plan_create_rejects_bad_descriptor(lib_path):
 
 def test_struct_layout_matches_header(lib_path):
     from vlapy_gb300 import _lib
-    src = "#include <stdio.h>\n#include \"vlagpu.h\"\nint main(){printf(\"%zu %zu %zu\", sizeof(vg_run_desc), sizeof(vg_history), sizeof(vg_pulse));}"
+    names = ["vg_run_desc", "vg_history", "vg_pulse", "vg_sweep_run", "vg_sweep_desc", "vg_prof_entry",
+             "vg_corr_batch"]
+    src = ("#include <stdio.h>\n#include \"vlagpu.h\"\nint main(){"
+           + "".join('printf("%%zu ", sizeof(%s));' % n for n in names) + "}")
     cc = shutil.which("gcc") or shutil.which("cc")
     if cc is None:
         pytest.skip("no C compiler")
@@ -76,8 +79,9 @@ def test_struct_layout_matches_header(lib_path):
         exe = os.path.join(td, "s")
         subprocess.check_call([cc, "-I", os.path.join(ROOT, "include"), c, "-o", exe])
         out = subprocess.check_output([exe]).decode().split()
-    assert [int(x) for x in out] == [ctypes.sizeof(_lib.VgRunDesc), ctypes.sizeof(_lib.VgHistory),
-                                     ctypes.sizeof(_lib.VgPulse)]
+    assert [int(x) for x in out] == [ctypes.sizeof(t) for t in (
+        _lib.VgRunDesc, _lib.VgHistory, _lib.VgPulse, _lib.VgSweepRun, _lib.VgSweepDesc, _lib.VgProfEntry,
+        _lib.VgCorrBatch)]
 
 
 def test_pairwise_tables():
@@ -132,3 +136,71 @@ def test_initializers_match_oracle():
         np.testing.assert_array_equal(a, b)
     p = I.specify_epw_params_to_dict(0.3, I.make_default_params_dictionary())
     np.testing.assert_allclose(p["w_epw"] + 1j * p["nu_ld"], vo.epw_root(0.3), rtol=1e-14)
+
+
+def test_corrector_layout_and_restriction():
+    """Corrector parameter layout (header, module, oracle agree) and the
+    spectral restriction fine -> coarse velocity grid."""
+    import re
+    from oracle import corrector_oracle as co
+    from vlapy_gb300 import corrector as cm
+    from vlapy_gb300.initializers import initialize_distribution
+    hdr = open(os.path.join(ROOT, "include", "vlagpu.h")).read()
+    assert int(re.search(r"vg_corr_num_params\(\) =\s*\*?\s*(\d+)\s*\*?\s*floats", hdr).group(1)) == co.N_PARAMS
+    assert cm.SHAPES == co.SHAPES
+    p = cm.init_params(0)
+    assert p.size == co.N_PARAMS and p.dtype == np.float32
+    d = co.unpack(p)
+    assert float(d["W4"].abs().max()) == 0.0 and float(d["b4"].abs().max()) == 0.0
+    assert float(d["W1"][:, 4:].abs().max()) == 0.0
+    np.testing.assert_array_equal(co.pack(d), p)
+    # restriction: exact on what the coarse grid represents, and maps the
+    # fine Maxwellian onto the coarse one
+    R = cm.restriction_matrix(1024, 128)
+    vf = -6.4 + 12.8 / 1024 * (np.arange(1024) + 0.5)
+    vc = -6.4 + 12.8 / 128 * (np.arange(128) + 0.5)
+    for m in (0, 1, 5, 63):
+        kv = 2 * np.pi * m / 12.8
+        np.testing.assert_allclose(R @ np.cos(kv * vf + 0.3), np.cos(kv * vc + 0.3), atol=1e-12)
+    mf = initialize_distribution(1, 1024, 6.4)[0]
+    mc = initialize_distribution(1, 128, 6.4)[0]
+    assert np.abs(R @ mf - mc).max() < 1e-9
+    # the collision-rate feature: zero without collisions, about 1 at nu = 1e-2
+    f = cm.nu_feature([0.0, 1e-5, 1e-2])
+    assert f[0] == 0.0 and 0.09 < f[1] < 0.11 and 0.99 < f[2] < 1.01
+
+
+def test_corrector_oracle_emulation_close_to_fp64():
+    """The BF16-emulating oracle differs from the FP64 network by BF16 noise only."""
+    torch = pytest.importorskip("torch")
+    from oracle import corrector_oracle as co
+    from vlapy_gb300 import corrector as cm
+    rng = np.random.default_rng(3)
+    p = cm.init_params(1)
+    d = co.unpack(p)
+    d["W4"][:] = torch.as_tensor(rng.uniform(-0.1, 0.1, (1, 64, 5)))
+    p = co.pack(d)
+    g = rng.standard_normal((20, 128)).astype(np.float32)
+    t = (g + 0.01 * rng.standard_normal((20, 128))).astype(np.float32)
+    feat = np.full(20, 0.5, np.float32)
+    le, ge = co.loss_and_grads(p, g, feat, t, 6.4, 0.01, emulate=True)
+    lx, gx = co.loss_and_grads(p, g, feat, t, 6.4, 0.01, emulate=False)
+    assert abs(le - lx) < 1e-3 * lx
+    # BF16 operands in the forward pass move the early-layer gradients by a
+    # few per cent on random data (sums with heavy cancellation)
+    assert np.linalg.norm(ge - gx) < 0.15 * np.linalg.norm(gx)
+
+
+def test_damping_fit_matches_oracle_fit():
+    """The product's damping diagnostic and the oracle's fit agree on a
+    synthetic damped standing wave and on an oracle Landau run."""
+    from oracle import vlapy_oracle as vo
+    from vlapy_gb300.diagnostics import damping_fit, mode_amplitude
+    t = 0.1 * np.arange(1, 1201)
+    amp = np.abs(np.exp(-0.0153 * t) * np.cos(1.41 * t + 0.2))
+    r, w = damping_fit(t, amp, t_min=5.0)
+    assert abs(r + 0.0153) < 1e-4 and abs(w - 1.41) < 1e-3
+    assert (r, w) == pytest.approx(vo.envelope_fit(t, amp, t_min=5.0), rel=1e-12)
+    e = np.random.default_rng(0).standard_normal((50, 16))
+    np.testing.assert_array_equal(mode_amplitude(e), vo.mode_amplitude(e))
+    assert np.isnan(damping_fit(t[:20], amp[:20])[0])

@@ -61,6 +61,11 @@ class VgSweepDesc(C.Structure):
                 ("runs", C.POINTER(VgSweepRun))]
 
 
+class VgCorrBatch(C.Structure):
+    _fields_ = [("g", C.c_void_p), ("g_prev", C.c_void_p), ("row_feat", C.c_void_p), ("target", C.c_void_p),
+                ("rows", C.c_int32), ("group_rows", C.c_int32)]
+
+
 class VgProfEntry(C.Structure):
     _fields_ = [("name", C.c_char * 32), ("launches", C.c_int64), ("total_ms", C.c_double),
                 ("bytes_per_launch", C.c_double)]
@@ -94,11 +99,26 @@ EXPORTS = {
     "vg_sweep_run_steps": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32,
                                      C.c_int32, C.c_void_p]),
     "vg_sweep_read_run": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "vg_sweep_get_state": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "vg_sweep_set_state": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "vg_sweep_state_ptr": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]),
     "vg_sweep_profile_enable": (C.c_int, [C.c_void_p, C.c_int32]),
     "vg_sweep_profile_read": (C.c_int, [C.c_void_p, C.POINTER(VgProfEntry), C.c_int32, C.POINTER(C.c_int32)]),
     "vg_profile_enable": (C.c_int, [C.c_void_p, C.c_int32]),
     "vg_profile_read": (C.c_int, [C.c_void_p, C.POINTER(VgProfEntry), C.c_int32,
                                   C.POINTER(C.c_int32)]),
+    "vg_corr_num_params": (C.c_int, []),
+    "vg_corr_create": (C.c_int, [C.c_int32, C.c_int32, C.c_float, C.c_float, C.c_void_p, C.POINTER(C.c_void_p)]),
+    "vg_corr_destroy": (C.c_int, [C.c_void_p]),
+    "vg_corr_set_tau": (C.c_int, [C.c_void_p, C.c_float]),
+    "vg_corr_get_params": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "vg_corr_set_params": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "vg_corr_apply": (C.c_int, [C.c_void_p, C.POINTER(VgCorrBatch), C.c_void_p, C.c_void_p]),
+    "vg_corr_loss": (C.c_int, [C.c_void_p, C.POINTER(VgCorrBatch), C.POINTER(C.c_double), C.c_void_p]),
+    "vg_corr_gradients": (C.c_int, [C.c_void_p, C.POINTER(VgCorrBatch), C.c_void_p, C.POINTER(C.c_double),
+                                    C.c_void_p]),
+    "vg_corr_train_step": (C.c_int, [C.c_void_p, C.POINTER(VgCorrBatch), C.c_float, C.POINTER(C.c_double),
+                                     C.c_void_p]),
 }
 
 _lib = None

@@ -173,7 +173,7 @@ void free_plan(vg_plan* p) {
   delete static_cast<ProfState*>(p->prof);
   if (p->f32) {
     F32Plan* q = p->f32;
-    void* qp[] = {q->F0, q->v32, q->f0_32, q->S, q->Mv, q->D, q->dpart, q->mpart, q->vhl, q->e32};
+    void* qp[] = {q->F0, q->v32, q->f0_32, q->S, q->Mv, q->D, q->dpart, q->mpart, q->vhl, q->e32, q->rc_dev};
     for (void* x : qp)
       if (x) cudaFree(x);
     delete q;
@@ -423,6 +423,10 @@ int setup_f32(vg_plan* p, const vg_run_desc* d) {
   q->rc.dv_sq = dv2;
   q->rc.dkv = q->dkv;
   for (int k = 0; k < 7; ++k) q->rc.f0m[k] = mom[k];
+  q->rc.dv2f = split_f2(dv);
+  q->rc.idv2f = split_f2(1.0 / dv2);
+  for (int k = 0; k < 3; ++k) q->rc.f0m2f[k] = split_f2(mom[k]);
+  VG_CHECK(upload(&q->rc_dev, std::vector<RowConsts>(1, q->rc), "f32 constants"));
   int dev = 0, nsm = 1;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);

@@ -40,6 +40,14 @@ __device__ __forceinline__ df32 df_warp_sum(df32 a) {
   return a;
 }
 __device__ __forceinline__ double df_to_double(df32 a) { return (double)a.hi + (double)a.lo; }
+// double-float product (TwoProd by FMA); accurate to ~1e-14 relative
+__device__ __forceinline__ df32 df_mul(df32 a, df32 b) {
+  const float p = a.hi * b.hi;
+  const float e = fmaf(a.hi, b.hi, -p) + fmaf(a.hi, b.lo, a.lo * b.hi);
+  const float hi = p + e;
+  return {hi, e - (hi - p)};
+}
+__device__ __forceinline__ float df_round(df32 a) { return a.hi + a.lo; }
 
 // ---- accurate phases ---------------------------------------------------
 struct Ang {

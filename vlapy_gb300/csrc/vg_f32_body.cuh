@@ -78,6 +78,15 @@ __device__ __forceinline__ void col_tile(float* __restrict__ g, int nv, int c0, 
 }
 
 
+// Moment slot q of one row (0..5: n, j, T, q, fv4, vN; 6: trapz(f^2);
+// 7: trapz(f log f)) from the raw double-float sums the row pass leaves in
+// its [8]-double slots: dv * sum + the background's share, in FP64.
+__device__ __forceinline__ double row_moment(const double* __restrict__ slots, int q, const RowConsts& rc) {
+  const df32 m = reinterpret_cast<const df32*>(slots)[q];
+  const double sum = (double)m.hi + (double)m.lo;
+  return q < 7 ? rc.dv * sum + rc.f0m[q] : rc.dv * sum;
+}
+
 // rotation of one packed row pair with the delta-f background term; the 1/N of
 // the inverse transform is folded in.  ha/hb: half-angle per kv index.
 template <int N>
@@ -137,7 +146,7 @@ __device__ __forceinline__ void kick(cx<float>* s, int t, float hk, float ea, fl
 
 // Fokker-Planck step of one row stored at x (stride 2 floats) in delta-f form.
 template <int N, int R>
-__device__ __forceinline__ void collide_row(float* x, int t, const RowConsts& rc, double nudt, float nudt_f,
+__device__ __forceinline__ void collide_row(float* x, int t, const RowConsts& rc, float2 nudt2, float nudt_f,
                                             int dougherty, df32* red, float* pcr) {
   constexpr int G = N / R;
   // moments of g over the thread's chunk: sum w g, sum w g v, sum w g v^2
@@ -159,22 +168,26 @@ __device__ __forceinline__ void collide_row(float* x, int t, const RowConsts& rc
     mv[2] = {a2, 0.f};
   }
   group_df_sum<3>(mv, red, G, t);
-  // per-row FP64 scalars: one thread computes them (FP64 is scarce on this
-  // part), the group reads them back as FP32 coefficients
+  // per-row scalars in double-float by one thread; the group reads them back
+  // as FP32 coefficients, each rounded once
   float* sc = reinterpret_cast<float*>(red);
   if (t == 0) {
-    const double M0 = rc.dv * df_to_double(mv[0]) + rc.f0m[0];
-    const double M1 = rc.dv * df_to_double(mv[1]) + rc.f0m[1];
-    const double M2 = rc.dv * df_to_double(mv[2]) + rc.f0m[2];
+    const df32 dv = {rc.dv2f.x, rc.dv2f.y};
+    const df32 M0 = df_add(df_mul(dv, mv[0]), {rc.f0m2f[0].x, rc.f0m2f[0].y});
+    const df32 M1 = df_add(df_mul(dv, mv[1]), {rc.f0m2f[1].x, rc.f0m2f[1].y});
+    const df32 M2 = df_add(df_mul(dv, mv[2]), {rc.f0m2f[2].x, rc.f0m2f[2].y});
     // DG: vbar = trapz(f v), v0t^2 = trapz(f (v - vbar)^2) = M2 + vbar^2 (M0 - 2)
     // LB: v0t^2 = trapz(f v^2), no drift
-    const double vbar = dougherty ? M1 : 0.0;
-    const double vth = dougherty ? M2 + vbar * vbar * (M0 - 2.0) : M2;
-    sc[0] = (float)(-vth / rc.dv_sq);
-    sc[1] = (float)(1.0 + nudt * (2.0 * vth / rc.dv_sq));
-    sc[2] = (float)vbar;
-    sc[3] = (float)(nudt * vth);
-    sc[4] = (float)(nudt * vbar);
+    const df32 vbar = dougherty ? M1 : df32{0.f, 0.f};
+    const df32 vth = dougherty ? df_add(M2, df_mul(df_mul(vbar, vbar), df_add(M0, {-2.f, 0.f}))) : M2;
+    const df32 nd = {nudt2.x, nudt2.y};
+    const df32 a = df_mul(vth, {rc.idv2f.x, rc.idv2f.y});  // vth / dv^2
+    const df32 na = df_mul(nd, a);
+    sc[0] = -df_round(a);
+    sc[1] = df_round(df_add({1.f, 0.f}, {2.f * na.hi, 2.f * na.lo}));
+    sc[2] = df_round(vbar);
+    sc[3] = df_round(df_mul(nd, vth));
+    sc[4] = df_round(df_mul(nd, vbar));
   }
   __syncthreads();
   const float Af = sc[0], bdiag = sc[1], vb = sc[2], cs = sc[3], cd = sc[4];
@@ -221,8 +234,8 @@ __device__ __forceinline__ void row_pair(const RowArgs& a, int pair, unsigned ch
   if (a.hk1 != 0.f) kick<N, R>(s, t, a.hk1, ea, eb, a.F0, a.tw);
   float* sx = reinterpret_cast<float*>(s);
   if (a.fp) {
-    collide_row<N, R>(sx, t, a.rc, a.nudt, a.nudt_f, a.dougherty, red, pcr);
-    collide_row<N, R>(sx + 1, t, a.rc, a.nudt, a.nudt_f, a.dougherty, red, pcr);
+    collide_row<N, R>(sx, t, *a.rc, a.nudt2, a.nudt_f, a.dougherty, red, pcr);
+    collide_row<N, R>(sx + 1, t, *a.rc, a.nudt2, a.nudt_f, a.dougherty, red, pcr);
   }
   if (a.want_mom) {
     // n, j, T, q, fv4, vN (sums of w g v^p), sum w g^2, sum w g f0, sum w f log f
@@ -232,7 +245,7 @@ __device__ __forceinline__ void row_pair(const RowArgs& a, int pair, unsigned ch
     for (int i = 0; i < R; ++i) {
       const int j = t * R + i;
       const float w = (j == 0 || j == N - 1) ? 0.5f : 1.f;
-      const float vj = a.rc.v[j], f0j = a.rc.f0[j];
+      const float vj = a.rc->v[j], f0j = a.rc->f0[j];
       const cx<float> z = s[sp<float>(j)];
       float pa = w * z.x, pb = w * z.y;
 #pragma unroll
@@ -258,15 +271,17 @@ __device__ __forceinline__ void row_pair(const RowArgs& a, int pair, unsigned ch
     group_df_sum<9>(mv, red, G, t);
     group_df_sum<9>(mw, red, G, t);
     if (t == 0) {
-      for (int r = 0; r < 2; ++r) {
-        const int row = r ? rb : ra;
-        if (!(r ? vb : va)) continue;
-        const df32* m = r ? mw : mv;
-        double* out = a.mom + (size_t)row * MOM_STRIDE;
-        for (int p = 0; p < 6; ++p) out[p] = a.rc.dv * df_to_double(m[p]) + a.rc.f0m[p];
-        out[6] = a.rc.dv * (df_to_double(m[6]) + 2.0 * df_to_double(m[7])) + a.rc.f0m[6];
-        out[7] = a.rc.dv * df_to_double(m[8]);
-      }
+      // raw sums; the storage kernels form dv * sum + trapz(f0 ...) in FP64.
+      // Each array is indexed by constants only, so it stays in registers.
+      auto put = [&](const df32 (&m)[9], int row) {
+        df32* out = reinterpret_cast<df32*>(a.mom + (size_t)row * MOM_STRIDE);
+#pragma unroll
+        for (int p = 0; p < 6; ++p) out[p] = m[p];
+        out[6] = df_add(m[6], {2.f * m[7].hi, 2.f * m[7].lo});  // sum w (g^2 + 2 g f0)
+        out[7] = m[8];
+      };
+      if (va) put(mv, ra);
+      if (vb) put(mw, rb);
     }
     // x-Fourier modes of f (the f0 part of mode 0 is added in the reduction);
     // the groups of a CTA hold different rows but add into the same bins,

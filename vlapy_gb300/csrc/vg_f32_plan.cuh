@@ -17,6 +17,10 @@ struct RowConsts {
   double dv, dv_sq, dkv;
   double f0m[7];    // trapz(f0 v^p), p = 0..5, and trapz(f0^2)
   float i2dv;       // 1 / (2 dv)
+  // the same in double-float, for the per-row collision scalars (the FP64
+  // pipe of this part is 1/64 of FP32, so a row's scalars stay off it)
+  float2 dv2f, idv2f;  // dv and 1 / dv^2 split (hi, lo)
+  float2 f0m2f[3];     // f0m[0..2] split
 };
 
 struct RowArgs {
@@ -26,15 +30,17 @@ struct RowArgs {
   double dt1, dt2;   // leading / trailing half-kick steps (0: skip)
   float hk1, hk2;    // -dkv dt / 2 of each kick: half angle per kv index and unit field
   int fp, dougherty;
-  double nudt;
+  float2 nudt2;   // nu dt split (hi, lo)
   float nudt_f;
   int want_mom;     // storage moments + x modes of the post-collision state
-  double* mom;      // [nx][8]
+  double* mom;      // [nx][8] slots, each the raw double-float sum (df32) of one moment
   int n_modes;
   cx<float>* mpart; // [grid][n_modes][nv] per-CTA partial x modes
   const cx<float>* F0;  // [nv/2+1] unnormalised FFT_v(f0)
   const cx<float>* tw;
-  RowConsts rc;
+  // the row constants in device memory: a kernel that built a RowConsts
+  // copy of its own would keep it on the stack (~150 B of local memory)
+  const RowConsts* rc;
 };
 
 struct F32Plan {
@@ -46,6 +52,7 @@ struct F32Plan {
   float* Mv;
   float* D;
   RowConsts rc;
+  RowConsts* rc_dev;   // device copy of rc (for RowArgs)
   float2* vhl;         // [nv] v as FP32 (hi, lo)
   float* e32;          // [nx] FP32 copy of the field
   float2* dpart;       // [max col grid][nx] density partials (hi, lo)

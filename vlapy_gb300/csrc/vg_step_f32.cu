@@ -135,14 +135,16 @@ __global__ void __launch_bounds__(row32_block(N, R)) k_row_f32(RowArgs a) {
 // storage of one step: fields, series and stored modes
 // ---------------------------------------------------------------------------
 
-__global__ void k_store_fields_f32(const double* __restrict__ mom, const double* __restrict__ e,
+__global__ void k_store_fields_f32(const double* __restrict__ mom, RowConsts rc, const double* __restrict__ e,
                                    const double* __restrict__ de, int nx, int i, vg_history h) {
   __shared__ df32 red[32 * 7];
   const size_t off = (size_t)i * nx;
   df32 acc[7];
   for (int q = 0; q < 7; ++q) acc[q] = {0.f, 0.f};
   for (int n = threadIdx.x; n < nx; n += blockDim.x) {
-    const double* m = mom + (size_t)n * MOM_STRIDE;
+    const double* slots = mom + (size_t)n * MOM_STRIDE;
+    double m[8];
+    for (int q = 0; q < 8; ++q) m[q] = row_moment(slots, q, rc);
     if (h.fields[0]) h.fields[0][off + n] = e[n];
     if (h.fields[1]) h.fields[1][off + n] = de ? de[n] : 0.0;
     for (int q = 0; q < 6; ++q)
@@ -331,7 +333,7 @@ cudaError_t launch_row_f32(const vg_plan& p, float* g, const double* e, double d
   a.hk2 = (float)(-0.5 * p.f32->dkv * dt2);
   a.fp = fp && p.collision != VG_COLL_NONE;
   a.dougherty = p.collision == VG_COLL_DG;
-  a.nudt = p.nudt;
+  a.nudt2 = split_f2(p.nudt);
   a.nudt_f = (float)p.nudt;
   a.want_mom = mom;
   a.mom = p.mom;
@@ -339,7 +341,7 @@ cudaError_t launch_row_f32(const vg_plan& p, float* g, const double* e, double d
   a.mpart = p.f32->mpart;
   a.F0 = p.f32->F0;
   a.tw = p.tw32;
-  a.rc = p.f32->rc;
+  a.rc = p.f32->rc_dev;
   switch (ilog2(p.nv)) {
 #define CASE(L) case L: return row_n<(1 << L)>(p, a, s);
     VG_F32_POW2_CASES(CASE)
@@ -350,7 +352,7 @@ cudaError_t launch_row_f32(const vg_plan& p, float* g, const double* e, double d
 
 cudaError_t launch_store_f32(const vg_plan& p, const float* g, const double* e, const double* de,
                              const vg_history& h, int i, int n_modes, cudaStream_t s) {
-  k_store_fields_f32<<<1, 256, 0, s>>>(p.mom, e, de, p.nx, i, h);
+  k_store_fields_f32<<<1, 256, 0, s>>>(p.mom, p.f32->rc, e, de, p.nx, i, h);
   cudaError_t err = cudaGetLastError();
   if (err != cudaSuccess) return err;
   if (h.stored_f && h.store_all) {

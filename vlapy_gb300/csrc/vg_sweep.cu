@@ -29,6 +29,7 @@ struct SweepRunDev {
   int x_off;           // x points before this run
   long long dp_off;    // density-partial elements (float2) before this run
   double k, nudt;
+  float2 nudt2;  // nudt split (hi, lo)
   float2 kdt;          // -k dt split into FP32 (hi, lo): the x-drift angle per unit m and v
   float nudt_f;
 };
@@ -163,7 +164,7 @@ __global__ void __launch_bounds__(SWEEP_BLOCK, 3) k_sweep_row(const SweepRunDev*
   a.hk2 = sa.hk2[r.cls];
   a.fp = sa.fp && r.fp;
   a.dougherty = sa.dougherty;
-  a.nudt = r.nudt;
+  a.nudt2 = r.nudt2;
   a.nudt_f = r.nudt_f;
   a.want_mom = sa.want_mom;
   a.mom = sa.mom + (size_t)r.x_off * MOM_STRIDE;
@@ -171,12 +172,13 @@ __global__ void __launch_bounds__(SWEEP_BLOCK, 3) k_sweep_row(const SweepRunDev*
   a.mpart = nullptr;
   a.F0 = scp->F0[r.cls];
   a.tw = sa.tw;
-  a.rc = scp->rc[r.cls];
+  a.rc = &scp->rc[r.cls];
   row_pair<N, R>(a, it.y * P + grp, smem_raw + (size_t)grp * row32_group_bytes(N, R), nullptr, P, grp, t);
 }
 
 // e history row and the seven series of every run (one CTA per run)
 __global__ void __launch_bounds__(128) k_sweep_store(const SweepRunDev* __restrict__ runs, int n_runs,
+                                                     const SweepConsts* __restrict__ scp,
                                                      const double* __restrict__ mom, const double* __restrict__ e,
                                                      double* __restrict__ e_row, double* __restrict__ s_row) {
   __shared__ df32 red[4 * 7];
@@ -186,8 +188,10 @@ __global__ void __launch_bounds__(128) k_sweep_store(const SweepRunDev* __restri
   for (int x = threadIdx.x; x < r.nx; x += blockDim.x) {
     const double ex = e[r.x_off + x];
     if (e_row) e_row[r.x_off + x] = ex;
-    const double* m = mom + (size_t)(r.x_off + x) * MOM_STRIDE;
-    const double src[7] = {m[0], m[1], m[2], ex * ex, 0.0, m[6], m[7]};
+    const double* slots = mom + (size_t)(r.x_off + x) * MOM_STRIDE;
+    const RowConsts& rc = scp->rc[r.cls];
+    const double src[7] = {row_moment(slots, 0, rc), row_moment(slots, 1, rc), row_moment(slots, 2, rc), ex * ex,
+                           0.0, row_moment(slots, 6, rc), row_moment(slots, 7, rc)};
     for (int q = 0; q < 7; ++q) {
       const float hi = (float)src[q];
       acc[q] = df_add(acc[q], {hi, (float)(src[q] - (double)hi)});
@@ -199,7 +203,8 @@ __global__ void __launch_bounds__(128) k_sweep_store(const SweepRunDev* __restri
 
 // initial state g = A cos(k x_j) M(v) (the x-mean of f = M (1 + A cos k x) is M)
 __global__ void k_sweep_init(const SweepRunDev* __restrict__ runs, const double* __restrict__ amp,
-                             const SweepConsts* __restrict__ scp, float* __restrict__ g, double* __restrict__ e) {
+                             const SweepConsts* __restrict__ scp, float* __restrict__ g, double* __restrict__ e,
+                             float* __restrict__ e32) {
   const SweepRunDev r = runs[blockIdx.x];
   const double A = amp[blockIdx.x];
   const float* f0 = scp->rc[r.cls].f0;
@@ -210,7 +215,15 @@ __global__ void k_sweep_init(const SweepRunDev* __restrict__ runs, const double*
     const double c = cospi((2.0 * x + 1.0) / (double)r.nx);
     g[r.g_off + q] = (float)(A * c * (double)f0[vj]);
   }
-  for (int x = threadIdx.x; x < r.nx; x += blockDim.x) e[r.x_off + x] = 0.0;
+  // the first half-kick of a batch reads the FP32 copy of the field
+  for (int x = threadIdx.x; x < r.nx; x += blockDim.x) {
+    e[r.x_off + x] = 0.0;
+    e32[r.x_off + x] = 0.f;
+  }
+}
+
+__global__ void k_sweep_e_to_f32(const double* __restrict__ e, int n, float* __restrict__ e32) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) e32[i] = (float)e[i];
 }
 
 __global__ void k_sweep_read(const SweepRunDev* __restrict__ runs, int run, const SweepConsts* __restrict__ scp,
@@ -381,6 +394,9 @@ int sweep_class(vg_sweep* s, int cls, int nv) {
   rc.dv_sq = dv2;
   rc.dkv = 2.0 * M_PI / (nv * dv);
   for (int k = 0; k < 7; ++k) rc.f0m[k] = mom[k];
+  rc.dv2f = split_f2(dv);
+  rc.idv2f = split_f2(1.0 / dv2);
+  for (int k = 0; k < 3; ++k) rc.f0m2f[k] = split_f2(mom[k]);
   s->consts_h.F0[cls] = dF0;
   s->consts_h.v64[cls] = dv64;
   s->consts_h.c0[cls] = mom[0] - 1.0;
@@ -489,7 +505,7 @@ int sweep_sequence(vg_sweep* s, int nsteps, double* e_hist, double* s_hist, int 
       double* er = e_hist ? e_hist + (size_t)r * s->x_points : nullptr;
       double* sr = s_hist ? s_hist + (size_t)r * s->n_runs * 7 : nullptr;
       SW_CHECK(cuda_status(prof_call(&s->prof, SK_STORE, st, [&] {
-                             k_sweep_store<<<s->n_runs, 128, 0, st>>>(s->runs, s->n_runs, s->mom, s->e, er, sr);
+                             k_sweep_store<<<s->n_runs, 128, 0, st>>>(s->runs, s->n_runs, s->consts, s->mom, s->e, er, sr);
                              return cudaGetLastError();
                            }),
                            "sweep store"));
@@ -554,6 +570,7 @@ int vg_sweep_create(const vg_sweep_desc* d, vg_sweep** out) {
     r.nudt = q.nu * d->dt;
     r.kdt = split_f2(-q.k * d->dt);
     r.nudt_f = (float)r.nudt;
+    r.nudt2 = split_f2(r.nudt);
     cells += (long long)q.nx * q.nv;
     xoff += q.nx;
     dp += (long long)r.ntiles * q.nx;
@@ -674,7 +691,7 @@ int vg_sweep_reset(vg_sweep* s, vg_stream stream) {
     return VG_ERR_ARG;
   }
   cudaStream_t st = (cudaStream_t)stream;
-  k_sweep_init<<<s->n_runs, 256, 0, st>>>(s->runs, s->amp, s->consts, s->g, s->e);
+  k_sweep_init<<<s->n_runs, 256, 0, st>>>(s->runs, s->amp, s->consts, s->g, s->e, s->e32);
   return cuda_status(cudaGetLastError(), "sweep reset");
 }
 
@@ -721,6 +738,51 @@ int vg_sweep_read_run(vg_sweep* s, int32_t run, double* f_out, double* e_out, vg
   const SweepRunDev& r = s->runs_h[run];
   k_sweep_read<<<64, 256, 0, st>>>(s->runs, run, s->consts, s->g, s->f0d[r.cls], s->e, f_out, e_out);
   return cuda_status(cudaGetLastError(), "sweep read");
+}
+
+int vg_sweep_get_state(vg_sweep* s, float* g_out, double* e_out, vg_stream stream) {
+  if (!s) {
+    set_error("null sweep");
+    return VG_ERR_ARG;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  if (g_out)
+    SW_CHECK(cuda_status(cudaMemcpyAsync(g_out, s->g, (size_t)s->cells * sizeof(float), cudaMemcpyDeviceToDevice, st),
+                         "sweep get state"));
+  if (e_out)
+    SW_CHECK(cuda_status(cudaMemcpyAsync(e_out, s->e, (size_t)s->x_points * sizeof(double),
+                                         cudaMemcpyDeviceToDevice, st),
+                         "sweep get state"));
+  return VG_OK;
+}
+
+int vg_sweep_set_state(vg_sweep* s, const float* g_in, const double* e_in, vg_stream stream) {
+  if (!s) {
+    set_error("null sweep");
+    return VG_ERR_ARG;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  if (g_in)
+    SW_CHECK(cuda_status(cudaMemcpyAsync(s->g, g_in, (size_t)s->cells * sizeof(float), cudaMemcpyDeviceToDevice, st),
+                         "sweep set state"));
+  if (e_in) {
+    SW_CHECK(cuda_status(cudaMemcpyAsync(s->e, e_in, (size_t)s->x_points * sizeof(double),
+                                         cudaMemcpyDeviceToDevice, st),
+                         "sweep set state"));
+    k_sweep_e_to_f32<<<div_up((int)s->x_points, 256), 256, 0, st>>>(s->e, (int)s->x_points, s->e32);
+    SW_CHECK(cuda_status(cudaGetLastError(), "sweep set state"));
+  }
+  return VG_OK;
+}
+
+int vg_sweep_state_ptr(vg_sweep* s, float** g, double** e) {
+  if (!s) {
+    set_error("null sweep");
+    return VG_ERR_ARG;
+  }
+  if (g) *g = s->g;
+  if (e) *e = s->e;
+  return VG_OK;
 }
 
 int vg_sweep_profile_enable(vg_sweep* s, int32_t enable) {

@@ -39,6 +39,16 @@ def sweep_config(n_runs=4096, seed=20261203, nx_choices=(32, 64, 128), nv_choice
             for a, b, c, d, e in zip(nx, nv, k, amp, nu)]
 
 
+class _DeviceArray:
+    """__cuda_array_interface__ of a device buffer owned by the library; it
+    holds its owner, and a tensor made from it holds this object."""
+
+    def __init__(self, owner, ptr_value, shape, typestr):
+        self.owner = owner
+        self.__cuda_array_interface__ = {"shape": tuple(shape), "typestr": typestr, "data": (int(ptr_value), False),
+                                         "version": 2, "strides": None}
+
+
 class Sweep:
     """Owns a vg_sweep; runs are advanced together on the current stream."""
 
@@ -104,6 +114,45 @@ class Sweep:
         e = torch.empty(r["nx"], dtype=torch.float64, device="cuda")
         check(self._lib.vg_sweep_read_run(self._h, int(i), ptr(f), ptr(e), stream_handle(stream)), "sweep read")
         return f, e
+
+    @property
+    def g_offsets(self):
+        """Start of each run's [nx][nv] block in the packed state (runs back to back)."""
+        sizes = np.array([r["nx"] * r["nv"] for r in self.runs], dtype=np.int64)
+        return np.concatenate([[0], np.cumsum(sizes)[:-1]])
+
+    def _state_buffer(self, t, n, dtype, what):
+        if t is None:
+            return None
+        if not (isinstance(t, torch.Tensor) and t.is_cuda and t.dtype == dtype and t.is_contiguous()
+                and t.numel() == n):
+            raise ValueError(f"{what} must be a contiguous CUDA {dtype} tensor of {n} elements")
+        return t
+
+    def get_state(self, g_out=None, e_out=None, stream=None):
+        """Packed FP32 deviations g [cells] and fields e [x_points] of all runs."""
+        if g_out is None:
+            g_out = torch.empty(self.cells, dtype=torch.float32, device="cuda")
+        if e_out is None:
+            e_out = torch.empty(self.x_points, dtype=torch.float64, device="cuda")
+        self._state_buffer(g_out, self.cells, torch.float32, "g_out")
+        self._state_buffer(e_out, self.x_points, torch.float64, "e_out")
+        check(self._lib.vg_sweep_get_state(self._h, ptr(g_out), ptr(e_out), stream_handle(stream)), "sweep get")
+        return g_out, e_out
+
+    def set_state(self, g_in=None, e_in=None, stream=None):
+        """Overwrite g and/or e of all runs (layouts as get_state)."""
+        g_in = self._state_buffer(g_in, self.cells, torch.float32, "g_in")
+        e_in = self._state_buffer(e_in, self.x_points, torch.float64, "e_in")
+        check(self._lib.vg_sweep_set_state(self._h, ptr(g_in), ptr(e_in), stream_handle(stream)), "sweep set")
+
+    def state_view(self):
+        """The sweep's own FP32 state g [cells] as a CUDA tensor (no copy; the
+        tensor keeps the sweep alive; g may be modified between run_steps
+        calls on the same stream)."""
+        gp = C.c_void_p()
+        check(self._lib.vg_sweep_state_ptr(self._h, C.byref(gp), None), "sweep state")
+        return torch.as_tensor(_DeviceArray(self, gp.value, (self.cells,), "<f4"), device="cuda")
 
     def e_of(self, e_hist, i):
         """e history [rows][nx] of run i from a sweep e-history buffer."""

@@ -41,6 +41,8 @@ WORKLOADS = {
     "large": dict(nx=4096, nv=8192, k=0.3, vmax=8.0, dt=0.05, nu=1e-4, op="dg", kind="two-stream"),
     "driven": dict(nx=64, nv=1024, k=0.3, vmax=6.4, dt=0.1, nu=1e-3, op="dg", kind="driven"),
     "landau": dict(nx=32, nv=512, k=0.3, vmax=6.4, dt=0.1, nu=0.0, op="dg", kind="landau"),
+    # the learned path's network alone: one correction of 2048 coarse runs x 64 x rows
+    "corrector": dict(kind="corrector", n_runs=2048, nx=64, vmax=6.4),
 }
 
 
@@ -414,7 +416,7 @@ def learned_path(args, w):
             # tensor roofline of the network alone: forward FLOPs of one apply over its time
             g = sw.state_view().view(-1, cm.NV)
             rows = g.shape[0]
-            flops = 2.0 * rows * cm.NV * 5 * (16 * 64 + 64 * 64 + 64 * 64 + 64 * 8)
+            flops = 2.0 * rows * cm.NV * 5 * (16 * 64 + 64 * 64 + 64 * 64 + 64 * 16)
             prev = g.clone()
             e0.record()
             for _ in range(K):
@@ -428,8 +430,8 @@ def learned_path(args, w):
             out[name]["tensor_roofline"] = {"bound": "tensor", "achieved": flops / (ams / 1e3) / 1e12, "peak": pk,
                                             "unit": "TFLOP/s", "frac": flops / (ams / 1e3) / 1e12 / pk,
                                             "flops_per_apply": flops,
-                                            "note": "mma.sync m16n8k16 BF16 (FP32 accumulate); padded channels "
-                                                    "counted as issued"}
+                                            "note": "fused tcgen05 forward (BF16, FP32 accumulate in TMEM) + "
+                                                    "projection; padded channels counted as issued"}
             big.close()
         sw.close()
     # plain FP64 GPU step of one 64x1024 run of the distribution
@@ -461,6 +463,81 @@ def learned_path(args, w):
         "throughput_2048_runs": out,
         "judge": "fine runs of the FP32 batched sweep (the GPU tests hold it to the FP64 oracle)",
     }
+
+
+def main_corrector(args, w, rank, world):
+    """Time one correction (vg_corr_apply) of every row of 2048 coarse runs
+    (nx = 64, nv = 128): seeded synthetic rows and seeded network weights,
+    on the fused tcgen05 kernel (the default engine)."""
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps({"impl": "reference", "unavailable": "the corrector has no reference counterpart"}))
+        return
+    import torch
+    from vlapy_gb300 import corrector as cm
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", rank)) % max(1, torch.cuda.device_count()))
+    nx, runs = w["nx"], w["n_runs"]
+    rows = runs * nx
+    rng = np.random.default_rng(11)
+    p = cm.init_params(3)
+    p[-(5 * 64 + 1):-1] = rng.uniform(-0.1, 0.1, 5 * 64).astype(np.float32)  # a live last layer
+    v = -w["vmax"] + 2 * w["vmax"] / cm.NV * (np.arange(cm.NV) + 0.5)
+    base = np.exp(-v ** 2 / 2)[None, :]
+    g = torch.as_tensor((1e-3 * base * rng.standard_normal((rows, cm.NV))).astype(np.float32), device="cuda")
+    prev = (g * 0.99).contiguous()
+    feat = torch.full((rows,), 0.5, dtype=torch.float32, device="cuda")
+    corr = cm.Corrector(rows, params=p, tau=0.02)
+    out = torch.empty_like(g)
+    K, W = args.steps, args.warmup
+    for _ in range(W):
+        corr.apply(g, prev, feat, out=out, group_rows=nx)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(K):
+        corr.apply(g, prev, feat, out=out, group_rows=nx)
+    e1.record()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    corr.check_status()
+    ms = e0.elapsed_time(e1) / K
+    # end to end: host rows in pinned memory, copied in and the corrected rows copied back
+    hg = g.cpu().pin_memory()
+    hp = prev.cpu().pin_memory()
+    ho = torch.empty_like(hg).pin_memory()
+    dg, dp = torch.empty_like(g), torch.empty_like(prev)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(K):
+        dg.copy_(hg, non_blocking=True)
+        dp.copy_(hp, non_blocking=True)
+        corr.apply(dg, dp, feat, out=out, group_rows=nx)
+        ho.copy_(out, non_blocking=True)
+        torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / K
+    flops = 2.0 * rows * cm.NV * 5 * (16 * 64 + 64 * 64 + 64 * 64 + 64 * 16)
+    pk = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["bf16_tflops"] if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else 1900.0
+    if rank != 0:
+        return
+    tf = flops / (ms / 1e3) / 1e12
+    line = {"metric": "corrected rows/s", "value": rows / (ms / 1e3), "unit": "rows/s", "n_gpus": 1, "steps": K,
+            "warmup": W, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "bf16", "data": "synthetic",
+            "config": {"workload": "corrector", "rows": rows, "nv": cm.NV, "layers": "4 x conv1d k=5, 64 ch",
+                       "engine": "tcgen05 fused forward + projected, capped correction",
+                       "l2": "rows %.0f MB in, %.0f MB out: larger than L2 (129 MB)" % (rows * 512 * 2 / 1e6,
+                                                                                      rows * 512 / 1e6)},
+            "roofline": {"bound": "tensor", "achieved": tf, "peak": pk, "unit": "TFLOP/s", "frac": tf / pk,
+                         "traffic": None, "peak_source": "measured" if pk != 1900.0 else "fallback",
+                         "flops_per_launch": flops,
+                         "note": "issued MMA FLOPs (layer 1 K padded 4 -> 16 channels, layer 4 N padded 1 -> 16)"},
+            "e2e": {"value": rows / e2e_s, "unit": "rows/s", "h2d_bytes_per_step": 2 * rows * cm.NV * 4,
+                    "d2h_bytes_per_step": rows * cm.NV * 4},
+            "gpu_launches": 4 * K, "clocks": clk, "cpu_baseline": None}
+    print(json.dumps(line))
 
 
 def _oracle_sweep_sample(args):
@@ -559,6 +636,8 @@ def main():
         w["n_runs"] = args.runs
     if w["kind"] == "sweep":
         return main_sweep(args, w, rank, world)
+    if w["kind"] == "corrector":
+        return main_corrector(args, w, rank, world)
     cells = w["nx"] * w["nv"]
     metric = "cell-updates/s"
     cfg = {"workload": args.workload, "nx": w["nx"], "nv": w["nv"], "dt": w["dt"], "nu": w["nu"],

@@ -61,9 +61,10 @@ def rel(a, b):
     return np.linalg.norm(np.asarray(a, np.float64) - b) / np.linalg.norm(b)
 
 
+@pytest.mark.parametrize("engine", ["tcgen05", "mma.sync"])
 @pytest.mark.parametrize("rows,group,modes", [(1, 0, 0), (77, 0, 0), (1000, 0, 32), (960, 64, 32), (64, 64, 0),
                                               (90, 3, 64), (128, 64, 1)])
-def test_forward_matches_oracle(rows, group, modes):
+def test_forward_matches_oracle(rows, group, modes, engine):
     from vlapy_gb300.corrector import Corrector
     p = random_params(1)
     g, _, feat, prev = random_rows(rows, rows, with_prev=True)
@@ -71,14 +72,18 @@ def test_forward_matches_oracle(rows, group, modes):
         prev = None  # the previous-state channel left empty
     tau = 0.05
     corr = Corrector(1024, params=p, tau=tau, protect_modes=modes)
+    corr.set_engine(engine)
     gt, ft = torch.as_tensor(g, device="cuda"), torch.as_tensor(feat, device="cuda")
     pt = None if prev is None else torch.as_tensor(prev, device="cuda")
     out = corr.apply(gt, prev=pt, feat=ft, group_rows=group).cpu().numpy().astype(np.float64)
     ref_e = co.apply(p, g, feat, 6.4, tau, emulate=True, group_rows=group, protect_modes=modes, prev=prev)
     ref_x = co.apply(p, g, feat, 6.4, tau, emulate=False, group_rows=group, protect_modes=modes, prev=prev)
-    # compare the corrections themselves (out - g), not the rows
-    assert rel(out - g, ref_e - g) <= 2e-3
-    assert rel(out - g, ref_x - g) <= 0.1
+    # compare the corrections themselves (out - g), not the rows; the output
+    # rows are FP32, so a correction near the rounding of g is resolved only
+    # to ~1e-7 |g| (the 1e-6 floor below)
+    gn = np.linalg.norm(g.astype(np.float64))
+    assert np.linalg.norm((out - g) - (ref_e - g)) <= 2e-3 * np.linalg.norm(ref_e - g) + 1e-6 * gn
+    assert np.linalg.norm((out - g) - (ref_x - g)) <= 0.1 * np.linalg.norm(ref_x - g) + 1e-6 * gn
     # the cap: no corrected row deviation is longer than the uncorrected one
     d = co.deviation(g, group).numpy().astype(np.float64)
     dn = d + (out - g)
@@ -91,6 +96,25 @@ def test_forward_matches_oracle(rows, group, modes):
     # in place: g_out aliasing g
     corr.apply(gt, prev=pt, feat=ft, out=gt, group_rows=group)
     np.testing.assert_array_equal(gt.cpu().numpy(), out.astype(np.float32))
+    corr.check_status()
+
+
+def test_engines_agree_on_many_rows():
+    """The fused tcgen05 forward and the per-layer mma.sync kernels see the
+    same BF16 operands; only FP32 accumulation order and rare BF16 rounding
+    flips of the activations separate them."""
+    from vlapy_gb300.corrector import Corrector
+    p = random_params(5)
+    rows = 64 * 300  # more rows than SMs: every persistent CTA loops
+    g, _, feat, prev = random_rows(rows, 9, with_prev=True)
+    gt, ft, pt = (torch.as_tensor(a, device="cuda") for a in (g, feat, prev))
+    corr = Corrector(rows, params=p, tau=0.05)
+    a = corr.apply(gt, prev=pt, feat=ft, group_rows=64)
+    corr.set_engine("mma.sync")
+    b = corr.apply(gt, prev=pt, feat=ft, group_rows=64)
+    corr.check_status()
+    da, db = (a - gt).double(), (b - gt).double()
+    assert float(torch.linalg.norm(da - db) / torch.linalg.norm(db)) <= 1e-3
 
 
 @pytest.mark.parametrize("group,modes", [(0, 0), (60, 32), (60, 0)])

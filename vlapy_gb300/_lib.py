@@ -114,6 +114,8 @@ EXPORTS = {
     "vg_corr_get_params": (C.c_int, [C.c_void_p, C.c_void_p]),
     "vg_corr_set_params": (C.c_int, [C.c_void_p, C.c_void_p]),
     "vg_corr_apply": (C.c_int, [C.c_void_p, C.POINTER(VgCorrBatch), C.c_void_p, C.c_void_p]),
+    "vg_corr_set_engine": (C.c_int, [C.c_void_p, C.c_int32]),
+    "vg_corr_status": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "vg_corr_loss": (C.c_int, [C.c_void_p, C.POINTER(VgCorrBatch), C.POINTER(C.c_double), C.c_void_p]),
     "vg_corr_gradients": (C.c_int, [C.c_void_p, C.POINTER(VgCorrBatch), C.c_void_p, C.POINTER(C.c_double),
                                     C.c_void_p]),

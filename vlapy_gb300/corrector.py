@@ -146,6 +146,17 @@ class Corrector:
         check(self._lib.vg_corr_set_tau(self._h, float(value)), "corrector tau")
         self._tau = float(value)
 
+    def set_engine(self, engine):
+        """"tcgen05" (default): the fused forward on the 5th-generation tensor
+        cores; "mma.sync": the per-layer kernels the training path uses."""
+        code = {"tcgen05": 0, "mma.sync": 1}[engine]
+        check(self._lib.vg_corr_set_engine(self._h, code), "corrector engine")
+
+    def check_status(self):
+        """Raise if a bounded wait of the fused kernel ran out (synchronises)."""
+        flags = C.c_int32()
+        check(self._lib.vg_corr_status(self._h, C.byref(flags)), "corrector status")
+
     @property
     def params(self):
         out = np.empty(self.n_params, dtype=np.float32)
@@ -362,4 +373,5 @@ def run_corrected(sweep, corr, nsteps, e_hist=None, series_hist=None, row0=0, st
         prev.copy_(g)
         sweep.run_steps(1, e_hist, series_hist, row0=row0 + i, stream=stream)
         corr.apply(g, prev, feat, out=g, group_rows=nx, stream=stream)
+    corr.check_status()
     return sweep

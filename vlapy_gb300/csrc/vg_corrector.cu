@@ -312,9 +312,16 @@ __global__ void k_wgrad_reduce(const float* __restrict__ part, const float* __re
 __global__ void k_group_mean(const float* __restrict__ g, int group_rows, double* __restrict__ out) {
   const int grp = blockIdx.x, p = threadIdx.x;  // blockDim = CP
   const float* src = g + (size_t)grp * group_rows * CP + p;
-  double acc = 0.0;
-  for (int r = 0; r < group_rows; ++r) acc += (double)src[(size_t)r * CP];
-  out[(size_t)grp * CP + p] = acc / (double)group_rows;
+  // double-float (TwoSum) accumulation: FP64-grade, on the FP32 pipes
+  float hi = 0.f, lo = 0.f;
+  for (int r = 0; r < group_rows; ++r) {
+    const float x = src[(size_t)r * CP];
+    const float t = hi + x;
+    const float bb = t - hi;
+    lo += (hi - (t - bb)) + (x - bb);
+    hi = t;
+  }
+  out[(size_t)grp * CP + p] = ((double)hi + (double)lo) / (double)group_rows;
 }
 
 // deviation of g[q] (row `row`, position p) from its group mean, rounded once
@@ -379,6 +386,45 @@ __device__ __forceinline__ float high_pass(float v, const float* __restrict__ ba
   return r;
 }
 
+// high_pass for two rows' values at once (one pass over the basis)
+__device__ __forceinline__ void high_pass2(float a, float b, const float* __restrict__ basis,
+                                           const float* __restrict__ basis_t, int nq, float* sh, float* coef,
+                                           float& ha, float& hb) {
+  const int p = threadIdx.x;
+  if (nq == 0) {
+    ha = a;
+    hb = b;
+    return;
+  }
+  sh[p] = a;
+  sh[CP + p] = b;
+  __syncthreads();
+  if (p < nq) {
+    float ca0 = 0.f, ca1 = 0.f, cb0 = 0.f, cb1 = 0.f;
+#pragma unroll 8
+    for (int j = 0; j < CP; j += 2) {
+      const float w0 = basis_t[j * CP + p], w1 = basis_t[(j + 1) * CP + p];
+      ca0 = fmaf(sh[j], w0, ca0);
+      cb0 = fmaf(sh[CP + j], w0, cb0);
+      ca1 = fmaf(sh[j + 1], w1, ca1);
+      cb1 = fmaf(sh[CP + j + 1], w1, cb1);
+    }
+    coef[p] = ca0 + ca1;
+    coef[CP + p] = cb0 + cb1;
+  }
+  __syncthreads();
+  float ra = a, rb = b;
+#pragma unroll 4
+  for (int q = 0; q < nq; ++q) {
+    const float w = basis[q * CP + p];
+    ra = fmaf(-coef[q], w, ra);
+    rb = fmaf(-coef[CP + q], w, rb);
+  }
+  __syncthreads();
+  ha = ra;
+  hb = rb;
+}
+
 // loss = mean((P (pred - want))^2) over rows x positions, P the projection
 // onto the corrected modes (|m| >= M) and want = ((target - tmean) - (g -
 // gmean)) / (s tau) the correction in units of the row RMS s times a global
@@ -424,24 +470,29 @@ __global__ void k_apply(const float* __restrict__ g, const double* __restrict__ 
                         const float* __restrict__ pred, const float* __restrict__ scale, float tau,
                         const float* __restrict__ basis, const float* __restrict__ basis_t, int nq,
                         float* __restrict__ out) {
-  __shared__ float r_old[CP], r_new[CP];
+  __shared__ float sh[2 * CP], coef[2 * CP];
+  __shared__ float wsum[2][CP / 32];
   const int row = blockIdx.x, p = threadIdx.x;
   const size_t q = (size_t)row * CP + p;
   const float d = deviation(g[q], gmean, group_rows, row, p);
-  const float dh = high_pass(d, basis, basis_t, nq, r_old, r_new);
-  const float c = high_pass((scale[row] * tau) * pred[q], basis, basis_t, nq, r_old, r_new);
+  float dh, c;
+  high_pass2(d, (scale[row] * tau) * pred[q], basis, basis_t, nq, sh, coef, dh, c);
   const float hn = dh + c;
-  r_old[p] = dh * dh;
-  r_new[p] = hn * hn;
-  __syncthreads();
-  for (int k = CP / 2; k > 0; k >>= 1) {
-    if (p < k) {
-      r_old[p] += r_old[p + k];
-      r_new[p] += r_new[p + k];
-    }
-    __syncthreads();
+  // row sums of dh^2 and hn^2: warp shuffles, then the four warps
+  float so = dh * dh, sn = hn * hn;
+#pragma unroll
+  for (int m = 16; m > 0; m >>= 1) {
+    so += __shfl_xor_sync(0xffffffffu, so, m);
+    sn += __shfl_xor_sync(0xffffffffu, sn, m);
   }
-  const float factor = r_new[0] > r_old[0] ? sqrtf(r_old[0] / r_new[0]) : 1.f;
+  if ((p & 31) == 0) {
+    wsum[0][p >> 5] = so;
+    wsum[1][p >> 5] = sn;
+  }
+  __syncthreads();
+  const float r_old = (wsum[0][0] + wsum[0][1]) + (wsum[0][2] + wsum[0][3]);
+  const float r_new = (wsum[1][0] + wsum[1][1]) + (wsum[1][2] + wsum[1][3]);
+  const float factor = r_new > r_old ? sqrtf(r_old / r_new) : 1.f;
   const float dn = (d - dh) + hn * factor;
   // g - d is the group mean rounded to FP32 next to g; adding the corrected
   // deviation in FP64 keeps the x-varying part exact to FP32
@@ -475,6 +526,380 @@ __global__ void k_pack(const float* __restrict__ w, int cout, int cin, int frows
   }
 }
 
+
+// ---------------------------------------------------------------------------
+// Fused forward pass on the 5th-generation tensor cores (tcgen05).
+//
+// One persistent CTA per SM (128 threads, 4 warps) keeps all four layers'
+// BF16 weights (100 KB) and two activation tiles in shared memory and runs
+// the network row by row: features -> 4 x (tcgen05.mma into a TMEM
+// accumulator of 128 lanes (positions) x N columns (channels), then an
+// epilogue that reads TMEM back with tcgen05.ld, adds the bias, applies the
+// ReLU and writes the next layer's BF16 tile) -> the network output and the
+// row scale.  No activation touches HBM.  The projected, capped correction
+// runs after it in k_apply, whose many small CTAs hide the latency of its
+// per-row projections (one CTA per SM here could not).
+//
+// Every tile is in the K-major, non-swizzled canonical layout: element
+// (row r, channel c) at (c / 8) * LBO + r * 16 + (c % 8) * 2 bytes, so that an
+// 8 x 16-byte core matrix is 128 contiguous bytes, core matrices along the
+// rows are 128 B apart (SBO) and along K LBO = 16 * rows apart.  A tap t of
+// the convolution is then the activation tile's descriptor moved by 16 t
+// bytes (rows t .. t + 127 of the 132-row tile with its 2-row halos).
+// ---------------------------------------------------------------------------
+
+constexpr int TC_SLOTS = 4;                             // rows in flight per CTA
+constexpr int TC_THREADS = TC_SLOTS * 128;               // 4 warps per slot
+constexpr int TC_TILE_ROWS = CROWS;                      // 132
+constexpr int TC_LBO_ACT = 16 * TC_TILE_ROWS;            // 2112 B
+constexpr int TC_ACT_BYTES = 8 * TC_LBO_ACT;             // 64 channels
+constexpr int TC_W1_TAP = HID * L1_IN * 2, TC_W2_TAP = HID * HID * 2, TC_W4_TAP = 16 * HID * 2;
+constexpr int TC_W_BYTES = 5 * (TC_W1_TAP + 2 * TC_W2_TAP + TC_W4_TAP);  // 102400
+constexpr int TC_OFF_W1 = 0;
+constexpr int TC_OFF_W2 = TC_OFF_W1 + 5 * TC_W1_TAP;
+constexpr int TC_OFF_W3 = TC_OFF_W2 + 5 * TC_W2_TAP;
+constexpr int TC_OFF_W4 = TC_OFF_W3 + 5 * TC_W2_TAP;
+// per slot one tile of 64 channels, updated in place: a layer's epilogue
+// overwrites the layer's own input, which its MMAs have finished reading
+// (their completion is what the epilogue waits for); the 16-channel input
+// of the first layer is the tile's first two channel groups
+constexpr int TC_OFF_SLOT = TC_W_BYTES;
+constexpr int TC_SLOT_BYTES = TC_ACT_BYTES;
+constexpr int TC_OFF_F = TC_OFF_SLOT + TC_SLOTS * TC_SLOT_BYTES;  // floats: bias[256], red[slots][128]
+constexpr int TC_NF = 256 + TC_SLOTS * 128;
+constexpr int TC_OFF_BAR = TC_OFF_F + TC_NF * 4;         // done[slots] mbarriers, TMEM address
+constexpr int TC_SMEM = TC_OFF_BAR + 8 * TC_SLOTS + 16;
+constexpr int TC_TMEM_COLS = 256;                        // 64 per slot, a power of two
+constexpr unsigned long long TC_WAIT_NS = 2000000000ull;  // 2 s: a wait that long has failed
+static_assert(TC_SMEM <= 227 * 1024, "fused corrector tiles exceed shared memory");
+static_assert(TC_SLOTS * 64 <= TC_TMEM_COLS, "TMEM columns");
+static_assert(TC_OFF_SLOT % 16 == 0 && TC_SLOT_BYTES % 16 == 0 && TC_OFF_BAR % 8 == 0,
+              "tile offsets must be 16-byte aligned");
+
+// byte offset of (row, channel) in a canonical K-major tile whose K-adjacent
+// core matrices are lbo bytes apart
+__host__ __device__ constexpr int tc_off(int r, int c, int lbo) { return (c >> 3) * lbo + r * 16 + (c & 7) * 2; }
+
+// shared-memory matrix descriptor: start address, LBO and SBO in 16-byte
+// units, descriptor version 1, no swizzle
+__device__ __forceinline__ uint64_t tc_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((addr >> 4) & 0x3FFF) | ((uint64_t)((lbo >> 4) & 0x3FFF) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) | (1ull << 46);
+}
+// instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both
+// K-major, M x N
+__host__ __device__ constexpr uint32_t tc_idesc(int m, int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, int accumulate) {
+  asm volatile(
+      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+      "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+__device__ __forceinline__ void tc_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(bar)
+               : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
+
+// bounded wait for the phase `parity` of an mbarrier: false once TC_WAIT_NS
+// of the global timer have passed without the phase completing
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;\n" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  const uint64_t t0 = global_ns();
+  for (;;) {
+    uint32_t done;
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if (global_ns() - t0 > TC_WAIT_NS) return false;
+  }
+}
+
+// 16 consecutive TMEM columns of this warp's 32 lanes, as FP32
+__device__ __forceinline__ void tc_ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15}, [%16];\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// the same without the wait: several loads in flight, then one tc_wait_ld()
+__device__ __forceinline__ void tc_ld16_nowait(uint32_t taddr, uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15}, [%16];\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+}
+__device__ __forceinline__ void tc_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory"); }
+
+// issue one layer: 5 taps x (CIN / 16) K-steps of M = 128, N = NOUT, reading
+// the activation tile at act (lbo = TC_LBO_ACT) and the weight taps at w
+template <int CIN, int NOUT>
+__device__ __forceinline__ void tc_layer_issue(uint32_t tmem, uint32_t act, uint32_t w) {
+  constexpr uint32_t idesc = tc_idesc(128, NOUT);
+  constexpr int WTAP = NOUT * CIN * 2;
+  int first = 1;
+#pragma unroll
+  for (int t = 0; t < 5; ++t) {
+#pragma unroll
+    for (int kc = 0; kc < CIN / 16; ++kc) {
+      const uint64_t a = tc_desc(act + 16 * t + 2 * kc * TC_LBO_ACT, TC_LBO_ACT, 128);
+      const uint64_t b = tc_desc(w + t * WTAP + 2 * kc * (16 * NOUT), 16 * NOUT, 128);
+      tc_mma(tmem, a, b, idesc, first ? 0 : 1);
+      first = 0;
+    }
+  }
+}
+
+// epilogue of a hidden layer: TMEM (this thread's position, 64 channels) +
+// bias, ReLU, BF16 into row p + 2 of the next tile; the four 16-column loads
+// are in flight together
+__device__ __forceinline__ void tc_hidden_epilogue(uint32_t tmem, int quarter, int p, const float* bias,
+                                                   unsigned char* out_tile) {
+  const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
+  uint32_t r[4][16];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) tc_ld16_nowait(tmem + lane_base + 16 * q, r[q]);
+  tc_wait_ld();
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      uint32_t w[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int c = 16 * q + 8 * h + 2 * j;
+        const __nv_bfloat162 pr =
+            __floats2bfloat162_rn(fmaxf(__uint_as_float(r[q][8 * h + 2 * j]) + bias[c], 0.f),
+                                  fmaxf(__uint_as_float(r[q][8 * h + 2 * j + 1]) + bias[c + 1], 0.f));
+        w[j] = *reinterpret_cast<const uint32_t*>(&pr);
+      }
+      *reinterpret_cast<uint4*>(out_tile + tc_off(p + CHALO, 16 * q + 8 * h, TC_LBO_ACT)) =
+          make_uint4(w[0], w[1], w[2], w[3]);
+    }
+  }
+}
+
+__device__ __forceinline__ void slot_sync(int slot) {
+  asm volatile("bar.sync %0, 128;\n" ::"r"(1 + slot) : "memory");
+}
+// true on every thread of the slot if v is true on any (a named-barrier vote)
+__device__ __forceinline__ bool slot_any(int slot, bool v) {
+  uint32_t r;
+  asm volatile(
+      "{\n.reg .pred pi, po;\nsetp.ne.u32 pi, %1, 0;\nbar.red.or.pred po, %2, 128, pi;\nselp.u32 %0, 1, 0, po;\n}\n"
+      : "=r"(r)
+      : "r"((uint32_t)v), "r"(1 + slot)
+      : "memory");
+  return r != 0;
+}
+
+// TC_SLOTS slots of 4 warps; each slot carries its own row through the
+// four layers with its own TMEM columns and tile, and one elected thread of
+// the slot issues the slot's MMAs, so that one slot's epilogue overlaps the
+// others' MMAs.  Per slot one mbarrier, done, armed by tcgen05.commit when
+// the layer's MMAs are complete.  Row k of slot s is blockIdx.x + gridDim.x *
+// (k * TC_SLOTS + s).  Every wait is bounded: a wait that gives up sets err,
+// and the slot leaves together after a barrier vote.
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    k_corr_forward_tc(const float* __restrict__ g, const float* __restrict__ gp, const double* __restrict__ gmean,
+                      const double* __restrict__ pmean, int group_rows, const float* __restrict__ row_feat, int rows,
+                      float vmax, const uint4* __restrict__ wtc, const float* __restrict__ params,
+                      float* __restrict__ pred_out, float* __restrict__ scale_out, int* __restrict__ err) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  float* bias = reinterpret_cast<float*>(smem + TC_OFF_F);  // b1, b2, b3 [64] each, b4
+  const uint32_t s_base = (uint32_t)__cvta_generic_to_shared(smem);
+  const uint32_t bar_done = s_base + TC_OFF_BAR;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + TC_OFF_BAR + 8 * TC_SLOTS);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
+                     s_base + TC_OFF_BAR + 8 * TC_SLOTS),
+                 "r"(TC_TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+  }
+  if (threadIdx.x == 0) {
+    for (int q = 0; q < TC_SLOTS; ++q)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar_done + 8 * q) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  for (int i = threadIdx.x; i < TC_W_BYTES / 16; i += TC_THREADS) reinterpret_cast<uint4*>(smem)[i] = wtc[i];
+  for (int i = threadIdx.x; i < 3 * HID; i += TC_THREADS)
+    bias[i] = params[i < HID ? OFF_B1 + i : (i < 2 * HID ? OFF_B2 + i - HID : OFF_B3 + i - 2 * HID)];
+  if (threadIdx.x == 0) bias[3 * HID] = params[OFF_B4];
+  // zero the halo rows (0, 1, 130, 131) of every tile
+  for (int i = threadIdx.x; i < TC_SLOTS * 4 * 8; i += TC_THREADS) {
+    const int grp = i & 7, hr = (i >> 3) & 3, tile = i >> 5;  // tile = slot
+    const int hrow = hr < 2 ? hr : CROWS - 4 + hr;
+    *reinterpret_cast<uint4*>(smem + TC_OFF_SLOT + tile * TC_ACT_BYTES + tc_off(hrow, 8 * grp, TC_LBO_ACT)) =
+        make_uint4(0, 0, 0, 0);
+  }
+  fence_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  const int slot = warp >> 2;
+  const int quarter = warp & 3;          // the TMEM lanes this warp may read
+  const int p = 32 * quarter + lane;     // position = TMEM lane
+  const bool issuer = (p == 0);          // the slot's MMA issuer
+  float* red = bias + 256 + 128 * slot;
+  unsigned char* tile = smem + TC_OFF_SLOT + slot * TC_SLOT_BYTES;
+  const uint32_t tile_s = s_base + TC_OFF_SLOT + slot * TC_SLOT_BYTES;
+  const uint32_t td = tmem + 64 * slot, lane_base = (uint32_t)(quarter * 32) << 16;
+  const uint32_t bar = bar_done + 8 * slot;
+  const float dvv = 2.f * vmax / CP;
+  const float vfeat = __fadd_rn(-vmax, __fmul_rn(dvv, (float)p + 0.5f)) / vmax;
+  uint32_t phase = 0;
+  int commits = 0;
+  bool ok = true;
+  // this thread's inputs of a row, loaded one row ahead so that their
+  // latency hides behind the current row's layers
+  float in_g = 0.f, in_gp = 0.f, in_f = 0.f;
+  double in_m = 0.0, in_pm = 0.0;
+  auto fetch = [&](int r) {
+    const size_t qq = (size_t)r * CP + p;
+    in_g = g[qq];
+    in_gp = gp ? gp[qq] : 0.f;
+    in_f = row_feat ? row_feat[r] : 0.f;
+    if (group_rows > 0) {
+      const size_t mi = (size_t)(r / group_rows) * CP + p;
+      in_m = gmean[mi];
+      in_pm = gp ? pmean[mi] : 0.0;
+    }
+  };
+  // the slot's tile is complete: make it visible to the tensor core, then
+  // its issuer starts layer L
+  auto issue = [&](int L) {
+    fence_async_smem();
+    tc_fence_before();
+    slot_sync(slot);
+    if (issuer) {
+      tc_fence_after();
+      switch (L) {
+        case 0: tc_layer_issue<L1_IN, HID>(td, tile_s, s_base + TC_OFF_W1); break;
+        case 1: tc_layer_issue<HID, HID>(td, tile_s, s_base + TC_OFF_W2); break;
+        case 2: tc_layer_issue<HID, HID>(td, tile_s, s_base + TC_OFF_W3); break;
+        default: tc_layer_issue<HID, 16>(td, tile_s, s_base + TC_OFF_W4); break;
+      }
+      tc_commit(bar);
+    }
+    ++commits;
+  };
+  int row = blockIdx.x + gridDim.x * slot;
+  if (row < rows) fetch(row);
+  while (ok && row < rows) {
+    const size_t q = (size_t)row * CP + p;
+    const float d = group_rows > 0 ? (float)((double)in_g - in_m) : in_g;
+    const float dp = gp ? (group_rows > 0 ? (float)((double)in_gp - in_pm) : in_gp) : 0.f;
+    const float feat = in_f;
+    const int next = row + gridDim.x * TC_SLOTS;
+    if (next < rows) fetch(next);
+    // row RMS: the same pairwise tree as k_features (partners 64, 32, ...,
+    // 1 apart), the last five levels by shuffles within a warp
+    red[p] = d * d;
+    slot_sync(slot);
+    if (p < 64) red[p] += red[p + 64];
+    slot_sync(slot);
+    if (p < 32) {
+      float ss = red[p] + red[p + 32];
+#pragma unroll
+      for (int m = 16; m > 0; m >>= 1) ss += __shfl_down_sync(0xffffffffu, ss, m);
+      if (p == 0) red[CP - 1] = ss;  // red[127] is no longer read
+    }
+    slot_sync(slot);
+    const float s = sqrtf(red[CP - 1] / CP) + 1e-30f;
+    {
+      const __nv_bfloat162 c01 = __floats2bfloat162_rn(d / s, vfeat);
+      const __nv_bfloat162 c23 = __floats2bfloat162_rn(feat, dp / s);
+      *reinterpret_cast<uint4*>(tile + tc_off(p + CHALO, 0, TC_LBO_ACT)) =
+          make_uint4(*reinterpret_cast<const uint32_t*>(&c01), *reinterpret_cast<const uint32_t*>(&c23), 0u, 0u);
+      *reinterpret_cast<uint4*>(tile + tc_off(p + CHALO, 8, TC_LBO_ACT)) = make_uint4(0, 0, 0, 0);
+    }
+    issue(0);
+    float pred = 0.f;
+    for (int L = 0; L < 4; ++L) {
+      const bool done = mbar_wait(bar, phase);
+      phase ^= 1u;
+      if (slot_any(slot, !done)) {  // the slot leaves together, never half of it
+        ok = false;
+        break;
+      }
+      tc_fence_after();
+      if (L < 3) {
+        tc_hidden_epilogue(td, quarter, p, bias + HID * L, tile);
+        issue(L + 1);
+      } else {
+        float v[16];
+        tc_ld16(td + lane_base, v);
+        pred = v[0] + bias[3 * HID];
+      }
+    }
+    if (!ok) break;
+    pred_out[q] = pred;
+    if (p == 0) scale_out[row] = s;
+    row = next;
+  }
+  if (!ok) {
+    if (p == 0) atomicOr(err, 1);
+    // no MMA of this slot may still write TMEM when it is freed
+    if (commits > 0) mbar_wait(bar, (uint32_t)((commits - 1) & 1));
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TC_TMEM_COLS) : "memory");
+  }
+}
+
+// the four layers' BF16 weights in the fused kernel's shared-memory image
+__global__ void k_pack_tc(const float* __restrict__ w, __nv_bfloat16* __restrict__ img) {
+  // layer l: (offset in params, cout real, cin, N padded, byte offset in the image)
+  const int n_total = 5 * (HID * L1_IN + 2 * HID * HID + 16 * HID);
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n_total; q += gridDim.x * blockDim.x) {
+    int r = q, off, cout, cin, np, base;
+    if (r < 5 * HID * L1_IN) {
+      off = OFF_W1; cout = HID; cin = L1_IN; np = HID; base = TC_OFF_W1;
+    } else if ((r -= 5 * HID * L1_IN) < 5 * HID * HID) {
+      off = OFF_W2; cout = HID; cin = HID; np = HID; base = TC_OFF_W2;
+    } else if ((r -= 5 * HID * HID) < 5 * HID * HID) {
+      off = OFF_W3; cout = HID; cin = HID; np = HID; base = TC_OFF_W3;
+    } else {
+      r -= 5 * HID * HID;
+      off = OFF_W4; cout = 1; cin = HID; np = 16; base = TC_OFF_W4;
+    }
+    const int t = r / (np * cin), o = (r / cin) % np, c = r % cin;
+    const float val = o < cout ? w[off + ((size_t)o * cin + c) * 5 + t] : 0.f;
+    const int byte = base + t * np * cin * 2 + tc_off(o, c, 16 * np);
+    img[byte / 2] = __float2bfloat16(val);
+  }
+}
+
 }  // namespace vg
 
 using namespace vg;
@@ -495,6 +920,10 @@ struct vg_corrector {
   float *pred, *scale, *part, *bpart, *loss_part;
   double *gmean, *tmean, *pmean;  // group means [groups][128]
   float vmax, tau;
+  int engine;               // 0: fused tcgen05 forward, 1: per-layer mma.sync kernels
+  int n_sm;
+  __nv_bfloat16* wtc;       // the fused kernel's weight image [TC_W_BYTES / 2]
+  int* err;                 // device error word of the fused kernel
   int protect_modes;      // M: the modes |m| < M are never corrected
   int nq;                 // 2M - 1 basis functions (0 when M = 0)
   float *basis, *basis_t; // [nq][128], [128][128] (transposed, padded)
@@ -561,7 +990,8 @@ int pack_all(vg_corrector* c, cudaStream_t s) {
     k_pack<<<div_up(5 * P * l.cin, 256), 256, 0, s>>>(c->params + l.off, l.cout, l.cin, l.frows, l.bcols, l.f, l.b);
     CR_CHECK(cuda_status(cudaGetLastError(), "corrector pack"));
   }
-  return VG_OK;
+  k_pack_tc<<<div_up(TC_W_BYTES / 2, 256), 256, 0, s>>>(c->params, c->wtc);
+  return cuda_status(cudaGetLastError(), "corrector pack");
 }
 
 // pred = net(features(batch)) for the batch's rows (FP32 [rows][128])
@@ -699,6 +1129,14 @@ int vg_corr_create(int32_t max_rows, int32_t protect_modes, float vmax, float ta
   CR_TRY(cr_alloc(c, &c->gmean, pos, "corrector group means"));
   CR_TRY(cr_alloc(c, &c->tmean, pos, "corrector group means"));
   CR_TRY(cr_alloc(c, &c->pmean, pos, "corrector group means"));
+  CR_TRY(cr_alloc(c, &c->wtc, (size_t)TC_W_BYTES / 2, "corrector weights"));
+  CR_TRY(cr_alloc(c, &c->err, 1, "corrector status"));
+  {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    c->n_sm = 1;
+    cudaDeviceGetAttribute(&c->n_sm, cudaDevAttrMultiProcessorCount, dev);
+  }
   {
     // orthonormal basis of the protected modes on the 128-point row
     std::vector<float> b((size_t)std::max(c->nq, 1) * CP, 0.f), bt((size_t)CP * CP, 0.f);
@@ -777,10 +1215,52 @@ int vg_corr_apply(vg_corrector* c, const vg_corr_batch* b, float* g_out, vg_stre
     return VG_ERR_ARG;
   }
   cudaStream_t s = (cudaStream_t)stream;
-  CR_CHECK(forward(c, *b, s));
+  if (c->engine == 0) {
+    if (b->group_rows > 0) {
+      k_group_mean<<<b->rows / b->group_rows, CP, 0, s>>>(b->g, b->group_rows, c->gmean);
+      CR_CHECK(cuda_status(cudaGetLastError(), "corrector group mean"));
+      if (b->g_prev) {
+        k_group_mean<<<b->rows / b->group_rows, CP, 0, s>>>(b->g_prev, b->group_rows, c->pmean);
+        CR_CHECK(cuda_status(cudaGetLastError(), "corrector group mean"));
+      }
+    }
+    CR_CHECK(cuda_status(ensure_smem((const void*)k_corr_forward_tc, TC_SMEM), "corrector fused kernel"));
+    const int grid = std::min(b->rows, c->n_sm);
+    k_corr_forward_tc<<<grid, TC_THREADS, TC_SMEM, s>>>(b->g, b->g_prev, c->gmean, c->pmean, b->group_rows,
+                                                        b->row_feat, b->rows, c->vmax,
+                                                        reinterpret_cast<const uint4*>(c->wtc), c->params, c->pred,
+                                                        c->scale, c->err);
+    CR_CHECK(cuda_status(cudaGetLastError(), "corrector forward"));
+  } else {
+    CR_CHECK(forward(c, *b, s));
+  }
   k_apply<<<b->rows, CP, 0, s>>>(b->g, c->gmean, b->group_rows, c->pred, c->scale, c->tau, c->basis, c->basis_t,
                                  c->nq, g_out);
   return cuda_status(cudaGetLastError(), "corrector apply");
+}
+
+int vg_corr_set_engine(vg_corrector* c, int32_t engine) {
+  if (!c || engine < 0 || engine > 1) {
+    set_error("corrector: engine must be 0 (fused tcgen05) or 1 (per-layer mma.sync)");
+    return VG_ERR_ARG;
+  }
+  c->engine = engine;
+  return VG_OK;
+}
+
+int vg_corr_status(vg_corrector* c, int32_t* flags) {
+  if (!c || !flags) {
+    set_error("corrector: null argument");
+    return VG_ERR_ARG;
+  }
+  int h = 0;
+  CR_CHECK(cuda_status(cudaMemcpy(&h, c->err, sizeof(int), cudaMemcpyDeviceToHost), "corrector status"));
+  *flags = h;
+  if (h) {
+    set_error("corrector: a bounded wait of the fused kernel ran out (its output is invalid)");
+    return VG_ERR_TIMEOUT;
+  }
+  return VG_OK;
 }
 
 int vg_corr_loss(vg_corrector* c, const vg_corr_batch* b, double* loss_out, vg_stream stream) {

@@ -35,6 +35,14 @@ struct SweepRunDev {
 };
 
 constexpr int SWEEP_BLOCK = 256;
+// resident CTAs per SM the row and column kernels are compiled for (the
+// register budget per thread follows); build-time tuning knobs
+#ifndef VG_ROW_MIN_BLOCKS
+#define VG_ROW_MIN_BLOCKS 4
+#endif
+#ifndef VG_COL_MIN_BLOCKS_SMALL
+#define VG_COL_MIN_BLOCKS_SMALL 3
+#endif
 constexpr int SWEEP_FIELD_BLOCK = 128;
 constexpr int SWEEP_MAX_CLASSES = 6;  // nv in {64, ..., 2048}
 
@@ -54,7 +62,7 @@ struct SweepConsts {
 // x-drift of one (run, tile) item per CTA; one kernel per nx class keeps
 // each instantiation's code and registers small
 template <int NX>
-__global__ void __launch_bounds__(SWEEP_BLOCK, (NX <= 64 ? 3 : 4)) k_sweep_col(const SweepRunDev* __restrict__ runs,
+__global__ void __launch_bounds__(SWEEP_BLOCK, (NX <= 64 ? VG_COL_MIN_BLOCKS_SMALL : 4)) k_sweep_col(const SweepRunDev* __restrict__ runs,
                                                               const int2* __restrict__ items, float* g,
                                                               const SweepConsts* __restrict__ scp,
                                                               const cx<float>* __restrict__ tw, float2* dpart) {
@@ -137,14 +145,16 @@ struct SweepRowArgs {
   const float* e32;
   double* mom;
   double dt1, dt2;
-  float hk1[SWEEP_MAX_CLASSES], hk2[SWEEP_MAX_CLASSES];  // -dkv dt / 2 per nv class
+  // -dkv dt / 2 of this launch's nv class: scalars, since indexing a kernel
+  // parameter array by the run's class would copy the arguments to the stack
+  float hk1, hk2;
   int fp, want_mom, dougherty;
   const cx<float>* tw;
 };
 
 // one (run, row-pair group) item per CTA; one kernel per nv class
 template <int N>
-__global__ void __launch_bounds__(SWEEP_BLOCK, 3) k_sweep_row(const SweepRunDev* __restrict__ runs,
+__global__ void __launch_bounds__(SWEEP_BLOCK, VG_ROW_MIN_BLOCKS) k_sweep_row(const SweepRunDev* __restrict__ runs,
                                                               const int2* __restrict__ items, SweepRowArgs sa,
                                                               const SweepConsts* __restrict__ scp) {
   constexpr int R = row32_radix(N);
@@ -160,8 +170,8 @@ __global__ void __launch_bounds__(SWEEP_BLOCK, 3) k_sweep_row(const SweepRunDev*
   a.e32 = sa.e32 + r.x_off;
   a.dt1 = sa.dt1;
   a.dt2 = sa.dt2;
-  a.hk1 = sa.hk1[r.cls];
-  a.hk2 = sa.hk2[r.cls];
+  a.hk1 = sa.hk1;
+  a.hk2 = sa.hk2;
   a.fp = sa.fp && r.fp;
   a.dougherty = sa.dougherty;
   a.nudt2 = r.nudt2;
@@ -205,15 +215,17 @@ __global__ void __launch_bounds__(128) k_sweep_store(const SweepRunDev* __restri
 __global__ void k_sweep_init(const SweepRunDev* __restrict__ runs, const double* __restrict__ amp,
                              const SweepConsts* __restrict__ scp, float* __restrict__ g, double* __restrict__ e,
                              float* __restrict__ e32) {
+  __shared__ double cx_s[256];  // cos(k x_j) of the run's x points (nx <= 256)
   const SweepRunDev r = runs[blockIdx.x];
   const double A = amp[blockIdx.x];
   const float* f0 = scp->rc[r.cls].f0;
   const size_t n = (size_t)r.nx * r.nv;
+  // k x_j = pi (2 j + 1) / nx on the cell-centred grid of [0, 2 pi / k)
+  for (int x = threadIdx.x; x < r.nx; x += blockDim.x) cx_s[x] = cospi((2.0 * x + 1.0) / (double)r.nx);
+  __syncthreads();
   for (size_t q = threadIdx.x; q < n; q += blockDim.x) {
     const int x = (int)(q / r.nv), vj = (int)(q % r.nv);
-    // k x_j = pi (2 j + 1) / nx on the cell-centred grid of [0, 2 pi / k)
-    const double c = cospi((2.0 * x + 1.0) / (double)r.nx);
-    g[r.g_off + q] = (float)(A * c * (double)f0[vj]);
+    g[r.g_off + q] = (float)(A * cx_s[x] * (double)f0[vj]);
   }
   // the first half-kick of a batch reads the FP32 copy of the field
   for (int x = threadIdx.x; x < r.nx; x += blockDim.x) {
@@ -448,11 +460,6 @@ int sweep_sequence(vg_sweep* s, int nsteps, double* e_hist, double* s_hist, int 
     a.mom = s->mom;
     a.dt1 = dt1;
     a.dt2 = dt2;
-    for (size_t c = 0; c < s->nv_of_class.size(); ++c) {
-      const double dkv = s->consts_h.rc[c].dkv;
-      a.hk1[c] = (float)(-0.5 * dkv * dt1);
-      a.hk2[c] = (float)(-0.5 * dkv * dt2);
-    }
     a.fp = fp;
     a.want_mom = mom;
     a.dougherty = dg;
@@ -460,13 +467,19 @@ int sweep_sequence(vg_sweep* s, int nsteps, double* e_hist, double* s_hist, int 
     return cuda_status(prof_call(&s->prof, kind, st, [&] {
                          for (size_t c = 0; c < s->row_nv.size(); ++c) {
                            cudaError_t err = cudaSuccess;
+                           SweepRowArgs ac = a;
+                           const int cls = (int)(std::find(s->nv_of_class.begin(), s->nv_of_class.end(),
+                                                           s->row_nv[c]) - s->nv_of_class.begin());
+                           const double dkv = s->consts_h.rc[cls].dkv;
+                           ac.hk1 = (float)(-0.5 * dkv * dt1);
+                           ac.hk2 = (float)(-0.5 * dkv * dt2);
                            switch (s->row_nv[c]) {
-                             case 64: err = sweep_row_launch<64>(s, (int)c, a, st); break;
-                             case 128: err = sweep_row_launch<128>(s, (int)c, a, st); break;
-                             case 256: err = sweep_row_launch<256>(s, (int)c, a, st); break;
-                             case 512: err = sweep_row_launch<512>(s, (int)c, a, st); break;
-                             case 1024: err = sweep_row_launch<1024>(s, (int)c, a, st); break;
-                             default: err = sweep_row_launch<2048>(s, (int)c, a, st); break;
+                             case 64: err = sweep_row_launch<64>(s, (int)c, ac, st); break;
+                             case 128: err = sweep_row_launch<128>(s, (int)c, ac, st); break;
+                             case 256: err = sweep_row_launch<256>(s, (int)c, ac, st); break;
+                             case 512: err = sweep_row_launch<512>(s, (int)c, ac, st); break;
+                             case 1024: err = sweep_row_launch<1024>(s, (int)c, ac, st); break;
+                             default: err = sweep_row_launch<2048>(s, (int)c, ac, st); break;
                            }
                            if (err != cudaSuccess) return err;
                          }

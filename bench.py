@@ -121,6 +121,13 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
+# DRAM bytes of one sweep row pass per cell (dram__bytes_read.sum +
+# dram__bytes_write.sum summed over the pass's three nv-class launches),
+# measured by ncu on the 800-run sweep (36.0 M cells): 145.04 MB read,
+# 34.40 MB written.  The full 4096-run pass is scaled from it per cell.
+ROW_PASS_DRAM_BYTES_PER_CELL = (145037312 + 34400768) / 36036608
+
+
 def peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -236,14 +243,16 @@ def run_e2e(plan, f, e, storage, hist, tb_host, drv_host, W, K, stream, torch):
     return (t1 - t0), h2d, d2h
 
 
-def run_sweep_gpu(args, w, rank, world):
+def run_sweep_gpu(args, w, rank, world, global_rank=0):
     import torch
     from vlapy_gb300 import _lib
+    from vlapy_gb300.replicas import shard_seed
     from vlapy_gb300.sweep import Sweep, sweep_config
 
     torch.cuda.set_device(rank % max(1, torch.cuda.device_count()))
     _lib.load()
-    runs = sweep_config(w["n_runs"], w["seed"])
+    # each rank advances its own shard of the sweep (weak scaling)
+    runs = sweep_config(w["n_runs"], shard_seed(w["seed"], global_rank))
     sw = Sweep(runs, vmax=w["vmax"], dt=w["dt"])
     K, W = args.steps, args.warmup
     eh, sh = sw.history(K)
@@ -661,18 +670,13 @@ def main():
         print(json.dumps(line))
         return
 
-    import torch
-    if world > 1:
-        torch.distributed.init_process_group("nccl")
+    from vlapy_gb300 import replicas
+    replicas.init(world)
     ms, prof, clk, e2e, plan = run_gpu(args, w, int(os.environ.get("LOCAL_RANK", rank)), world)
-    t_max = ms
-    if world > 1:
-        tt = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_max = float(tt.item())
-    value = world * cells * args.steps / (t_max / 1e3)
+    # replicas: every rank advances its own copy of the run
+    t_max, _, value = replicas.aggregate(ms, cells * args.steps, world)
     e2e_sec, h2d, d2h = e2e
-    e2e_val = world * cells * args.steps / e2e_sec
+    _, _, e2e_val = replicas.aggregate(1e3 * e2e_sec, cells * args.steps, world)
     dom = max(prof.items(), key=lambda kv: kv[1]["total_ms"])
     name, pd = dom
     avg_ms = pd["total_ms"] / pd["launches"]
@@ -716,7 +720,7 @@ def main_sweep(args, w, rank, world):
     if args.impl == "reference":
         if rank != 0:
             return
-        val, rps, cores, n, steps, wall = cpu_baseline_sweep(w, n_sample=max(36, args.steps), steps=60)
+        val, rps, cores, n, steps, wall = cpu_baseline_sweep(w, n_sample=max(36, args.steps), steps=360)
         line = {"metric": "cell-updates/s", "value": val, "unit": "cell-updates/s", "n_gpus": args.gpus,
                 "steps": steps, "warmup": 0, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg, "impl": "reference",
@@ -728,19 +732,15 @@ def main_sweep(args, w, rank, world):
                 "e2e": {"value": val, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
         return
-    import torch
-    if world > 1:
-        torch.distributed.init_process_group("nccl")
-    ms, prof, clk, e2e, sw = run_sweep_gpu(args, w, int(os.environ.get("LOCAL_RANK", rank)), world)
-    t_max = ms
-    if world > 1:
-        tt = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_max = float(tt.item())
+    from vlapy_gb300 import replicas
+    replicas.init(world)
+    ms, prof, clk, e2e, sw = run_sweep_gpu(args, w, int(os.environ.get("LOCAL_RANK", rank)), world, rank)
     cells = sw.cells
-    value = world * cells * args.steps / (t_max / 1e3)
+    # every rank advances its own shard: units summed, time the slowest rank's
+    t_max, total_cells, value = replicas.aggregate(ms, cells * args.steps, world)
     runs_per_s = world * sw.n_runs / (t_max / args.steps / 1e3 * SWEEP_STEPS)
     e2e_sec, h2d, d2h = e2e
+    _, _, e2e_value = replicas.aggregate(1e3 * e2e_sec, cells * args.steps, world)
     dom_name, dom = max(prof.items(), key=lambda kv: kv[1]["total_ms"])
     avg_ms = dom["total_ms"] / dom["launches"]
     peak, peak_kind = peaks()
@@ -770,10 +770,14 @@ def main_sweep(args, w, rank, world):
         "runs_per_s": runs_per_s,
         "fp64_plain_gpu": fp64,
         "learned_path": learned,
-        "e2e": {"value": world * cells * args.steps / e2e_sec, "unit": "cell-updates/s",
+        "e2e": {"value": e2e_value, "unit": "cell-updates/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "kernel": dom_name, "peak_source": peak_kind, "kernel_ms": avg_ms,
+                     "traffic": ROW_PASS_DRAM_BYTES_PER_CELL * cells if dom_name == "sweep_row_pass" else None,
+                     "traffic_source": "ncu dram bytes of one row pass of the 800-run sweep, scaled per cell; "
+                                       "below the algorithmic 8 B/cell because written rows stay in L2 past the "
+                                       "launch",
+                     "kernel": dom_name, "peak_source": peak_kind, "kernel_ms": avg_ms,
                      "bytes_per_launch": dom["bytes_per_launch"]},
         "kernels": {k: {"launches": d["launches"], "avg_ms": d["total_ms"] / d["launches"]} for k, d in prof.items()},
         "gpu_launches": int(round(launches_per_step * args.steps)),

@@ -216,6 +216,16 @@ int vg_sweep_set_state(vg_sweep* sweep, const float* g_in, const double* e_in, v
  * calls on the same stream (the corrector does).  Writing e this way would
  * bypass the FP32 copy the kicks read: use vg_sweep_set_state for e. */
 int vg_sweep_state_ptr(vg_sweep* sweep, float** g, double** e);
+/* Damping rate and frequency of every run from an e history [rows][x_points]
+ * (DEVICE) whose row k is time t0 + k dt: the peaks of |FFT_x(e)[1]| in
+ * [t_min, t_max], each refined by a parabola in log space, give the rate as
+ * the least-squares slope of log peak height against time and the frequency
+ * as pi over the mean peak spacing; NaN with fewer than three peaks.
+ * rate_out, freq_out: DEVICE [n_runs].  Replaces the host post-processing of
+ * vlapy/diagnostics/low_level_helpers.py:69-87 with one launch per sweep (an
+ * estimator that is unbiased for undriven runs; rows <= 16384). */
+int vg_sweep_damping(vg_sweep* sweep, const double* e_hist, int32_t rows, double t0, double t_min, double t_max,
+                     double* rate_out, double* freq_out, vg_stream stream);
 /* per-kernel timing of vg_sweep_run_steps (same contract as vg_profile_*) */
 int vg_sweep_profile_enable(vg_sweep* sweep, int32_t enable);
 int vg_sweep_profile_read(vg_sweep* sweep, vg_prof_entry* out, int32_t max, int32_t* n_out);

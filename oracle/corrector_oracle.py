@@ -75,13 +75,23 @@ def group_mean(g32, group_rows):
     return (acc / group_rows).repeat_interleave(group_rows, dim=0)
 
 
+def mean_pair(g32, group_rows):
+    """The group mean as the kernels carry it: an FP32 pair (hi, lo) with
+    hi + lo = the float64 mean (to ~1e-14)."""
+    m = group_mean(g32, group_rows)
+    hi = m.to(torch.float32)
+    lo = (m - hi.to(torch.float64)).to(torch.float32)
+    return hi, lo
+
+
 def deviation(g, group_rows):
-    """Rows minus their group mean, rounded once to float32 (the rows
+    """Rows minus their group mean in FP32 as (g - hi) - lo (the rows
     themselves without groups)."""
     g32 = torch.as_tensor(np.asarray(g, dtype=np.float32))
     if not group_rows:
         return g32
-    return (g32.to(torch.float64) - group_mean(g32, group_rows)).to(torch.float32)
+    hi, lo = mean_pair(g32, group_rows)
+    return (g32 - hi) - lo
 
 
 def features(g, row_feat, vmax, emulate, group_rows=0, prev=None):
@@ -179,9 +189,12 @@ def apply(params, g, row_feat, vmax, tau, emulate=True, group_rows=0, protect_mo
     pred, s, _, _ = forward(params, g, row_feat, vmax, emulate, group_rows, prev)
     g32 = torch.as_tensor(np.asarray(g, dtype=np.float32))
     d = deviation(g, group_rows).to(torch.float64)
-    m = group_mean(g32, group_rows) if group_rows else torch.zeros_like(d)
     dh = high_pass(d, protect_modes)
     hn = dh + high_pass(s[:, None] * tau * pred, protect_modes)
     old, new = (dh * dh).sum(1), (hn * hn).sum(1)
     factor = torch.where(new > old, torch.sqrt(old / new), torch.ones_like(old))
-    return (m + (d - dh) + hn * factor[:, None]).numpy()
+    dn = (d - dh) + hn * factor[:, None]
+    if not group_rows:
+        return dn.numpy()
+    hi, lo = mean_pair(g32, group_rows)
+    return (hi.to(torch.float64) + (lo.to(torch.float64) + dn)).numpy()

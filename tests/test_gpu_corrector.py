@@ -140,15 +140,16 @@ def test_gradients_match_oracle(group, modes):
         if name == "W1":  # input channels 4..15 carry zeros: their gradient is exactly zero
             a3 = a.reshape(shape)
             assert np.all(a3[:, 4:, :] == 0)
-        # emulated rounding: only FP32 accumulation order and rare BF16
-        # rounding flips differ; plain FP64: the BF16 quantisation itself
-        assert rel(a, e) <= 5e-3, (name, rel(a, e))
         if name == "b4" and modes:
             # the projected loss is blind to a constant output: the exact b4
-            # gradient is zero, and only the BF16 rounding of the loss
-            # gradient leaves a residue (matched by the emulation above)
+            # gradient is zero, and what remains is the sum of the BF16
+            # rounding errors of the loss gradient, noise of no fixed value
             assert abs(a[0]) <= 1e-2 * np.abs(grad_x).max()
+            assert abs(e[0]) <= 1e-2 * np.abs(grad_x).max()
         else:
+            # emulated rounding: only FP32 accumulation order and rare BF16
+            # rounding flips differ; plain FP64: the BF16 quantisation itself
+            assert rel(a, e) <= 5e-3, (name, rel(a, e))
             assert rel(a, x) <= 0.15, (name, rel(a, x))
         o += n
 

@@ -173,3 +173,28 @@ def test_sweep_state_moves_between_sweeps():
     # the split run applies the two half-kicks at step 6 as separate passes
     assert torch.linalg.norm(gc - ga) <= 1e-5 * torch.linalg.norm(ga)
     assert torch.linalg.norm(ec - ea) <= 1e-5 * torch.linalg.norm(ea)
+
+
+def test_sweep_damping_on_device_matches_host_fit():
+    """vg_sweep_damping equals the host diagnostic on the same histories."""
+    from vlapy_gb300.diagnostics import damping_fit, mode_amplitude
+    from vlapy_gb300.sweep import Sweep
+    runs = mixed_runs()
+    sw = Sweep(runs)
+    sw.reset()
+    nsteps = 400
+    eh, sh = sw.history(nsteps)
+    sw.run_steps(nsteps, eh, sh)
+    t = 0.1 * np.arange(1, nsteps + 1)
+    for t_min, t_max in ((5.0, 40.0), (5.0, None), (30.0, 30.4)):
+        rate, freq = sw.damping(eh, t_min=t_min, t_max=t_max)
+        rate, freq = rate.cpu().numpy(), freq.cpu().numpy()
+        for i in range(len(runs)):
+            rh, fh = damping_fit(t, mode_amplitude(sw.e_of(eh, i).cpu().numpy()), t_min=t_min, t_max=t_max)
+            if np.isnan(rh):
+                assert np.isnan(rate[i]) and np.isnan(freq[i]), (i, t_min, t_max)
+            else:
+                np.testing.assert_allclose(rate[i], rh, rtol=1e-7, atol=1e-12)
+                np.testing.assert_allclose(freq[i], fh, rtol=1e-9)
+    with pytest.raises(ValueError):
+        sw.damping(eh[:, :5].contiguous())

@@ -309,7 +309,7 @@ __global__ void k_wgrad_reduce(const float* __restrict__ part, const float* __re
 // can exceed its x-varying part by 1e3 or more (the coarse grid's slow
 // collisional drift of the background), so an FP32 mean would leave errors
 // comparable to the deviations it is subtracted from.  out[group][p].
-__global__ void k_group_mean(const float* __restrict__ g, int group_rows, double* __restrict__ out) {
+__global__ void k_group_mean(const float* __restrict__ g, int group_rows, float2* __restrict__ out) {
   const int grp = blockIdx.x, p = threadIdx.x;  // blockDim = CP
   const float* src = g + (size_t)grp * group_rows * CP + p;
   // double-float (TwoSum) accumulation: FP64-grade, on the FP32 pipes
@@ -321,21 +321,36 @@ __global__ void k_group_mean(const float* __restrict__ g, int group_rows, double
     lo += (hi - (t - bb)) + (x - bb);
     hi = t;
   }
-  out[(size_t)grp * CP + p] = ((double)hi + (double)lo) / (double)group_rows;
+  // the mean as a double-float pair (hi, lo), so that the kernels that take
+  // it out of a row stay on the FP32 pipes
+  const double m = ((double)hi + (double)lo) / (double)group_rows;
+  const float mh = (float)m;
+  out[(size_t)grp * CP + p] = make_float2(mh, (float)(m - (double)mh));
 }
 
 // deviation of g[q] (row `row`, position p) from its group mean, rounded once
-__device__ __forceinline__ float deviation(float gq, const double* __restrict__ gmean, int group_rows, int row,
+// (g - hi is exact when g is within a factor 2 of the mean, the case where
+// the mean dwarfs the deviation; then one rounding for lo)
+__device__ __forceinline__ float deviation(float gq, const float2* __restrict__ gmean, int group_rows, int row,
                                            int p) {
-  return group_rows > 0 ? (float)((double)gq - gmean[(size_t)(row / group_rows) * CP + p]) : gq;
+  if (group_rows <= 0) return gq;
+  const float2 m = gmean[(size_t)(row / group_rows) * CP + p];
+  return __fsub_rn(__fsub_rn(gq, m.x), m.y);
+}
+// the group mean plus a deviation, rounded once more (inverse of deviation)
+__device__ __forceinline__ float with_mean(float dn, const float2* __restrict__ gmean, int group_rows, int row,
+                                           int p) {
+  if (group_rows <= 0) return dn;
+  const float2 m = gmean[(size_t)(row / group_rows) * CP + p];
+  return __fadd_rn(m.x, __fadd_rn(m.y, dn));
 }
 
 // features [row][p][16]: d / s, v / vmax, the row's scalar feature (the
 // collision-rate channel), d_prev / s, zeros; d = g minus its group mean
 // (or g itself without groups), d_prev the same of the row before the
 // coarse step (zero channel without it), s = RMS of d over the row
-__global__ void k_features(const float* __restrict__ g, const double* __restrict__ gmean,
-                           const float* __restrict__ gp, const double* __restrict__ pmean, int group_rows,
+__global__ void k_features(const float* __restrict__ g, const float2* __restrict__ gmean,
+                           const float* __restrict__ gp, const float2* __restrict__ pmean, int group_rows,
                            const float* __restrict__ row_feat, int rows, float vmax, __nv_bfloat16* __restrict__ x0,
                            float* __restrict__ scale) {
   __shared__ float red[CP];
@@ -431,7 +446,7 @@ __device__ __forceinline__ void high_pass2(float a, float b, const float* __rest
 // scale tau (means only with groups); dy4 channel 0 = d loss / d pred =
 // 2 P (pred - want) / n.  One row at a time per CTA, blockDim = CP.
 __global__ void k_loss(const float* __restrict__ pred, const float* __restrict__ g, const float* __restrict__ target,
-                       const double* __restrict__ gmean, const double* __restrict__ tmean, int group_rows,
+                       const float2* __restrict__ gmean, const float2* __restrict__ tmean, int group_rows,
                        const float* __restrict__ scale, float tau, const float* __restrict__ basis,
                        const float* __restrict__ basis_t, int nq, int rows, __nv_bfloat16* __restrict__ dy4,
                        float* __restrict__ loss_part) {
@@ -466,7 +481,7 @@ __global__ void k_loss(const float* __restrict__ pred, const float* __restrict__
 // never touched, and the corrected high part is never longer in L2 norm
 // than the coarse step left it, so repeated corrections cannot feed energy
 // into a run.  blockDim = CP, one row per CTA.
-__global__ void k_apply(const float* __restrict__ g, const double* __restrict__ gmean, int group_rows,
+__global__ void k_apply(const float* __restrict__ g, const float2* __restrict__ gmean, int group_rows,
                         const float* __restrict__ pred, const float* __restrict__ scale, float tau,
                         const float* __restrict__ basis, const float* __restrict__ basis_t, int nq,
                         float* __restrict__ out) {
@@ -494,9 +509,7 @@ __global__ void k_apply(const float* __restrict__ g, const double* __restrict__ 
   const float r_new = (wsum[1][0] + wsum[1][1]) + (wsum[1][2] + wsum[1][3]);
   const float factor = r_new > r_old ? sqrtf(r_old / r_new) : 1.f;
   const float dn = (d - dh) + hn * factor;
-  // g - d is the group mean rounded to FP32 next to g; adding the corrected
-  // deviation in FP64 keeps the x-varying part exact to FP32
-  out[q] = group_rows > 0 ? (float)(gmean[(size_t)(row / group_rows) * CP + p] + (double)dn) : dn;
+  out[q] = with_mean(dn, gmean, group_rows, row, p);
 }
 
 __global__ void k_adam(float* __restrict__ w, const float* __restrict__ grad, float* __restrict__ m,
@@ -548,7 +561,7 @@ __global__ void k_pack(const float* __restrict__ w, int cout, int cin, int frows
 // bytes (rows t .. t + 127 of the 132-row tile with its 2-row halos).
 // ---------------------------------------------------------------------------
 
-constexpr int TC_SLOTS = 4;                             // rows in flight per CTA
+constexpr int TC_SLOTS = 6;                             // rows in flight per CTA
 constexpr int TC_THREADS = TC_SLOTS * 128;               // 4 warps per slot
 constexpr int TC_TILE_ROWS = CROWS;                      // 132
 constexpr int TC_LBO_ACT = 16 * TC_TILE_ROWS;            // 2112 B
@@ -569,7 +582,7 @@ constexpr int TC_OFF_F = TC_OFF_SLOT + TC_SLOTS * TC_SLOT_BYTES;  // floats: bia
 constexpr int TC_NF = 256 + TC_SLOTS * 128;
 constexpr int TC_OFF_BAR = TC_OFF_F + TC_NF * 4;         // done[slots] mbarriers, TMEM address
 constexpr int TC_SMEM = TC_OFF_BAR + 8 * TC_SLOTS + 16;
-constexpr int TC_TMEM_COLS = 256;                        // 64 per slot, a power of two
+constexpr int TC_TMEM_COLS = 512;                        // 64 per slot, rounded up to a power of two
 constexpr unsigned long long TC_WAIT_NS = 2000000000ull;  // 2 s: a wait that long has failed
 static_assert(TC_SMEM <= 227 * 1024, "fused corrector tiles exceed shared memory");
 static_assert(TC_SLOTS * 64 <= TC_TMEM_COLS, "TMEM columns");
@@ -673,30 +686,34 @@ __device__ __forceinline__ void tc_layer_issue(uint32_t tmem, uint32_t act, uint
 }
 
 // epilogue of a hidden layer: TMEM (this thread's position, 64 channels) +
-// bias, ReLU, BF16 into row p + 2 of the next tile; the four 16-column loads
-// are in flight together
+// bias, ReLU, BF16 into row p + 2 of the next tile; two halves of 32
+// columns, each with its two 16-column loads in flight together (the
+// register budget of six slots per CTA)
 __device__ __forceinline__ void tc_hidden_epilogue(uint32_t tmem, int quarter, int p, const float* bias,
                                                    unsigned char* out_tile) {
   const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
-  uint32_t r[4][16];
 #pragma unroll
-  for (int q = 0; q < 4; ++q) tc_ld16_nowait(tmem + lane_base + 16 * q, r[q]);
-  tc_wait_ld();
+  for (int half = 0; half < 2; ++half) {
+    uint32_t r[2][16];
+    tc_ld16_nowait(tmem + lane_base + 32 * half, r[0]);
+    tc_ld16_nowait(tmem + lane_base + 32 * half + 16, r[1]);
+    tc_wait_ld();
 #pragma unroll
-  for (int q = 0; q < 4; ++q) {
+    for (int q = 0; q < 2; ++q) {
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      uint32_t w[4];
+      for (int h = 0; h < 2; ++h) {
+        uint32_t w[4];
 #pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const int c = 16 * q + 8 * h + 2 * j;
-        const __nv_bfloat162 pr =
-            __floats2bfloat162_rn(fmaxf(__uint_as_float(r[q][8 * h + 2 * j]) + bias[c], 0.f),
-                                  fmaxf(__uint_as_float(r[q][8 * h + 2 * j + 1]) + bias[c + 1], 0.f));
-        w[j] = *reinterpret_cast<const uint32_t*>(&pr);
+        for (int j = 0; j < 4; ++j) {
+          const int c = 32 * half + 16 * q + 8 * h + 2 * j;
+          const __nv_bfloat162 pr =
+              __floats2bfloat162_rn(fmaxf(__uint_as_float(r[q][8 * h + 2 * j]) + bias[c], 0.f),
+                                    fmaxf(__uint_as_float(r[q][8 * h + 2 * j + 1]) + bias[c + 1], 0.f));
+          w[j] = *reinterpret_cast<const uint32_t*>(&pr);
+        }
+        *reinterpret_cast<uint4*>(out_tile + tc_off(p + CHALO, 32 * half + 16 * q + 8 * h, TC_LBO_ACT)) =
+            make_uint4(w[0], w[1], w[2], w[3]);
       }
-      *reinterpret_cast<uint4*>(out_tile + tc_off(p + CHALO, 16 * q + 8 * h, TC_LBO_ACT)) =
-          make_uint4(w[0], w[1], w[2], w[3]);
     }
   }
 }
@@ -723,8 +740,8 @@ __device__ __forceinline__ bool slot_any(int slot, bool v) {
 // (k * TC_SLOTS + s).  Every wait is bounded: a wait that gives up sets err,
 // and the slot leaves together after a barrier vote.
 __global__ void __launch_bounds__(TC_THREADS, 1)
-    k_corr_forward_tc(const float* __restrict__ g, const float* __restrict__ gp, const double* __restrict__ gmean,
-                      const double* __restrict__ pmean, int group_rows, const float* __restrict__ row_feat, int rows,
+    k_corr_forward_tc(const float* __restrict__ g, const float* __restrict__ gp, const float2* __restrict__ gmean,
+                      const float2* __restrict__ pmean, int group_rows, const float* __restrict__ row_feat, int rows,
                       float vmax, const uint4* __restrict__ wtc, const float* __restrict__ params,
                       float* __restrict__ pred_out, float* __restrict__ scale_out, int* __restrict__ err) {
   extern __shared__ __align__(128) unsigned char smem[];
@@ -780,7 +797,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   // this thread's inputs of a row, loaded one row ahead so that their
   // latency hides behind the current row's layers
   float in_g = 0.f, in_gp = 0.f, in_f = 0.f;
-  double in_m = 0.0, in_pm = 0.0;
+  float2 in_m = make_float2(0.f, 0.f), in_pm = make_float2(0.f, 0.f);
   auto fetch = [&](int r) {
     const size_t qq = (size_t)r * CP + p;
     in_g = g[qq];
@@ -789,7 +806,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     if (group_rows > 0) {
       const size_t mi = (size_t)(r / group_rows) * CP + p;
       in_m = gmean[mi];
-      in_pm = gp ? pmean[mi] : 0.0;
+      in_pm = gp ? pmean[mi] : make_float2(0.f, 0.f);
     }
   };
   // the slot's tile is complete: make it visible to the tensor core, then
@@ -814,8 +831,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   if (row < rows) fetch(row);
   while (ok && row < rows) {
     const size_t q = (size_t)row * CP + p;
-    const float d = group_rows > 0 ? (float)((double)in_g - in_m) : in_g;
-    const float dp = gp ? (group_rows > 0 ? (float)((double)in_gp - in_pm) : in_gp) : 0.f;
+    const float d = group_rows > 0 ? __fsub_rn(__fsub_rn(in_g, in_m.x), in_m.y) : in_g;
+    const float dp = gp ? (group_rows > 0 ? __fsub_rn(__fsub_rn(in_gp, in_pm.x), in_pm.y) : in_gp) : 0.f;
     const float feat = in_f;
     const int next = row + gridDim.x * TC_SLOTS;
     if (next < rows) fetch(next);
@@ -918,7 +935,7 @@ struct vg_corrector {
   // activations and gradients, channels-last [rows][128][C]
   __nv_bfloat16 *x0, *a1, *a2, *a3, *dy4, *d3, *d2, *d1;
   float *pred, *scale, *part, *bpart, *loss_part;
-  double *gmean, *tmean, *pmean;  // group means [groups][128]
+  float2 *gmean, *tmean, *pmean;  // group means [groups][128] as double-float pairs
   float vmax, tau;
   int engine;               // 0: fused tcgen05 forward, 1: per-layer mma.sync kernels
   int n_sm;

@@ -238,6 +238,88 @@ __global__ void k_sweep_e_to_f32(const double* __restrict__ e, int n, float* __r
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) e32[i] = (float)e[i];
 }
 
+// Damping rate and frequency of every run from its field history, on the
+// device: the amplitude of the first x-Fourier mode per step,
+// a_t = |sum_x e_t(x) exp(-2 pi i x / nx)|, its peaks inside [t_min, t_max]
+// (interior samples above the previous one and not below the next), each
+// refined by a parabola through log a at its three samples, then the
+// least-squares slope of log peak height against peak time (the rate) and
+// pi over the mean peak spacing (the frequency of a standing wave, whose |E_1|
+// peaks twice a period).  Fewer than three peaks give NaN.  One CTA per run;
+// dynamic shared memory holds the amplitudes (rows doubles) and the mode's
+// twiddles (2 nx doubles).
+__global__ void k_sweep_damping(const SweepRunDev* __restrict__ runs, const double* __restrict__ e_hist, int x_points,
+                                int rows, double t0, double dt, double t_min, double t_max,
+                                double* __restrict__ rate, double* __restrict__ freq) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double* amp = reinterpret_cast<double*>(smem_raw);
+  double* cw = amp + rows;
+  const SweepRunDev r = runs[blockIdx.x];
+  double* sw = cw + r.nx;
+  for (int x = threadIdx.x; x < r.nx; x += blockDim.x) sincospi(2.0 * x / (double)r.nx, &sw[x], &cw[x]);
+  __syncthreads();
+  for (int t = threadIdx.x; t < rows; t += blockDim.x) {
+    const double* e = e_hist + (size_t)t * x_points + r.x_off;
+    double re = 0.0, im = 0.0;
+    for (int x = 0; x < r.nx; ++x) {
+      re = fma(e[x], cw[x], re);
+      im = fma(-e[x], sw[x], im);
+    }
+    amp[t] = sqrt(re * re + im * im);
+  }
+  __syncthreads();
+  // the window [i0, i1] of samples with t_min <= t <= t_max
+  int i0 = (int)ceil((t_min - t0) / dt - 1e-9), i1 = (int)floor((t_max - t0) / dt + 1e-9);
+  if (i0 < 0) i0 = 0;
+  if (i1 > rows - 1) i1 = rows - 1;
+  double n = 0.0, st = 0.0, sl = 0.0, stt = 0.0, stl = 0.0, first = 1e300, last = -1e300;
+  for (int j = i0 + 1 + threadIdx.x; j <= i1 - 1; j += blockDim.x) {
+    const double a0 = amp[j - 1], a1 = amp[j], a2 = amp[j + 1];
+    if (!(a1 > a0 && a1 >= a2) || !(a0 > 0.0) || !(a2 > 0.0)) continue;
+    const double y0 = log(a0), y1 = log(a1), y2 = log(a2);
+    const double den = y0 - 2.0 * y1 + y2;
+    const double off = den != 0.0 ? 0.5 * (y0 - y2) / den : 0.0;
+    const double tp = t0 + j * dt + off * dt, lp = y1 - 0.25 * (y0 - y2) * off;
+    n += 1.0;
+    st += tp;
+    sl += lp;
+    stt += tp * tp;
+    stl += tp * lp;
+    first = fmin(first, tp);
+    last = fmax(last, tp);
+  }
+  __shared__ double red[7][32];
+  double v[7] = {n, st, sl, stt, stl, first, last};
+#pragma unroll
+  for (int k = 0; k < 7; ++k) {
+    for (int m = 16; m > 0; m >>= 1) {
+      const double o = __shfl_xor_sync(0xffffffffu, v[k], m);
+      v[k] = k == 5 ? fmin(v[k], o) : (k == 6 ? fmax(v[k], o) : v[k] + o);
+    }
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if (lane == 0)
+    for (int k = 0; k < 7; ++k) red[k][wid] = v[k];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a[7] = {0, 0, 0, 0, 0, 1e300, -1e300};
+    for (int w = 0; w < nw; ++w) {
+      for (int k = 0; k < 5; ++k) a[k] += red[k][w];
+      a[5] = fmin(a[5], red[5][w]);
+      a[6] = fmax(a[6], red[6][w]);
+    }
+    const double nan = __longlong_as_double(0x7ff8000000000000ll);
+    if (a[0] < 3.0) {
+      rate[blockIdx.x] = nan;
+      freq[blockIdx.x] = nan;
+    } else {
+      const double mt = a[1] / a[0], ml = a[2] / a[0];
+      rate[blockIdx.x] = (a[4] - a[0] * mt * ml) / (a[3] - a[0] * mt * mt);
+      freq[blockIdx.x] = 3.14159265358979323846 * (a[0] - 1.0) / (a[6] - a[5]);
+    }
+  }
+}
+
 __global__ void k_sweep_read(const SweepRunDev* __restrict__ runs, int run, const SweepConsts* __restrict__ scp,
                              const float* __restrict__ g, const double* __restrict__ f0d, const double* __restrict__ e,
                              double* __restrict__ f_out, double* __restrict__ e_out) {
@@ -786,6 +868,20 @@ int vg_sweep_set_state(vg_sweep* s, const float* g_in, const double* e_in, vg_st
     SW_CHECK(cuda_status(cudaGetLastError(), "sweep set state"));
   }
   return VG_OK;
+}
+
+int vg_sweep_damping(vg_sweep* s, const double* e_hist, int32_t rows, double t0, double t_min, double t_max,
+                     double* rate_out, double* freq_out, vg_stream stream) {
+  if (!s || !e_hist || !rate_out || !freq_out || rows < 3 || rows > 16384 || !(t_max > t_min)) {
+    set_error("sweep damping: needs a history of 3..16384 rows, outputs and t_min < t_max");
+    return VG_ERR_ARG;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t smem = (size_t)rows * sizeof(double) + 2 * 256 * sizeof(double);
+  SW_CHECK(cuda_status(ensure_smem((const void*)k_sweep_damping, smem), "sweep damping"));
+  k_sweep_damping<<<s->n_runs, 256, smem, st>>>(s->runs, e_hist, (int)s->x_points, rows, t0, s->dt, t_min, t_max,
+                                                 rate_out, freq_out);
+  return cuda_status(cudaGetLastError(), "sweep damping");
 }
 
 int vg_sweep_state_ptr(vg_sweep* s, float** g, double** e) {

@@ -154,6 +154,23 @@ class Sweep:
         check(self._lib.vg_sweep_state_ptr(self._h, C.byref(gp), None), "sweep state")
         return torch.as_tensor(_DeviceArray(self, gp.value, (self.cells,), "<f4"), device="cuda")
 
+    def damping(self, e_hist, t0=None, t_min=5.0, t_max=None, stream=None):
+        """(rate, frequency) float64 CUDA tensors [n_runs] of every run, fitted
+        on the device to the peaks of |E_1|(t) of an e history whose row k is
+        time t0 + k dt (t0 defaults to dt: the history of run_steps from a
+        reset); NaN for a run with fewer than three peaks in the window."""
+        rows = int(e_hist.shape[0])
+        if not (isinstance(e_hist, torch.Tensor) and e_hist.is_cuda and e_hist.dtype == torch.float64
+                and e_hist.is_contiguous() and tuple(e_hist.shape) == (rows, self.x_points)):
+            raise ValueError("e_hist must be a contiguous CUDA float64 tensor [rows][x_points]")
+        t0 = self.dt if t0 is None else float(t0)
+        t_max = t0 + (rows - 1) * self.dt if t_max is None else float(t_max)
+        rate = torch.empty(self.n_runs, dtype=torch.float64, device="cuda")
+        freq = torch.empty(self.n_runs, dtype=torch.float64, device="cuda")
+        check(self._lib.vg_sweep_damping(self._h, ptr(e_hist), rows, t0, float(t_min), t_max, ptr(rate), ptr(freq),
+                                         stream_handle(stream)), "sweep damping")
+        return rate, freq
+
     def e_of(self, e_hist, i):
         """e history [rows][nx] of run i from a sweep e-history buffer."""
         o = int(self.x_offsets[i])

@@ -29,7 +29,7 @@ def _worker(rank, world, port, out):
 
 def test_aggregate_over_two_gloo_ranks():
     world, port = 2, _free_port()
-    out = mp.Manager().dict()
+    out = mp.get_context("spawn").Manager().dict()
     mp.spawn(_worker, args=(world, port, out), nprocs=world, join=True)
     for r in range(world):
         t_max, total, rate = out[r]

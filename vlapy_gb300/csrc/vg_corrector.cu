@@ -481,35 +481,90 @@ __global__ void k_loss(const float* __restrict__ pred, const float* __restrict__
 // never touched, and the corrected high part is never longer in L2 norm
 // than the coarse step left it, so repeated corrections cannot feed energy
 // into a run.  blockDim = CP, one row per CTA.
-__global__ void k_apply(const float* __restrict__ g, const float2* __restrict__ gmean, int group_rows,
-                        const float* __restrict__ pred, const float* __restrict__ scale, float tau,
-                        const float* __restrict__ basis, const float* __restrict__ basis_t, int nq,
-                        float* __restrict__ out) {
-  __shared__ float sh[2 * CP], coef[2 * CP];
-  __shared__ float wsum[2][CP / 32];
-  const int row = blockIdx.x, p = threadIdx.x;
-  const size_t q = (size_t)row * CP + p;
-  const float d = deviation(g[q], gmean, group_rows, row, p);
-  float dh, c;
-  high_pass2(d, (scale[row] * tau) * pred[q], basis, basis_t, nq, sh, coef, dh, c);
-  const float hn = dh + c;
-  // row sums of dh^2 and hn^2: warp shuffles, then the four warps
-  float so = dh * dh, sn = hn * hn;
+constexpr int APPLY_ROWS = 8;  // rows per CTA of k_apply: each basis value loaded once serves 8 rows
+
+__global__ void __launch_bounds__(CP) k_apply(const float* __restrict__ g, const float2* __restrict__ gmean,
+                                               int group_rows, const float* __restrict__ pred,
+                                               const float* __restrict__ scale, float tau,
+                                               const float* __restrict__ basis, const float* __restrict__ basis_t,
+                                               int nq, int rows, float* __restrict__ out) {
+  __shared__ float sh[2][APPLY_ROWS][CP];    // d and c of each row
+  __shared__ float coef[2][APPLY_ROWS][CP];  // their coefficients on the protected modes
+  __shared__ float wsum[2][APPLY_ROWS][CP / 32];
+  const int p = threadIdx.x, row0 = blockIdx.x * APPLY_ROWS;
+  float d[APPLY_ROWS], c[APPLY_ROWS];
 #pragma unroll
-  for (int m = 16; m > 0; m >>= 1) {
-    so += __shfl_xor_sync(0xffffffffu, so, m);
-    sn += __shfl_xor_sync(0xffffffffu, sn, m);
-  }
-  if ((p & 31) == 0) {
-    wsum[0][p >> 5] = so;
-    wsum[1][p >> 5] = sn;
+  for (int r = 0; r < APPLY_ROWS; ++r) {
+    const int row = row0 + r < rows ? row0 + r : rows - 1;  // a short last block repeats its last row
+    const size_t q = (size_t)row * CP + p;
+    d[r] = deviation(g[q], gmean, group_rows, row, p);
+    c[r] = (scale[row] * tau) * pred[q];
+    sh[0][r][p] = d[r];
+    sh[1][r][p] = c[r];
   }
   __syncthreads();
-  const float r_old = (wsum[0][0] + wsum[0][1]) + (wsum[0][2] + wsum[0][3]);
-  const float r_new = (wsum[1][0] + wsum[1][1]) + (wsum[1][2] + wsum[1][3]);
-  const float factor = r_new > r_old ? sqrtf(r_old / r_new) : 1.f;
-  const float dn = (d - dh) + hn * factor;
-  out[q] = with_mean(dn, gmean, group_rows, row, p);
+  if (p < nq) {
+    float ad[APPLY_ROWS], ac[APPLY_ROWS];
+#pragma unroll
+    for (int r = 0; r < APPLY_ROWS; ++r) ad[r] = ac[r] = 0.f;
+#pragma unroll 4
+    for (int j = 0; j < CP; ++j) {
+      const float w = basis_t[j * CP + p];
+#pragma unroll
+      for (int r = 0; r < APPLY_ROWS; ++r) {
+        ad[r] = fmaf(sh[0][r][j], w, ad[r]);
+        ac[r] = fmaf(sh[1][r][j], w, ac[r]);
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < APPLY_ROWS; ++r) {
+      coef[0][r][p] = ad[r];
+      coef[1][r][p] = ac[r];
+    }
+  }
+  __syncthreads();
+  // the high parts Pd and Pc (projection off the protected modes)
+  float dh[APPLY_ROWS], hn[APPLY_ROWS];
+#pragma unroll
+  for (int r = 0; r < APPLY_ROWS; ++r) {
+    dh[r] = d[r];
+    hn[r] = c[r];
+  }
+#pragma unroll 4
+  for (int qq = 0; qq < nq; ++qq) {
+    const float w = basis[qq * CP + p];
+#pragma unroll
+    for (int r = 0; r < APPLY_ROWS; ++r) {
+      dh[r] = fmaf(-coef[0][r][qq], w, dh[r]);
+      hn[r] = fmaf(-coef[1][r][qq], w, hn[r]);
+    }
+  }
+  // hn = Pd + Pc; row sums of (Pd)^2 and hn^2 by warp shuffles, then the warps
+#pragma unroll
+  for (int r = 0; r < APPLY_ROWS; ++r) {
+    hn[r] += dh[r];
+    float so = dh[r] * dh[r], sn = hn[r] * hn[r];
+#pragma unroll
+    for (int m = 16; m > 0; m >>= 1) {
+      so += __shfl_xor_sync(0xffffffffu, so, m);
+      sn += __shfl_xor_sync(0xffffffffu, sn, m);
+    }
+    if ((p & 31) == 0) {
+      wsum[0][r][p >> 5] = so;
+      wsum[1][r][p >> 5] = sn;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int r = 0; r < APPLY_ROWS; ++r) {
+    const int row = row0 + r;
+    if (row >= rows) break;
+    const float r_old = (wsum[0][r][0] + wsum[0][r][1]) + (wsum[0][r][2] + wsum[0][r][3]);
+    const float r_new = (wsum[1][r][0] + wsum[1][r][1]) + (wsum[1][r][2] + wsum[1][r][3]);
+    const float factor = r_new > r_old ? sqrtf(r_old / r_new) : 1.f;
+    const float dn = (d[r] - dh[r]) + hn[r] * factor;
+    out[(size_t)row * CP + p] = with_mean(dn, gmean, group_rows, row, p);
+  }
 }
 
 __global__ void k_adam(float* __restrict__ w, const float* __restrict__ grad, float* __restrict__ m,
@@ -1251,8 +1306,8 @@ int vg_corr_apply(vg_corrector* c, const vg_corr_batch* b, float* g_out, vg_stre
   } else {
     CR_CHECK(forward(c, *b, s));
   }
-  k_apply<<<b->rows, CP, 0, s>>>(b->g, c->gmean, b->group_rows, c->pred, c->scale, c->tau, c->basis, c->basis_t,
-                                 c->nq, g_out);
+  k_apply<<<div_up(b->rows, APPLY_ROWS), CP, 0, s>>>(b->g, c->gmean, b->group_rows, c->pred, c->scale, c->tau,
+                                                     c->basis, c->basis_t, c->nq, b->rows, g_out);
   return cuda_status(cudaGetLastError(), "corrector apply");
 }
 

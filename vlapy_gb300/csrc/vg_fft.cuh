@@ -118,8 +118,16 @@ struct StockhamPass {
 #pragma unroll
       for (int m = 0; m < r; ++m) a[b][m] = s[sp<T>(j + m * NB)];
       if (NS > 1) {
+        // twiddles w^m: the power-of-two m from the table, the others as
+        // products of those (one extra rounding), halving the table loads
+        cx<T> w[r];
 #pragma unroll
-        for (int m = 1; m < r; ++m) a[b][m] = cmul(a[b][m], twiddle(tw, m * k * TWS, INV));
+        for (int m = 1; m < r; m <<= 1) w[m] = twiddle(tw, m * k * TWS, INV);
+#pragma unroll
+        for (int m = 3; m < r; ++m)
+          if (m & (m - 1)) w[m] = cmul(w[m & (m - 1)], w[m & -m]);
+#pragma unroll
+        for (int m = 1; m < r; ++m) a[b][m] = cmul(a[b][m], w[m]);
       }
       Dft<T, r, INV>::run(a[b]);
     }

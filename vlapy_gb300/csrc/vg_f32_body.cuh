@@ -26,11 +26,23 @@ __device__ __forceinline__ void col_tile(float* __restrict__ g, int nv, int c0, 
   const int grp = threadIdx.x / G, t = threadIdx.x - grp * G;
   cx<float>* sg = s + (size_t)grp * LD;
   const float scale = 1.f / NX;
-  const int total = NX * W;
-  for (int q = threadIdx.x; q < total; q += blockDim.x) {
-    const int x = q / W, c = q - x * W;
-    sf[2 * ((c >> 1) * LD + sp<float>(x)) + (c & 1)] = g[(size_t)x * nv + c0 + c];
+  // the tile in 16-byte vectors when W and nv are multiples of 4 floats
+  // (then so are c0 and every row start), else float by float
+  const bool vec = ((W | nv) & 3) == 0;
+  const int total = NX * W, total4 = vec ? total / 4 : 0;
+  for (int q = threadIdx.x; q < total4; q += blockDim.x) {
+    const int x = q / (W / 4), c = 4 * (q - x * (W / 4));
+    const float4 v = *reinterpret_cast<const float4*>(g + (size_t)x * nv + c0 + c);
+    sf[2 * ((c >> 1) * LD + sp<float>(x))] = v.x;
+    sf[2 * ((c >> 1) * LD + sp<float>(x)) + 1] = v.y;
+    sf[2 * (((c >> 1) + 1) * LD + sp<float>(x))] = v.z;
+    sf[2 * (((c >> 1) + 1) * LD + sp<float>(x)) + 1] = v.w;
   }
+  if (!vec)
+    for (int q = threadIdx.x; q < total; q += blockDim.x) {
+      const int x = q / W, c = q - x * W;
+      sf[2 * ((c >> 1) * LD + sp<float>(x)) + (c & 1)] = g[(size_t)x * nv + c0 + c];
+    }
   __syncthreads();
   block_fft<float, NX, false, R>(sg, t, tw);
   // theta(m) = m * (-dkx dt) v_col (kx = m dkx on the bins m <= NX/2); the angle
@@ -60,20 +72,45 @@ __device__ __forceinline__ void col_tile(float* __restrict__ g, int nv, int c0, 
   }
   __syncthreads();
   block_fft<float, NX, true, R>(sg, t, tw);
-  // density partial sums (trapz weights: 1/2 at the two v end points)
-  for (int x = threadIdx.x; x < NX; x += blockDim.x) {
+  // density partial sums (trapz weights: 1/2 at the two v end points): the
+  // tpx threads of an x point (consecutive lanes) share its W columns and
+  // add their sums by shuffles
+  const int tpx = (int)blockDim.x >= NX ? (int)blockDim.x / NX : 1;
+  if (tpx > 1 && tpx <= 32) {
+    const int x = threadIdx.x / tpx, part = threadIdx.x - x * tpx;
     float acc = 0.f;
-    for (int c = 0; c < W; ++c) {
+    for (int c = part; c < W; c += tpx) {
       const int col = c0 + c;
       const float w = (col == 0 || col == nv - 1) ? 0.5f : 1.f;
       acc = fmaf(w, sf[2 * ((c >> 1) * LD + sp<float>(x)) + (c & 1)], acc);
     }
-    dacc[x] = df_add(dacc[x], {acc, 0.f});
+    for (int m = tpx >> 1; m > 0; m >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, m);
+    if (part == 0) dacc[x] = df_add(dacc[x], {acc, 0.f});
+  } else {
+    for (int x = threadIdx.x; x < NX; x += blockDim.x) {
+      float acc = 0.f;
+      for (int c = 0; c < W; ++c) {
+        const int col = c0 + c;
+        const float w = (col == 0 || col == nv - 1) ? 0.5f : 1.f;
+        acc = fmaf(w, sf[2 * ((c >> 1) * LD + sp<float>(x)) + (c & 1)], acc);
+      }
+      dacc[x] = df_add(dacc[x], {acc, 0.f});
+    }
   }
-  for (int q = threadIdx.x; q < total; q += blockDim.x) {
-    const int x = q / W, c = q - x * W;
-    g[(size_t)x * nv + c0 + c] = sf[2 * ((c >> 1) * LD + sp<float>(x)) + (c & 1)];
+  for (int q = threadIdx.x; q < total4; q += blockDim.x) {
+    const int x = q / (W / 4), c = 4 * (q - x * (W / 4));
+    float4 v;
+    v.x = sf[2 * ((c >> 1) * LD + sp<float>(x))];
+    v.y = sf[2 * ((c >> 1) * LD + sp<float>(x)) + 1];
+    v.z = sf[2 * (((c >> 1) + 1) * LD + sp<float>(x))];
+    v.w = sf[2 * (((c >> 1) + 1) * LD + sp<float>(x)) + 1];
+    *reinterpret_cast<float4*>(g + (size_t)x * nv + c0 + c) = v;
   }
+  if (!vec)
+    for (int q = threadIdx.x; q < total; q += blockDim.x) {
+      const int x = q / W, c = q - x * W;
+      g[(size_t)x * nv + c0 + c] = sf[2 * ((c >> 1) * LD + sp<float>(x)) + (c & 1)];
+    }
   __syncthreads();
 }
 

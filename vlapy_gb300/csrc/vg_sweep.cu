@@ -40,13 +40,25 @@ constexpr int SWEEP_BLOCK = 256;
 #ifndef VG_ROW_MIN_BLOCKS
 #define VG_ROW_MIN_BLOCKS 4
 #endif
+// nv classes (bit log2 nv) whose row kernel runs radix-16 FFT passes (16
+// elements per thread, one pass fewer for nv = 256 and 1024); build-time knob
+#ifndef VG_SWEEP_R16_MASK
+#define VG_SWEEP_R16_MASK 0x500  // nv = 256 and 1024: measured 4.5 % faster row pass
+#endif
 #ifndef VG_COL_MIN_BLOCKS_SMALL
 #define VG_COL_MIN_BLOCKS_SMALL 3
+#endif
+#ifndef VG_COL_MIN_BLOCKS_32
+#define VG_COL_MIN_BLOCKS_32 VG_COL_MIN_BLOCKS_SMALL
 #endif
 constexpr int SWEEP_FIELD_BLOCK = 128;
 constexpr int SWEEP_MAX_CLASSES = 6;  // nv in {64, ..., 2048}
 
 __host__ __device__ constexpr int sweep_col_w(int nx) { return 2 * (SWEEP_BLOCK / (nx / col32_radix(nx))); }
+__host__ __device__ constexpr int sweep_row_radix(int nv) {
+  return (nv >= 64 && nv <= 4096 && ((VG_SWEEP_R16_MASK >> ilog2(nv)) & 1)) ? 16 : row32_radix(nv);
+}
+__host__ __device__ constexpr int sweep_row_min_blocks(int nv) { return sweep_row_radix(nv) == 16 ? 2 : VG_ROW_MIN_BLOCKS; }
 
 struct SweepConsts {
   RowConsts rc[SWEEP_MAX_CLASSES];
@@ -62,7 +74,7 @@ struct SweepConsts {
 // x-drift of one (run, tile) item per CTA; one kernel per nx class keeps
 // each instantiation's code and registers small
 template <int NX>
-__global__ void __launch_bounds__(SWEEP_BLOCK, (NX <= 64 ? VG_COL_MIN_BLOCKS_SMALL : 4)) k_sweep_col(const SweepRunDev* __restrict__ runs,
+__global__ void __launch_bounds__(SWEEP_BLOCK, (NX == 32 ? VG_COL_MIN_BLOCKS_32 : (NX <= 64 ? VG_COL_MIN_BLOCKS_SMALL : 4))) k_sweep_col(const SweepRunDev* __restrict__ runs,
                                                               const int2* __restrict__ items, float* g,
                                                               const SweepConsts* __restrict__ scp,
                                                               const cx<float>* __restrict__ tw, float2* dpart) {
@@ -154,10 +166,10 @@ struct SweepRowArgs {
 
 // one (run, row-pair group) item per CTA; one kernel per nv class
 template <int N>
-__global__ void __launch_bounds__(SWEEP_BLOCK, VG_ROW_MIN_BLOCKS) k_sweep_row(const SweepRunDev* __restrict__ runs,
+__global__ void __launch_bounds__(SWEEP_BLOCK, sweep_row_min_blocks(N)) k_sweep_row(const SweepRunDev* __restrict__ runs,
                                                               const int2* __restrict__ items, SweepRowArgs sa,
                                                               const SweepConsts* __restrict__ scp) {
-  constexpr int R = row32_radix(N);
+  constexpr int R = sweep_row_radix(N);
   constexpr int G = N / R;
   constexpr int P = SWEEP_BLOCK / G;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -523,7 +535,7 @@ cudaError_t sweep_col_launch(vg_sweep* s, int c, cudaStream_t st) {
 
 template <int N>
 cudaError_t sweep_row_launch(vg_sweep* s, int c, const SweepRowArgs& a, cudaStream_t st) {
-  constexpr int R = row32_radix(N);
+  constexpr int R = sweep_row_radix(N);
   const size_t smem = (size_t)(SWEEP_BLOCK / (N / R)) * row32_group_bytes(N, R);
   cudaError_t err = ensure_smem((const void*)k_sweep_row<N>, smem);
   if (err != cudaSuccess) return err;
@@ -712,7 +724,7 @@ int vg_sweep_create(const vg_sweep_desc* d, vg_sweep** out) {
   for (int i = 0; i < s->n_runs; ++i) {
     const SweepRunDev& r = s->runs_h[i];
     for (int t = 0; t < r.ntiles; ++t) col_by[r.nx].push_back(make_int2(i, t));
-    const int G = r.nv / row32_radix(r.nv);
+    const int G = r.nv / sweep_row_radix(r.nv);
     const int P = SWEEP_BLOCK / G;
     for (int pg = 0; pg * P < r.nx / 2; ++pg) row_by[r.nv].push_back(make_int2(i, pg));
     by_nx[r.nx].push_back(i);

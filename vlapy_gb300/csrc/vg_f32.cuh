@@ -100,8 +100,8 @@ __device__ __forceinline__ void block_df_sum(df32 (&v)[NQ], df32* red) {
 // divisor of 32); red holds (G/32 rounded up) * NQ entries per group.  Within
 // a warp the partial sums are added in FP32 (a thread's partial covers a few
 // terms, the tree five levels: ~5e-7 relative), across warps in double-float.
-template <int NQ>
-__device__ __forceinline__ void group_df_sum(df32 (&v)[NQ], df32* red, int G, int t) {
+template <int NQ, typename Sync = CtaSync>
+__device__ __forceinline__ void group_df_sum(df32 (&v)[NQ], df32* red, int G, int t, const Sync& sync = Sync()) {
   if (G >= 32) {
     const int lane = t & 31, wid = t >> 5, nw = G >> 5;
 #pragma unroll
@@ -115,21 +115,21 @@ __device__ __forceinline__ void group_df_sum(df32 (&v)[NQ], df32* red, int G, in
 #pragma unroll
       for (int q = 0; q < NQ; ++q) red[wid * NQ + q] = v[q];
     }
-    __syncthreads();
+    sync();
 #pragma unroll
     for (int q = 0; q < NQ; ++q) {
       df32 tt = {0.f, 0.f};
       for (int w = 0; w < nw; ++w) tt = df_add(tt, red[w * NQ + q]);
       v[q] = tt;
     }
-    __syncthreads();
+    sync();
   } else {
     // groups smaller than a warp: shuffle within the aligned sub-warp
 #pragma unroll
     for (int q = 0; q < NQ; ++q)
       for (int m = G >> 1; m > 0; m >>= 1) v[q] = df_add(v[q], df_shfl_xor(v[q], m));
-    __syncthreads();
-    __syncthreads();
+    sync();
+    sync();
   }
 }
 
@@ -139,9 +139,9 @@ __device__ __forceinline__ void group_df_sum(df32 (&v)[NQ], df32* red, int G, in
 // sequence in shared memory (element j at float offset 2*sp<float>(j)); thread
 // t of G owns the contiguous chunk [t*m, t*m+m), m = N/G >= 2.
 // red: shared scratch of 4 * 2G floats.  All threads of the CTA must call it.
-template <int M, typename LFn, typename UFn>
+template <int M, typename LFn, typename UFn, typename Sync = CtaSync>
 __device__ __forceinline__ void partition_solve(float* x, int t, int G, float b, LFn lf, UFn uf,
-                                                float* red) {
+                                                float* red, const Sync& sync = Sync()) {
   const int s = t * M, e = s + M - 1;
   float y[M > 2 ? M - 2 : 1], al[M > 2 ? M - 2 : 1], be[M > 2 ? M - 2 : 1];
   float r_s = x[2 * sp<float>(s)], r_e = x[2 * sp<float>(e)];
@@ -204,7 +204,7 @@ __device__ __forceinline__ void partition_solve(float* x, int t, int G, float b,
   B[2 * t + 1] = RB1;
   C[2 * t + 1] = RC1;
   D[2 * t + 1] = RD1;
-  __syncthreads();
+  sync();
   for (int st = 1; st < NR; st <<= 1) {
     float na[2], nb[2], nc[2], nd[2];
 #pragma unroll
@@ -230,7 +230,7 @@ __device__ __forceinline__ void partition_solve(float* x, int t, int G, float b,
       nb[q] = bi;
       nd[q] = di;
     }
-    __syncthreads();
+    sync();
 #pragma unroll
     for (int q = 0; q < 2; ++q) {
       const int i = 2 * t + q;
@@ -239,7 +239,7 @@ __device__ __forceinline__ void partition_solve(float* x, int t, int G, float b,
       C[i] = nc[q];
       D[i] = nd[q];
     }
-    __syncthreads();
+    sync();
   }
   const float xs = D[2 * t] / B[2 * t];
   const float xe = D[2 * t + 1] / B[2 * t + 1];
@@ -249,7 +249,7 @@ __device__ __forceinline__ void partition_solve(float* x, int t, int G, float b,
 #pragma unroll
     for (int i = 0; i < M - 2; ++i) x[2 * sp<float>(s + 1 + i)] = y[i] + al[i] * xs + be[i] * xe;
   }
-  __syncthreads();
+  sync();
 }
 
 }  // namespace vg

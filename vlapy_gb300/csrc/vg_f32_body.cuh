@@ -166,25 +166,26 @@ __device__ __forceinline__ void kick_rotate(cx<float>* s, int t, int G, Ang ha, 
   }
 }
 
-template <int N, int R>
+template <int N, int R, typename Sync = CtaSync>
 __device__ __forceinline__ void kick(cx<float>* s, int t, float hk, float ea, float eb,
-                                     const cx<float>* __restrict__ F0, const cx<float>* __restrict__ tw) {
+                                     const cx<float>* __restrict__ F0, const cx<float>* __restrict__ tw,
+                                     const Sync& sync = Sync()) {
   constexpr int G = N / R;
-  block_fft<float, N, false, R>(s, t, tw);
+  block_fft<float, N, false, R>(s, t, tw, sync);
   // theta(k) = -kv_k dt e = k * (-dkv dt e); hk = -dkv dt / 2 gives the half
   // angle for P - 1.  The kick angle stays O(10) rad, so an FP32 product is
   // accurate to ~1e-6 rad here
   const Ang ha = {hk * ea, 0.f};
   const Ang hb = {hk * eb, 0.f};
   kick_rotate<N>(s, t, G, ha, hb, F0);
-  __syncthreads();
-  block_fft<float, N, true, R>(s, t, tw);
+  sync();
+  block_fft<float, N, true, R>(s, t, tw, sync);
 }
 
 // Fokker-Planck step of one row stored at x (stride 2 floats) in delta-f form.
-template <int N, int R>
+template <int N, int R, typename Sync = CtaSync>
 __device__ __forceinline__ void collide_row(float* x, int t, const RowConsts& rc, float2 nudt2, float nudt_f,
-                                            int dougherty, df32* red, float* pcr) {
+                                            int dougherty, df32* red, float* pcr, const Sync& sync = Sync()) {
   constexpr int G = N / R;
   // moments of g over the thread's chunk: sum w g, sum w g v, sum w g v^2
   df32 mv[3];
@@ -204,7 +205,7 @@ __device__ __forceinline__ void collide_row(float* x, int t, const RowConsts& rc
     mv[1] = {a1, 0.f};
     mv[2] = {a2, 0.f};
   }
-  group_df_sum<3>(mv, red, G, t);
+  group_df_sum<3>(mv, red, G, t, sync);
   // per-row scalars in double-float by one thread; the group reads them back
   // as FP32 coefficients, each rounded once
   float* sc = reinterpret_cast<float*>(red);
@@ -226,30 +227,30 @@ __device__ __forceinline__ void collide_row(float* x, int t, const RowConsts& rc
     sc[3] = df_round(df_mul(nd, vth));
     sc[4] = df_round(df_mul(nd, vbar));
   }
-  __syncthreads();
+  sync();
   const float Af = sc[0], bdiag = sc[1], vb = sc[2], cs = sc[3], cd = sc[4];
   const float nu = nudt_f;
   const float cm = nu;
   const float i2dv = rc.i2dv;
-  __syncthreads();
+  sync();
   // right-hand side: g - (A - I) f0 with (A - I) f0 = nudt (-vth S + Mv - vbar D)
 #pragma unroll
   for (int i = 0; i < R; ++i) {
     const int j = t * R + i;
     x[2 * sp<float>(j)] -= -cs * rc.S[j] + cm * rc.Mv[j] - cd * rc.D[j];
   }
-  __syncthreads();
+  sync();
   auto lf = [&](int j) { return nu * (Af + (rc.v[j - 1] - vb) * i2dv); };
   auto uf = [&](int j) { return nu * (Af - (rc.v[j + 1] - vb) * i2dv); };
-  partition_solve<R>(x, t, G, bdiag, lf, uf, pcr);
+  partition_solve<R>(x, t, G, bdiag, lf, uf, pcr, sync);
 }
 
 // One row-pair group of the row pass: load, [kick dt1], [collide], [moments
 // and x-mode partials], [kick dt2], store.  grp_base: this group's shared
 // memory (row32_group_bytes); macc: the CTA's mode accumulators [n_modes][N].
-template <int N, int R>
+template <int N, int R, typename Sync = CtaSync>
 __device__ __forceinline__ void row_pair(const RowArgs& a, int pair, unsigned char* grp_base, cx<float>* macc,
-                                         int P, int grp, int t) {
+                                         int P, int grp, int t, const Sync& sync = Sync()) {
   constexpr int G = N / R;
   cx<float>* s = reinterpret_cast<cx<float>*>(grp_base);
   const size_t seq_bytes = (size_t)sp_len<float>(N) * sizeof(cx<float>) + 16;
@@ -265,14 +266,14 @@ __device__ __forceinline__ void row_pair(const RowArgs& a, int pair, unsigned ch
     const int n = t + i * G;
     s[sp<float>(n)] = {va ? ga[n] : 0.f, vb ? gbp[n] : 0.f};
   }
-  __syncthreads();
+  sync();
   const bool kicks = a.hk1 != 0.f || a.hk2 != 0.f;
   const float ea = (kicks && va) ? a.e32[ra] : 0.f, eb = (kicks && vb) ? a.e32[rb] : 0.f;
-  if (a.hk1 != 0.f) kick<N, R>(s, t, a.hk1, ea, eb, a.F0, a.tw);
+  if (a.hk1 != 0.f) kick<N, R>(s, t, a.hk1, ea, eb, a.F0, a.tw, sync);
   float* sx = reinterpret_cast<float*>(s);
   if (a.fp) {
-    collide_row<N, R>(sx, t, *a.rc, a.nudt2, a.nudt_f, a.dougherty, red, pcr);
-    collide_row<N, R>(sx + 1, t, *a.rc, a.nudt2, a.nudt_f, a.dougherty, red, pcr);
+    collide_row<N, R>(sx, t, *a.rc, a.nudt2, a.nudt_f, a.dougherty, red, pcr, sync);
+    collide_row<N, R>(sx + 1, t, *a.rc, a.nudt2, a.nudt_f, a.dougherty, red, pcr, sync);
   }
   if (a.want_mom) {
     // n, j, T, q, fv4, vN (sums of w g v^p), sum w g^2, sum w g f0, sum w f log f
@@ -305,8 +306,8 @@ __device__ __forceinline__ void row_pair(const RowArgs& a, int pair, unsigned ch
       mv[q] = {sa[q], 0.f};
       mw[q] = {sb[q], 0.f};
     }
-    group_df_sum<9>(mv, red, G, t);
-    group_df_sum<9>(mw, red, G, t);
+    group_df_sum<9>(mv, red, G, t, sync);
+    group_df_sum<9>(mw, red, G, t, sync);
     if (t == 0) {
       // raw sums; the storage kernels form dv * sum + trapz(f0 ...) in FP64.
       // Each array is indexed by constants only, so it stays in registers.
@@ -323,7 +324,8 @@ __device__ __forceinline__ void row_pair(const RowArgs& a, int pair, unsigned ch
     // x-Fourier modes of f (the f0 part of mode 0 is added in the reduction);
     // the groups of a CTA hold different rows but add into the same bins,
     // so they take turns
-    if (nm > 0) {
+    // (only with a CTA-wide sync: the turns are CTA barriers)
+    if (Sync::cta_wide && nm > 0) {
       for (int gq = 0; gq < P; ++gq) {
         if (gq == grp) {
           for (int mq = 0; mq < nm; ++mq) {
@@ -343,7 +345,7 @@ __device__ __forceinline__ void row_pair(const RowArgs& a, int pair, unsigned ch
       }
     }
   }
-  if (a.hk2 != 0.f) kick<N, R>(s, t, a.hk2, ea, eb, a.F0, a.tw);
+  if (a.hk2 != 0.f) kick<N, R>(s, t, a.hk2, ea, eb, a.F0, a.tw, sync);
 #pragma unroll
   for (int i = 0; i < R; ++i) {
     const int n = t + i * G;
@@ -351,7 +353,7 @@ __device__ __forceinline__ void row_pair(const RowArgs& a, int pair, unsigned ch
     if (va) ga[n] = z.x;
     if (vb) gbp[n] = z.y;
   }
-  __syncthreads();
+  sync();
 }
 
 

@@ -11,11 +11,40 @@
 //
 // Twiddles come from one table tw[q] = exp(-2 pi i q / FFT_NMAX) built once
 // per plan (sincospi in FP64), indexed with stride FFT_NMAX / (Ns r).
+//
+// The passes synchronise through a policy object: CtaSync (__syncthreads,
+// every thread of the CTA calls the transform) or GroupSync (only the
+// threads that share the sequence: a named barrier for groups of whole
+// warps, __syncwarp for a group inside one warp), which lets the sequences of
+// a CTA run their passes independently.
 #pragma once
 
 #include "vg_common.cuh"
 
 namespace vg {
+
+struct CtaSync {
+  static constexpr bool cta_wide = true;
+  __device__ __forceinline__ void operator()() const { __syncthreads(); }
+};
+struct GroupSync {
+  static constexpr bool cta_wide = false;
+  unsigned id;     // named barrier (1..15) of a group of count > 32 threads
+  unsigned count;  // threads in the group: a multiple of 32, or a divisor of 32
+  unsigned mask;   // the group's lanes when count <= 32
+  __device__ __forceinline__ void operator()() const {
+    if (count > 32) asm volatile("bar.sync %0, %1;\n" ::"r"(id), "r"(count) : "memory");
+    else __syncwarp(mask);
+  }
+  // the sync of group grp of g threads, groups laid out back to back
+  static __device__ __forceinline__ GroupSync of(int grp, int g) {
+    GroupSync s;
+    s.id = 1u + (unsigned)grp;
+    s.count = (unsigned)g;
+    s.mask = g >= 32 ? 0xffffffffu : (((1u << g) - 1u) << ((grp * g) & 31));
+    return s;
+  }
+};
 
 constexpr int FFT_LOG_NMAX = 14;
 constexpr int FFT_NMAX = 1 << FFT_LOG_NMAX;
@@ -104,7 +133,8 @@ __device__ __forceinline__ cx<T> twiddle(const cx<T>* __restrict__ tw, int q, bo
 
 template <typename T, int N, int R, bool INV, int NS>
 struct StockhamPass {
-  static __device__ __forceinline__ void run(cx<T>* s, int t, const cx<T>* __restrict__ tw) {
+  template <typename Sync>
+  static __device__ __forceinline__ void run(cx<T>* s, int t, const cx<T>* __restrict__ tw, const Sync& sync) {
     constexpr int r = (N / NS < R) ? (N / NS) : R;
     constexpr int NB = N / r;      // butterflies in this pass
     constexpr int G = N / R;       // threads per sequence
@@ -131,7 +161,7 @@ struct StockhamPass {
       }
       Dft<T, r, INV>::run(a[b]);
     }
-    __syncthreads();
+    sync();
 #pragma unroll
     for (int b = 0; b < BPT; ++b) {
       const int j = t + b * G;
@@ -140,21 +170,22 @@ struct StockhamPass {
 #pragma unroll
       for (int m = 0; m < r; ++m) s[sp<T>(base + m * NS)] = a[b][m];
     }
-    __syncthreads();
-    StockhamPass<T, N, R, INV, NS * r>::run(s, t, tw);
+    sync();
+    StockhamPass<T, N, R, INV, NS * r>::run(s, t, tw, sync);
   }
 };
 template <typename T, int N, int R, bool INV>
 struct StockhamPass<T, N, R, INV, N> {
-  static __device__ __forceinline__ void run(cx<T>*, int, const cx<T>* __restrict__) {}
+  template <typename Sync>
+  static __device__ __forceinline__ void run(cx<T>*, int, const cx<T>* __restrict__, const Sync&) {}
 };
 
 // In-place unnormalised transform of s[0..N) by the N/R threads t = 0..N/R-1
 // (R defaults to fft_radix<T>(N)).  Caller must have synchronised after
-// writing s; the result is visible to the whole CTA on return.
-template <typename T, int N, bool INV, int R = fft_radix<T>(N)>
-__device__ __forceinline__ void block_fft(cx<T>* s, int t, const cx<T>* __restrict__ tw) {
-  StockhamPass<T, N, (R < N ? R : N), INV, 1>::run(s, t, tw);
+// writing s; the result is visible to the synchronised threads on return.
+template <typename T, int N, bool INV, int R = fft_radix<T>(N), typename Sync = CtaSync>
+__device__ __forceinline__ void block_fft(cx<T>* s, int t, const cx<T>* __restrict__ tw, const Sync& sync = Sync()) {
+  StockhamPass<T, N, (R < N ? R : N), INV, 1>::run(s, t, tw, sync);
 }
 
 // Two real sequences a, b packed as z = a + i b; s holds Z = FFT(z).  Replace

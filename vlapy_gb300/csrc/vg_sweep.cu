@@ -195,7 +195,9 @@ __global__ void __launch_bounds__(SWEEP_BLOCK, sweep_row_min_blocks(N)) k_sweep_
   a.F0 = scp->F0[r.cls];
   a.tw = sa.tw;
   a.rc = &scp->rc[r.cls];
-  row_pair<N, R>(a, it.y * P + grp, smem_raw + (size_t)grp * row32_group_bytes(N, R), nullptr, P, grp, t);
+  // the row-pair groups of a CTA are independent: each synchronises alone
+  row_pair<N, R>(a, it.y * P + grp, smem_raw + (size_t)grp * row32_group_bytes(N, R), nullptr, P, grp, t,
+                 GroupSync::of(grp, G));
 }
 
 // e history row and the seven series of every run (one CTA per run)

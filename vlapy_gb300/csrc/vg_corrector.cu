@@ -481,15 +481,21 @@ __global__ void k_loss(const float* __restrict__ pred, const float* __restrict__
 // never touched, and the corrected high part is never longer in L2 norm
 // than the coarse step left it, so repeated corrections cannot feed energy
 // into a run.  blockDim = CP, one row per CTA.
-constexpr int APPLY_ROWS = 8;  // rows per CTA of k_apply: each basis value loaded once serves 8 rows
+constexpr int APPLY_ROWS = 8;  // rows per CTA of k_apply: 4 packed pairs of d and 4 of c
 
+// The projection P off the protected modes |m| < M of the 128-point rows, by
+// FFT: two real rows packed as one complex sequence z = a + i b, FFT, the
+// bins k < M and k > 128 - M set to zero (which removes those modes from a
+// and b alike), inverse FFT / 128.  Each of a CTA's 8 sequences (4 pairs of
+// deviations d, 4 pairs of corrections c) is transformed by its own 16
+// threads.  Then the cap: m + P'd + (Pd + c') * min(1, |Pd| / |Pd + c'|),
+// c' = P c, per row.
 __global__ void __launch_bounds__(CP) k_apply(const float* __restrict__ g, const float2* __restrict__ gmean,
                                                int group_rows, const float* __restrict__ pred,
-                                               const float* __restrict__ scale, float tau,
-                                               const float* __restrict__ basis, const float* __restrict__ basis_t,
-                                               int nq, int rows, float* __restrict__ out) {
-  __shared__ float sh[2][APPLY_ROWS][CP];    // d and c of each row
-  __shared__ float coef[2][APPLY_ROWS][CP];  // their coefficients on the protected modes
+                                               const float* __restrict__ scale, float tau, int protect_modes,
+                                               const cx<float>* __restrict__ tw, int rows, float* __restrict__ out) {
+  constexpr int SL = sp_len<float>(CP) + 1;  // padded length of one sequence
+  __shared__ cx<float> seq[2 * (APPLY_ROWS / 2)][SL];
   __shared__ float wsum[2][APPLY_ROWS][CP / 32];
   const int p = threadIdx.x, row0 = blockIdx.x * APPLY_ROWS;
   float d[APPLY_ROWS], c[APPLY_ROWS];
@@ -499,50 +505,48 @@ __global__ void __launch_bounds__(CP) k_apply(const float* __restrict__ g, const
     const size_t q = (size_t)row * CP + p;
     d[r] = deviation(g[q], gmean, group_rows, row, p);
     c[r] = (scale[row] * tau) * pred[q];
-    sh[0][r][p] = d[r];
-    sh[1][r][p] = c[r];
   }
-  __syncthreads();
-  if (p < nq) {
-    float ad[APPLY_ROWS], ac[APPLY_ROWS];
+  float dh[APPLY_ROWS], ch[APPLY_ROWS];
+  if (protect_modes > 0) {
 #pragma unroll
-    for (int r = 0; r < APPLY_ROWS; ++r) ad[r] = ac[r] = 0.f;
-#pragma unroll 4
-    for (int j = 0; j < CP; ++j) {
-      const float w = basis_t[j * CP + p];
-#pragma unroll
-      for (int r = 0; r < APPLY_ROWS; ++r) {
-        ad[r] = fmaf(sh[0][r][j], w, ad[r]);
-        ac[r] = fmaf(sh[1][r][j], w, ac[r]);
-      }
+    for (int h = 0; h < APPLY_ROWS / 2; ++h) {
+      seq[h][sp<float>(p)] = {d[2 * h], d[2 * h + 1]};
+      seq[APPLY_ROWS / 2 + h][sp<float>(p)] = {c[2 * h], c[2 * h + 1]};
     }
+    __syncthreads();
+    {
+      constexpr int GT = CP / 8;  // 16 threads per radix-8 sequence of 128
+      const int sq = p / GT, t = p - sq * GT;
+      const GroupSync gs = GroupSync::of(sq, GT);
+      cx<float>* z = seq[sq];
+      block_fft<float, CP, false, 8>(z, t, tw, gs);
+      for (int k = t; k < CP; k += GT)
+        if (k < protect_modes || k > CP - protect_modes) z[sp<float>(k)] = {0.f, 0.f};
+      gs();
+      block_fft<float, CP, true, 8>(z, t, tw, gs);
+    }
+    __syncthreads();
+    const float inv = 1.f / CP;
+#pragma unroll
+    for (int h = 0; h < APPLY_ROWS / 2; ++h) {
+      const cx<float> zd = seq[h][sp<float>(p)], zc = seq[APPLY_ROWS / 2 + h][sp<float>(p)];
+      dh[2 * h] = zd.x * inv;
+      dh[2 * h + 1] = zd.y * inv;
+      ch[2 * h] = zc.x * inv;
+      ch[2 * h + 1] = zc.y * inv;
+    }
+  } else {
 #pragma unroll
     for (int r = 0; r < APPLY_ROWS; ++r) {
-      coef[0][r][p] = ad[r];
-      coef[1][r][p] = ac[r];
-    }
-  }
-  __syncthreads();
-  // the high parts Pd and Pc (projection off the protected modes)
-  float dh[APPLY_ROWS], hn[APPLY_ROWS];
-#pragma unroll
-  for (int r = 0; r < APPLY_ROWS; ++r) {
-    dh[r] = d[r];
-    hn[r] = c[r];
-  }
-#pragma unroll 4
-  for (int qq = 0; qq < nq; ++qq) {
-    const float w = basis[qq * CP + p];
-#pragma unroll
-    for (int r = 0; r < APPLY_ROWS; ++r) {
-      dh[r] = fmaf(-coef[0][r][qq], w, dh[r]);
-      hn[r] = fmaf(-coef[1][r][qq], w, hn[r]);
+      dh[r] = d[r];
+      ch[r] = c[r];
     }
   }
   // hn = Pd + Pc; row sums of (Pd)^2 and hn^2 by warp shuffles, then the warps
+  float hn[APPLY_ROWS];
 #pragma unroll
   for (int r = 0; r < APPLY_ROWS; ++r) {
-    hn[r] += dh[r];
+    hn[r] = dh[r] + ch[r];
     float so = dh[r] * dh[r], sn = hn[r] * hn[r];
 #pragma unroll
     for (int m = 16; m > 0; m >>= 1) {
@@ -995,6 +999,8 @@ struct vg_corrector {
   int engine;               // 0: fused tcgen05 forward, 1: per-layer mma.sync kernels
   int n_sm;
   __nv_bfloat16* wtc;       // the fused kernel's weight image [TC_W_BYTES / 2]
+  cx<double>* tw64;         // FFT twiddles of the projection
+  cx<float>* tw32;
   int* err;                 // device error word of the fused kernel
   int protect_modes;      // M: the modes |m| < M are never corrected
   int nq;                 // 2M - 1 basis functions (0 when M = 0)
@@ -1202,6 +1208,15 @@ int vg_corr_create(int32_t max_rows, int32_t protect_modes, float vmax, float ta
   CR_TRY(cr_alloc(c, &c->tmean, pos, "corrector group means"));
   CR_TRY(cr_alloc(c, &c->pmean, pos, "corrector group means"));
   CR_TRY(cr_alloc(c, &c->wtc, (size_t)TC_W_BYTES / 2, "corrector weights"));
+  CR_TRY(cr_alloc(c, &c->tw64, (size_t)FFT_NMAX, "corrector twiddles"));
+  CR_TRY(cr_alloc(c, &c->tw32, (size_t)FFT_NMAX, "corrector twiddles"));
+  {
+    vg_plan tmp;
+    std::memset(&tmp, 0, sizeof(tmp));
+    tmp.tw64 = c->tw64;
+    tmp.tw32 = c->tw32;
+    CR_TRY(cuda_status(launch_twiddles(tmp, 0), "corrector twiddles"));
+  }
   CR_TRY(cr_alloc(c, &c->err, 1, "corrector status"));
   {
     int dev = 0;
@@ -1307,7 +1322,7 @@ int vg_corr_apply(vg_corrector* c, const vg_corr_batch* b, float* g_out, vg_stre
     CR_CHECK(forward(c, *b, s));
   }
   k_apply<<<div_up(b->rows, APPLY_ROWS), CP, 0, s>>>(b->g, c->gmean, b->group_rows, c->pred, c->scale, c->tau,
-                                                     c->basis, c->basis_t, c->nq, b->rows, g_out);
+                                                     c->protect_modes, c->tw32, b->rows, g_out);
   return cuda_status(cudaGetLastError(), "corrector apply");
 }
 

@@ -198,3 +198,19 @@ def test_sweep_damping_on_device_matches_host_fit():
                 np.testing.assert_allclose(freq[i], fh, rtol=1e-9)
     with pytest.raises(ValueError):
         sw.damping(eh[:, :5].contiguous())
+
+
+@pytest.mark.parametrize("nx,nv", [(8, 512), (256, 64), (16, 2048), (256, 256), (128, 2048)])
+def test_sweep_extreme_shapes_match_oracle(nx, nv):
+    """The smallest and largest supported nx and nv of a sweep class (nx in
+    [8, 256], nv in [64, 2048], nv >= 4096 / nx), alone and beside another class."""
+    from vlapy_gb300.sweep import Sweep
+    runs = [dict(nx=nx, nv=nv, k=0.35, amplitude=1e-3, nu=1e-3), dict(nx=32, nv=256, k=0.3, amplitude=1e-2, nu=0.0)]
+    sw = Sweep(runs)
+    sw.reset()
+    sw.run_steps(5)
+    torch.cuda.synchronize()
+    for i, r in enumerate(runs):
+        f_ref, _, f0 = oracle_run(r, 5)
+        f = sw.read_run(i)[0].cpu().numpy()
+        assert np.linalg.norm(f - f_ref) / np.linalg.norm(f_ref - f0[None, :]) <= 1e-4, (nx, nv, i)

@@ -375,3 +375,58 @@ def run_corrected(sweep, corr, nsteps, e_hist=None, series_hist=None, row0=0, st
         corr.apply(g, prev, feat, out=g, group_rows=nx, stream=stream)
     corr.check_status()
     return sweep
+
+
+def fine_reference(runs, nsteps=2000, vmax=6.4, dt=0.1):
+    """Field-energy history [nsteps][runs] of the fine (nv = 1024) runs."""
+    fine = Sweep([dict(r, nv=1024) for r in runs], vmax=vmax, dt=dt)
+    fine.reset()
+    eh, sh = fine.history(nsteps)
+    fine.run_steps(nsteps, eh, sh)
+    e2 = sh[:, :, 3].clone()
+    fine.close()
+    return e2
+
+
+def rollout_error(corr, runs, e2_fine, vmax=6.4, dt=0.1):
+    """Per-run relative L2 error of the corrected coarse runs' field-energy
+    history against the fine runs' (float64 CPU tensor [runs])."""
+    nsteps = e2_fine.shape[0]
+    sw = Sweep([dict(r, nv=NV) for r in runs], vmax=vmax, dt=dt)
+    sw.reset()
+    eh, sh = sw.history(nsteps)
+    run_corrected(sw, corr, nsteps, eh, sh)
+    e2 = sh[:, :, 3]
+    err = torch.linalg.norm(e2 - e2_fine, dim=0) / torch.linalg.norm(e2_fine, dim=0)
+    sw.close()
+    return err.cpu()
+
+
+def train_selected(data, val_runs, seeds=(0, 1, 2), epochs=4, batch_runs=128, lr=1e-3, max_rows=None,
+                   protect_modes=PROTECT_MODES, log=None):
+    """Train one network per seed (initialisation and shuffling) and keep the
+    one whose corrected coarse runs follow the fine runs best on validation
+    runs (the mean field-energy-history error over 2000 steps).  Training one
+    step at a time leaves the rollout quality of a network to chance; the
+    validation runs are drawn apart from both the training and any held-out
+    runs.  Returns (corrector, report)."""
+    tau = output_scale(data, protect_modes=protect_modes)
+    e2_fine = fine_reference(val_runs)
+    rows = max(batch_runs * data.nx, len(val_runs) * data.nx, max_rows or 0)
+    best, report = None, []
+    for seed in seeds:
+        corr = Corrector(rows, tau=tau, seed=seed, protect_modes=protect_modes)
+        hist = train(corr, data, epochs=epochs, batch_runs=batch_runs, lr=lr, seed=seed)
+        err = rollout_error(corr, val_runs, e2_fine)
+        score = float(err.mean())
+        report.append({"seed": seed, "train_loss": hist[-1], "val_field_energy_err_mean": score,
+                       "val_within_1pct": float((err <= 0.01).double().mean())})
+        if log:
+            log(f"seed {seed}: validation field-energy error {score:.3e}")
+        if best is None or score < best[0]:
+            if best is not None:
+                best[1].close()
+            best = (score, corr)
+        else:
+            corr.close()
+    return best[1], report

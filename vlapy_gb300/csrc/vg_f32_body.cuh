@@ -166,12 +166,14 @@ __device__ __forceinline__ void kick_rotate(cx<float>* s, int t, int G, Ang ha, 
   }
 }
 
-template <int N, int R, typename Sync = CtaSync>
-__device__ __forceinline__ void kick(cx<float>* s, int t, float hk, float ea, float eb,
-                                     const cx<float>* __restrict__ F0, const cx<float>* __restrict__ tw,
-                                     const Sync& sync = Sync()) {
+// the kick with the row pair in registers at one end (IO = 1: io holds the
+// pair's elements t + i G on entry and s need not; IO = 2: they end in io)
+template <int N, int R, int IO, typename Sync>
+__device__ __forceinline__ void kick_io(cx<float>* s, int t, float hk, float ea, float eb,
+                                        const cx<float>* __restrict__ F0, const cx<float>* __restrict__ tw,
+                                        const Sync& sync, cx<float> (&io)[R]) {
   constexpr int G = N / R;
-  block_fft<float, N, false, R>(s, t, tw, sync);
+  block_fft_io<float, N, false, R, IO & 1>(s, t, tw, sync, io);
   // theta(k) = -kv_k dt e = k * (-dkv dt e); hk = -dkv dt / 2 gives the half
   // angle for P - 1.  The kick angle stays O(10) rad, so an FP32 product is
   // accurate to ~1e-6 rad here
@@ -179,7 +181,15 @@ __device__ __forceinline__ void kick(cx<float>* s, int t, float hk, float ea, fl
   const Ang hb = {hk * eb, 0.f};
   kick_rotate<N>(s, t, G, ha, hb, F0);
   sync();
-  block_fft<float, N, true, R>(s, t, tw, sync);
+  block_fft_io<float, N, true, R, IO & 2>(s, t, tw, sync, io);
+}
+
+template <int N, int R, typename Sync = CtaSync>
+__device__ __forceinline__ void kick(cx<float>* s, int t, float hk, float ea, float eb,
+                                     const cx<float>* __restrict__ F0, const cx<float>* __restrict__ tw,
+                                     const Sync& sync = Sync()) {
+  cx<float> none[R];
+  kick_io<N, R, 0>(s, t, hk, ea, eb, F0, tw, sync, none);
 }
 
 // Fokker-Planck step of one row stored at x (stride 2 floats) in delta-f form.
@@ -261,15 +271,23 @@ __device__ __forceinline__ void row_pair(const RowArgs& a, int pair, unsigned ch
   const bool va = ra < a.nx, vb = rb < a.nx;
   float* ga = a.g + (size_t)ra * N;
   float* gbp = a.g + (size_t)rb * N;
+  // the pair's elements t + i G: exactly what the first FFT pass of the kick
+  // reads, so they go from global memory straight into that pass
+  cx<float> io[R];
 #pragma unroll
   for (int i = 0; i < R; ++i) {
     const int n = t + i * G;
-    s[sp<float>(n)] = {va ? ga[n] : 0.f, vb ? gbp[n] : 0.f};
+    io[i] = {va ? ga[n] : 0.f, vb ? gbp[n] : 0.f};
   }
-  sync();
   const bool kicks = a.hk1 != 0.f || a.hk2 != 0.f;
   const float ea = (kicks && va) ? a.e32[ra] : 0.f, eb = (kicks && vb) ? a.e32[rb] : 0.f;
-  if (a.hk1 != 0.f) kick<N, R>(s, t, a.hk1, ea, eb, a.F0, a.tw, sync);
+  if (a.hk1 != 0.f) {
+    kick_io<N, R, 1>(s, t, a.hk1, ea, eb, a.F0, a.tw, sync, io);
+  } else {
+#pragma unroll
+    for (int i = 0; i < R; ++i) s[sp<float>(t + i * G)] = io[i];
+    sync();
+  }
   float* sx = reinterpret_cast<float*>(s);
   if (a.fp) {
     collide_row<N, R>(sx, t, *a.rc, a.nudt2, a.nudt_f, a.dougherty, red, pcr, sync);
@@ -345,13 +363,19 @@ __device__ __forceinline__ void row_pair(const RowArgs& a, int pair, unsigned ch
       }
     }
   }
-  if (a.hk2 != 0.f) kick<N, R>(s, t, a.hk2, ea, eb, a.F0, a.tw, sync);
+  // the last FFT pass of the kick leaves elements t + i G in registers: the
+  // store pattern, so they go straight back to global memory
+  if (a.hk2 != 0.f) {
+    kick_io<N, R, 2>(s, t, a.hk2, ea, eb, a.F0, a.tw, sync, io);
+  } else {
+#pragma unroll
+    for (int i = 0; i < R; ++i) io[i] = s[sp<float>(t + i * G)];
+  }
 #pragma unroll
   for (int i = 0; i < R; ++i) {
     const int n = t + i * G;
-    const cx<float> z = s[sp<float>(n)];
-    if (va) ga[n] = z.x;
-    if (vb) gbp[n] = z.y;
+    if (va) ga[n] = io[i].x;
+    if (vb) gbp[n] = io[i].y;
   }
   sync();
 }

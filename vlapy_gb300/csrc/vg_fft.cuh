@@ -131,22 +131,34 @@ __device__ __forceinline__ cx<T> twiddle(const cx<T>* __restrict__ tw, int q, bo
   return w;
 }
 
-template <typename T, int N, int R, bool INV, int NS>
+// One Stockham pass and the ones after it.  IO bit 0: the first pass takes
+// its inputs from the caller's registers io (thread t's elements t + i N/R,
+// exactly what that pass reads) instead of shared memory; bit 1: the last
+// pass leaves its outputs in io (again elements t + i N/R) instead of
+// writing them back.  Either saves one round trip through shared memory.
+template <typename T, int N, int R, bool INV, int NS, int IO = 0>
 struct StockhamPass {
   template <typename Sync>
-  static __device__ __forceinline__ void run(cx<T>* s, int t, const cx<T>* __restrict__ tw, const Sync& sync) {
+  static __device__ __forceinline__ void run(cx<T>* s, int t, const cx<T>* __restrict__ tw, const Sync& sync,
+                                             cx<T> (&io)[R]) {
     constexpr int r = (N / NS < R) ? (N / NS) : R;
     constexpr int NB = N / r;      // butterflies in this pass
     constexpr int G = N / R;       // threads per sequence
     constexpr int BPT = NB / G;    // butterflies per thread
     constexpr int TWS = FFT_NMAX / (NS * r);
+    constexpr bool from_regs = (IO & 1) && NS == 1;
+    constexpr bool to_regs = (IO & 2) && NS * r == N;
+    static_assert(!from_regs || (BPT == 1 && r == R), "the first pass reads one radix-R butterfly per thread");
     cx<T> a[BPT][r];
 #pragma unroll
     for (int b = 0; b < BPT; ++b) {
       const int j = t + b * G;
       const int k = j & (NS - 1);
 #pragma unroll
-      for (int m = 0; m < r; ++m) a[b][m] = s[sp<T>(j + m * NB)];
+      for (int m = 0; m < r; ++m) {
+        if constexpr (from_regs) a[b][m] = io[m];
+        else a[b][m] = s[sp<T>(j + m * NB)];
+      }
       if (NS > 1) {
         // twiddles w^m: the power-of-two m from the table, the others as
         // products of those (one extra rounding), halving the table loads
@@ -161,23 +173,31 @@ struct StockhamPass {
       }
       Dft<T, r, INV>::run(a[b]);
     }
-    sync();
+    if constexpr (to_regs) {
+      // outputs base + m NS with base = j = t + b G, i.e. elements t + G (b + m BPT)
 #pragma unroll
-    for (int b = 0; b < BPT; ++b) {
-      const int j = t + b * G;
-      const int k = j & (NS - 1);
-      const int base = (j - k) * r + k;
+      for (int b = 0; b < BPT; ++b)
 #pragma unroll
-      for (int m = 0; m < r; ++m) s[sp<T>(base + m * NS)] = a[b][m];
+        for (int m = 0; m < r; ++m) io[b + m * BPT] = a[b][m];
+    } else {
+      sync();
+#pragma unroll
+      for (int b = 0; b < BPT; ++b) {
+        const int j = t + b * G;
+        const int k = j & (NS - 1);
+        const int base = (j - k) * r + k;
+#pragma unroll
+        for (int m = 0; m < r; ++m) s[sp<T>(base + m * NS)] = a[b][m];
+      }
+      sync();
+      StockhamPass<T, N, R, INV, NS * r, IO>::run(s, t, tw, sync, io);
     }
-    sync();
-    StockhamPass<T, N, R, INV, NS * r>::run(s, t, tw, sync);
   }
 };
-template <typename T, int N, int R, bool INV>
-struct StockhamPass<T, N, R, INV, N> {
+template <typename T, int N, int R, bool INV, int IO>
+struct StockhamPass<T, N, R, INV, N, IO> {
   template <typename Sync>
-  static __device__ __forceinline__ void run(cx<T>*, int, const cx<T>* __restrict__, const Sync&) {}
+  static __device__ __forceinline__ void run(cx<T>*, int, const cx<T>* __restrict__, const Sync&, cx<T> (&)[R]) {}
 };
 
 // In-place unnormalised transform of s[0..N) by the N/R threads t = 0..N/R-1
@@ -185,7 +205,18 @@ struct StockhamPass<T, N, R, INV, N> {
 // writing s; the result is visible to the synchronised threads on return.
 template <typename T, int N, bool INV, int R = fft_radix<T>(N), typename Sync = CtaSync>
 __device__ __forceinline__ void block_fft(cx<T>* s, int t, const cx<T>* __restrict__ tw, const Sync& sync = Sync()) {
-  StockhamPass<T, N, (R < N ? R : N), INV, 1>::run(s, t, tw, sync);
+  constexpr int RR = R < N ? R : N;
+  cx<T> unused[RR];
+  StockhamPass<T, N, RR, INV, 1, 0>::run(s, t, tw, sync, unused);
+}
+// The same with register input (IO = 1: io holds elements t + i N/R, s need
+// not hold the sequence) or register output (IO = 2: the result's elements
+// t + i N/R end in io and s is left as scratch).
+template <typename T, int N, bool INV, int R, int IO, typename Sync>
+__device__ __forceinline__ void block_fft_io(cx<T>* s, int t, const cx<T>* __restrict__ tw, const Sync& sync,
+                                             cx<T> (&io)[R]) {
+  static_assert(R <= N, "radix larger than the sequence");
+  StockhamPass<T, N, R, INV, 1, IO>::run(s, t, tw, sync, io);
 }
 
 // Two real sequences a, b packed as z = a + i b; s holds Z = FFT(z).  Replace

@@ -32,9 +32,9 @@ def mixed_runs():
     return runs
 
 
-def oracle_run(r, nsteps, vmax=6.4, dt=0.1):
+def oracle_run(r, nsteps, vmax=6.4, dt=0.1, operator="dg"):
     nx, nv, k = r["nx"], r["nv"], r["k"]
-    run = vo.OracleRun(nx, nv, 2 * np.pi / k, vmax, dt, nu=r["nu"], operator="dg")
+    run = vo.OracleRun(nx, nv, 2 * np.pi / k, vmax, dt, nu=r["nu"], operator=operator)
     dx, x, kx, inv = vo.spatial_axis(0.0, 2 * np.pi / k, nx)
     f = vo.maxwellian(nx, nv, vmax) * (1.0 + r["amplitude"] * np.cos(k * x))[:, None]
     f0 = vo.maxwellian(1, nv, vmax)[0]
@@ -214,3 +214,17 @@ def test_sweep_extreme_shapes_match_oracle(nx, nv):
         f_ref, _, f0 = oracle_run(r, 5)
         f = sw.read_run(i)[0].cpu().numpy()
         assert np.linalg.norm(f - f_ref) / np.linalg.norm(f_ref - f0[None, :]) <= 1e-4, (nx, nv, i)
+
+
+def test_sweep_lenard_bernstein_matches_oracle():
+    """The sweep with the Lenard-Bernstein operator (vlapy/core/collisions.py:26-83)."""
+    from vlapy_gb300.sweep import Sweep
+    runs = [dict(nx=32, nv=512, k=0.3, amplitude=1e-3, nu=5e-3), dict(nx=64, nv=256, k=0.4, amplitude=1e-2, nu=1e-2)]
+    sw = Sweep(runs, collision="lb")
+    sw.reset()
+    sw.run_steps(10)
+    torch.cuda.synchronize()
+    for i, r in enumerate(runs):
+        f_ref, _, f0 = oracle_run(r, 10, operator="lb")
+        f = sw.read_run(i)[0].cpu().numpy()
+        assert np.linalg.norm(f - f_ref) / np.linalg.norm(f_ref - f0[None, :]) <= 1e-4, (i, r)

@@ -731,13 +731,19 @@ template <int CIN, int NOUT>
 __device__ __forceinline__ void tc_layer_issue(uint32_t tmem, uint32_t act, uint32_t w) {
   constexpr uint32_t idesc = tc_idesc(128, NOUT);
   constexpr int WTAP = NOUT * CIN * 2;
+  // the descriptors of tap t, K-step kc are the tile's and the weights' base
+  // descriptors with the start address moved by a compile-time offset (the
+  // 14-bit address field holds any shared-memory address, so adding the
+  // offset in 16-byte units cannot carry out of it)
+  const uint64_t a0 = tc_desc(act, TC_LBO_ACT, 128);
+  const uint64_t b0 = tc_desc(w, 16 * NOUT, 128);
   int first = 1;
 #pragma unroll
   for (int t = 0; t < 5; ++t) {
 #pragma unroll
     for (int kc = 0; kc < CIN / 16; ++kc) {
-      const uint64_t a = tc_desc(act + 16 * t + 2 * kc * TC_LBO_ACT, TC_LBO_ACT, 128);
-      const uint64_t b = tc_desc(w + t * WTAP + 2 * kc * (16 * NOUT), 16 * NOUT, 128);
+      const uint64_t a = a0 + (uint64_t)((16 * t + 2 * kc * TC_LBO_ACT) >> 4);
+      const uint64_t b = b0 + (uint64_t)((t * WTAP + 2 * kc * (16 * NOUT)) >> 4);
       tc_mma(tmem, a, b, idesc, first ? 0 : 1);
       first = 0;
     }

@@ -263,7 +263,9 @@ __device__ __forceinline__ void row_pair(const RowArgs& a, int pair, unsigned ch
                                          int P, int grp, int t, const Sync& sync = Sync()) {
   constexpr int G = N / R;
   cx<float>* s = reinterpret_cast<cx<float>*>(grp_base);
-  const size_t seq_bytes = (size_t)sp_len<float>(N) * sizeof(cx<float>) + 16;
+  constexpr size_t seq_bytes = (size_t)sp_len<float>(N) * sizeof(cx<float>) + 16;
+  static_assert(seq_bytes + 8 * G * sizeof(float) + (G / 32 + 1) * 9 * sizeof(df32) == row32_group_bytes(N, R),
+                "row-pair group layout and its host-side size disagree");
   float* pcr = reinterpret_cast<float*>(grp_base + seq_bytes);
   df32* red = reinterpret_cast<df32*>(grp_base + seq_bytes + 8 * G * sizeof(float));
   const int nm = a.n_modes;

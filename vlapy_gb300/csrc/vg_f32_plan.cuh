@@ -2,6 +2,7 @@
 #pragma once
 
 #include "vg_common.cuh"
+#include "vg_fft.cuh"
 
 namespace vg {
 
@@ -75,10 +76,10 @@ __host__ __device__ constexpr int col32_seqs(int nx, int r) {
 }
 __host__ __device__ constexpr int row32_radix(int n) { return n <= 8 ? n : (n <= 4096 ? 8 : 16); }
 __host__ __device__ constexpr int row32_block(int n, int r) { return (n / r) >= 256 ? (n / r) : 256; }
-// per row-pair group: padded sequence (one pad per 16 complex floats), PCR
-// scratch of 4 x 2G floats, double-float reduction slots
+// per row-pair group: padded sequence (sp_len<float>, the layout the row
+// kernels index), PCR scratch of 4 x 2G floats, double-float reduction slots
 __host__ __device__ constexpr size_t row32_group_bytes(int n, int r) {
-  return (size_t)(n + (n >> 4)) * 8 + 16 + (size_t)8 * (n / r) * 4 + (size_t)((n / r) / 32 + 1) * 9 * 8;
+  return (size_t)sp_len<float>(n) * 8 + 16 + (size_t)8 * (n / r) * 4 + (size_t)((n / r) / 32 + 1) * 9 * 8;
 }
 
 constexpr int F32_MAX_MODES = 4;

@@ -74,8 +74,12 @@ __host__ __device__ constexpr int col_seqs(int nx) {
 // (complex double) or 16 (complex float) elements, so that the stride-r
 // Stockham writes and the contiguous per-thread chunks of the tridiagonal
 // solver fall in distinct banks.
+// one pad element per 2^shift elements (FP32 value: build-time knob)
+#ifndef VG_PAD_SHIFT_F32
+#define VG_PAD_SHIFT_F32 4
+#endif
 template <typename T>
-__host__ __device__ constexpr int pad_shift() { return sizeof(T) == 8 ? 3 : 4; }
+__host__ __device__ constexpr int pad_shift() { return sizeof(T) == 8 ? 3 : VG_PAD_SHIFT_F32; }
 template <typename T>
 __device__ __forceinline__ int sp(int i) { return i + (i >> pad_shift<T>()); }
 template <typename T>

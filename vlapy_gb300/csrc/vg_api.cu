@@ -419,6 +419,8 @@ int setup_f32(vg_plan* p, const vg_run_desc* d) {
   q->rc.D = q->D;
   q->rc.vhl = q->vhl;
   q->rc.i2dv = (float)(0.5 / dv);
+  q->rc.v0f = (float)v[0];
+  q->rc.dvf = (float)dv;
   q->rc.dv = dv;
   q->rc.dv_sq = dv2;
   q->rc.dkv = q->dkv;

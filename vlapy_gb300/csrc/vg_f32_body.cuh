@@ -197,13 +197,15 @@ template <int N, int R, typename Sync = CtaSync>
 __device__ __forceinline__ void collide_row(float* x, int t, const RowConsts& rc, float2 nudt2, float nudt_f,
                                             int dougherty, df32* red, float* pcr, const Sync& sync = Sync()) {
   constexpr int G = N / R;
-  // moments of g over the thread's chunk: sum w g, sum w g v, sum w g v^2
+  // moments of g: sum w g, sum w g v, sum w g v^2.  The elementwise parts
+  // give consecutive threads consecutive j, so the constant vectors load
+  // coalesced; only the tridiagonal solve works on contiguous chunks
   df32 mv[3];
   {
     float a0 = 0.f, a1 = 0.f, a2 = 0.f;
 #pragma unroll
     for (int i = 0; i < R; ++i) {
-      const int j = t * R + i;
+      const int j = t + i * G;
       const float w = (j == 0 || j == N - 1) ? 0.5f : 1.f;
       const float gv = w * x[2 * sp<float>(j)];
       const float vj = rc.v[j];
@@ -246,12 +248,15 @@ __device__ __forceinline__ void collide_row(float* x, int t, const RowConsts& rc
   // right-hand side: g - (A - I) f0 with (A - I) f0 = nudt (-vth S + Mv - vbar D)
 #pragma unroll
   for (int i = 0; i < R; ++i) {
-    const int j = t * R + i;
+    const int j = t + i * G;
     x[2 * sp<float>(j)] -= -cs * rc.S[j] + cm * rc.Mv[j] - cd * rc.D[j];
   }
   sync();
-  auto lf = [&](int j) { return nu * (Af + (rc.v[j - 1] - vb) * i2dv); };
-  auto uf = [&](int j) { return nu * (Af - (rc.v[j + 1] - vb) * i2dv); };
+  // off-diagonals at v[j -+ 1] of the uniform grid v[j] = v[0] + j dv,
+  // formed in registers (within an FP32 ulp of the tabulated grid)
+  const float v0 = rc.v0f, dvf = rc.dvf;
+  auto lf = [&](int j) { return nu * (Af + (fmaf((float)(j - 1), dvf, v0) - vb) * i2dv); };
+  auto uf = [&](int j) { return nu * (Af - (fmaf((float)(j + 1), dvf, v0) - vb) * i2dv); };
   partition_solve<R>(x, t, G, bdiag, lf, uf, pcr, sync);
 }
 
@@ -301,7 +306,7 @@ __device__ __forceinline__ void row_pair(const RowArgs& a, int pair, unsigned ch
     float sa[9] = {0}, sb[9] = {0};
 #pragma unroll
     for (int i = 0; i < R; ++i) {
-      const int j = t * R + i;
+      const int j = t + i * G;  // consecutive threads, consecutive j: coalesced loads
       const float w = (j == 0 || j == N - 1) ? 0.5f : 1.f;
       const float vj = a.rc->v[j], f0j = a.rc->f0[j];
       const cx<float> z = s[sp<float>(j)];

@@ -18,6 +18,7 @@ struct RowConsts {
   double dv, dv_sq, dkv;
   double f0m[7];    // trapz(f0 v^p), p = 0..5, and trapz(f0^2)
   float i2dv;       // 1 / (2 dv)
+  float v0f, dvf;   // v[0] and dv in FP32 (the grid is uniform)
   // the same in double-float, for the per-row collision scalars (the FP64
   // pipe of this part is 1/64 of FP32, so a row's scalars stay off it)
   float2 dv2f, idv2f;  // dv and 1 / dv^2 split (hi, lo)

@@ -9,8 +9,11 @@
 // passes in lockstep and synchronise with __syncthreads, so every thread of
 // the CTA must call the transform.
 //
-// Twiddles come from one table tw[q] = exp(-2 pi i q / FFT_NMAX) built once
-// per plan (sincospi in FP64), indexed with stride FFT_NMAX / (Ns r).
+// Twiddles come from one table built once per plan (sincospi in FP64),
+// ordered by span: for every power of two L = 2..FFT_NMAX it holds
+// exp(-2 pi i k / L), k = 0..L/2-1, at index L/2 - 1 + k (tw_index).  The
+// twiddle w^(m k) of span Ns r is entry k of span Ns r / m, so the threads of
+// a pass (consecutive k) load consecutive entries: one coalesced load per m.
 //
 // The passes synchronise through a policy object: CtaSync (__syncthreads,
 // every thread of the CTA calls the transform) or GroupSync (only the
@@ -128,6 +131,18 @@ struct Dft<T, 1, INV> {
   static __device__ __forceinline__ void run(cx<T>*) {}
 };
 
+// index of exp(-2 pi i k / L) in the span-ordered table (L a power of two,
+// 0 <= k < L/2)
+__host__ __device__ constexpr int tw_index(int L, int k) { return L / 2 - 1 + k; }
+
+// the table entry q: its span L = 2h (h the largest power of two <= q + 1)
+// and k = q + 1 - h, so the entry is exp(-2 pi i k / L) = exp(-i pi k / h)
+__host__ __device__ inline void tw_entry(int q, int& k, int& h) {
+  h = 1;
+  while (2 * h <= q + 1) h *= 2;
+  k = q + 1 - h;
+}
+
 template <typename T>
 __device__ __forceinline__ cx<T> twiddle(const cx<T>* __restrict__ tw, int q, bool inv) {
   cx<T> w = tw[q];
@@ -149,7 +164,6 @@ struct StockhamPass {
     constexpr int NB = N / r;      // butterflies in this pass
     constexpr int G = N / R;       // threads per sequence
     constexpr int BPT = NB / G;    // butterflies per thread
-    constexpr int TWS = FFT_NMAX / (NS * r);
     constexpr bool from_regs = (IO & 1) && NS == 1;
     constexpr bool to_regs = (IO & 2) && NS * r == N;
     static_assert(!from_regs || (BPT == 1 && r == R), "the first pass reads one radix-R butterfly per thread");
@@ -168,7 +182,7 @@ struct StockhamPass {
         // products of those (one extra rounding), halving the table loads
         cx<T> w[r];
 #pragma unroll
-        for (int m = 1; m < r; m <<= 1) w[m] = twiddle(tw, m * k * TWS, INV);
+        for (int m = 1; m < r; m <<= 1) w[m] = twiddle(tw, tw_index(NS * r / m, k), INV);
 #pragma unroll
         for (int m = 3; m < r; ++m)
           if (m & (m - 1)) w[m] = cmul(w[m & (m - 1)], w[m & -m]);

@@ -44,8 +44,10 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[NA_BYTES];
 __global__ void k_noalloc_twiddles(cx<double>* __restrict__ t64) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= FFT_NMAX) return;
+  int k, h;
+  tw_entry(q, k, h);
   double sn, cs;
-  sincospi(2.0 * (double)q / (double)FFT_NMAX, &sn, &cs);
+  sincospi((double)k / (double)h, &sn, &cs);
   t64[q] = {cs, -sn};
 }
 

@@ -411,10 +411,16 @@ __global__ void k_store_modes_f64(const double* __restrict__ f, int nx, int nv, 
     for (int xx = 0; xx < nx; ++xx) {
       const long long q = ((long long)m * xx) % nx;
       double cs, sn;
-      if (nx_pow2) {
-        const cx<double> w = tw[q * (FFT_NMAX / nx)];
-        cs = w.x;
-        sn = -w.y;
+      if (q == 0) {
+        cs = 1.0;
+        sn = 0.0;
+      } else if (nx_pow2) {
+        // exp(-2 pi i q / nx) from the span-ordered table; q >= nx/2 is the
+        // negated entry q - nx/2
+        const bool hi = 2 * q >= nx;
+        const cx<double> w = tw[tw_index(nx, hi ? (int)(q - nx / 2) : (int)q)];
+        cs = hi ? -w.x : w.x;
+        sn = hi ? w.y : -w.y;
       } else {
         sincospi(2.0 * (double)q / (double)nx, &sn, &cs);
       }
@@ -468,8 +474,10 @@ cudaError_t launch_storage_f64(const vg_plan& p, const double* f, const double* 
 __global__ void k_twiddles(cx<double>* __restrict__ t64, cx<float>* __restrict__ t32) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= FFT_NMAX) return;
+  int k, h;
+  tw_entry(q, k, h);
   double sn, cs;
-  sincospi(2.0 * (double)q / (double)FFT_NMAX, &sn, &cs);
+  sincospi((double)k / (double)h, &sn, &cs);
   t64[q] = {cs, -sn};
   t32[q] = {(float)cs, (float)-sn};
 }

@@ -498,6 +498,8 @@ int sweep_class(vg_sweep* s, int cls, int nv) {
   rc.D = dD;
   rc.vhl = dvhl;
   rc.i2dv = (float)(0.5 / dv);
+  rc.v0f = (float)v[0];
+  rc.dvf = (float)dv;
   rc.dv = dv;
   rc.dv_sq = dv2;
   rc.dkv = 2.0 * M_PI / (nv * dv);

@@ -149,6 +149,15 @@ def test_fp32_steps_match_oracle():
     np.testing.assert_allclose(sf[:, 1], rf[:, 1], atol=2e-5 * np.abs(rf[:, 1]).max())
 
 
+def test_fp32_entropy_series():
+    """mean f log f of the FP32 storage step against the FP64 oracle, on a
+    grid (vmax = 5) whose tails keep f > 0, so that the series is finite."""
+    p, f0, g, e, gst, st = _run_both(32, 256, 6, nu=1e-3, vmax=5.0)
+    got, ref = gst["series"]["mean_flogf"].cpu().numpy(), st["series"]["mean_flogf"]
+    assert np.isfinite(ref).all() and np.isfinite(got).all()
+    np.testing.assert_allclose(got, ref, rtol=1e-5)
+
+
 def test_fp32_graph_equals_direct():
     """The captured graph of the fused FP32 step replays the direct launches."""
     from vlapy_gb300.plan import history_struct

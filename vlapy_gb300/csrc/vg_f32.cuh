@@ -100,7 +100,9 @@ __device__ __forceinline__ void block_df_sum(df32 (&v)[NQ], df32* red) {
 // divisor of 32); red holds (G/32 rounded up) * NQ entries per group.  Within
 // a warp the partial sums are added in FP32 (a thread's partial covers a few
 // terms, the tree five levels: ~5e-7 relative), across warps in double-float.
-template <int NQ, typename Sync = CtaSync>
+// LEADER: only thread 0 of the group needs the totals (the other threads'
+// v are left partial), so only it adds up the warps' sums.
+template <int NQ, bool LEADER = false, typename Sync = CtaSync>
 __device__ __forceinline__ void group_df_sum(df32 (&v)[NQ], df32* red, int G, int t, const Sync& sync = Sync()) {
   if (G >= 32) {
     const int lane = t & 31, wid = t >> 5, nw = G >> 5;
@@ -116,11 +118,13 @@ __device__ __forceinline__ void group_df_sum(df32 (&v)[NQ], df32* red, int G, in
       for (int q = 0; q < NQ; ++q) red[wid * NQ + q] = v[q];
     }
     sync();
+    if (!LEADER || t == 0) {
 #pragma unroll
-    for (int q = 0; q < NQ; ++q) {
-      df32 tt = {0.f, 0.f};
-      for (int w = 0; w < nw; ++w) tt = df_add(tt, red[w * NQ + q]);
-      v[q] = tt;
+      for (int q = 0; q < NQ; ++q) {
+        df32 tt = {0.f, 0.f};
+        for (int w = 0; w < nw; ++w) tt = df_add(tt, red[w * NQ + q]);
+        v[q] = tt;
+      }
     }
     sync();
   } else {
@@ -139,6 +143,8 @@ __device__ __forceinline__ void group_df_sum(df32 (&v)[NQ], df32* red, int G, in
 // sequence in shared memory (element j at float offset 2*sp<float>(j)); thread
 // t of G owns the contiguous chunk [t*m, t*m+m), m = N/G >= 2.
 // red: shared scratch of 4 * 2G floats.  All threads of the CTA must call it.
+// The system is diagonally dominant with pivots of order one, so its divides
+// use the fast intrinsic (__fdividef, within 2 ulp there).
 template <int M, typename LFn, typename UFn, typename Sync = CtaSync>
 __device__ __forceinline__ void partition_solve(float* x, int t, int G, float b, LFn lf, UFn uf,
                                                 float* red, const Sync& sync = Sync()) {
@@ -158,7 +164,7 @@ __device__ __forceinline__ void partition_solve(float* x, int t, int G, float b,
       const int j = s + 1 + i;
       const float lj = lf(j), uj = uf(j);
       const float den = (i == 0) ? b : b - lj * cp[i - 1];
-      const float inv = 1.f / den;
+      const float inv = __fdividef(1.f, den);
       cp[i] = uj * inv;
       const float rj = x[2 * sp<float>(j)];
       y[i] = (i == 0) ? rj * inv : (rj - lj * y[i - 1]) * inv;
@@ -216,13 +222,13 @@ __device__ __forceinline__ void partition_solve(float* x, int t, int G, float b,
       na[q] = 0.f;
       nc[q] = 0.f;
       if (lo >= 0) {
-        k1 = ai / B[lo];
+        k1 = __fdividef(ai, B[lo]);
         na[q] = -A[lo] * k1;
         bi -= C[lo] * k1;
         di -= D[lo] * k1;
       }
       if (hi < NR) {
-        k2 = ci / B[hi];
+        k2 = __fdividef(ci, B[hi]);
         nc[q] = -C[hi] * k2;
         bi -= A[hi] * k2;
         di -= D[hi] * k2;
@@ -241,8 +247,8 @@ __device__ __forceinline__ void partition_solve(float* x, int t, int G, float b,
     }
     sync();
   }
-  const float xs = D[2 * t] / B[2 * t];
-  const float xe = D[2 * t + 1] / B[2 * t + 1];
+  const float xs = __fdividef(D[2 * t], B[2 * t]);
+  const float xe = __fdividef(D[2 * t + 1], B[2 * t + 1]);
   x[2 * sp<float>(s)] = xs;
   x[2 * sp<float>(e)] = xe;
   if (M > 2) {

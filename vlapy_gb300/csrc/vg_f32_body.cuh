@@ -217,7 +217,7 @@ __device__ __forceinline__ void collide_row(float* x, int t, const RowConsts& rc
     mv[1] = {a1, 0.f};
     mv[2] = {a2, 0.f};
   }
-  group_df_sum<3>(mv, red, G, t, sync);
+  group_df_sum<3, true>(mv, red, G, t, sync);
   // per-row scalars in double-float by one thread; the group reads them back
   // as FP32 coefficients, each rounded once
   float* sc = reinterpret_cast<float*>(red);
@@ -322,17 +322,18 @@ __device__ __forceinline__ void row_pair(const RowArgs& a, int pair, unsigned ch
       sb[6] = fmaf(w * z.y, z.y, sb[6]);
       sa[7] = fmaf(w * z.x, f0j, sa[7]);
       sb[7] = fmaf(w * z.y, f0j, sb[7]);
+      // f log f by the fast logarithm (3 ulp; NaN for f < 0 as in FP64)
       const float fa = z.x + f0j, fb = z.y + f0j;
-      sa[8] = fmaf(w * fa, logf(fa), sa[8]);
-      sb[8] = fmaf(w * fb, logf(fb), sb[8]);
+      sa[8] = fmaf(w * fa, __logf(fa), sa[8]);
+      sb[8] = fmaf(w * fb, __logf(fb), sb[8]);
     }
 #pragma unroll
     for (int q = 0; q < 9; ++q) {
       mv[q] = {sa[q], 0.f};
       mw[q] = {sb[q], 0.f};
     }
-    group_df_sum<9>(mv, red, G, t, sync);
-    group_df_sum<9>(mw, red, G, t, sync);
+    group_df_sum<9, true>(mv, red, G, t, sync);
+    group_df_sum<9, true>(mw, red, G, t, sync);
     if (t == 0) {
       // raw sums; the storage kernels form dv * sum + trapz(f0 ...) in FP64.
       // Each array is indexed by constants only, so it stays in registers.

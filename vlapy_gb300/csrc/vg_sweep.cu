@@ -45,11 +45,9 @@ constexpr int SWEEP_BLOCK = 256;
 #ifndef VG_SWEEP_R16_MASK
 #define VG_SWEEP_R16_MASK 0x500  // nv = 256 and 1024: measured 4.5 % faster row pass
 #endif
-#ifndef VG_COL_MIN_BLOCKS_SMALL
-#define VG_COL_MIN_BLOCKS_SMALL 3
-#endif
-#ifndef VG_COL_MIN_BLOCKS_32
-#define VG_COL_MIN_BLOCKS_32 VG_COL_MIN_BLOCKS_SMALL
+// CTAs per SM of the x-drift kernels (64 registers a thread at 4)
+#ifndef VG_COL_MIN_BLOCKS
+#define VG_COL_MIN_BLOCKS 4
 #endif
 constexpr int SWEEP_FIELD_BLOCK = 128;
 constexpr int SWEEP_MAX_CLASSES = 6;  // nv in {64, ..., 2048}
@@ -72,24 +70,114 @@ struct SweepConsts {
 // ---------------------------------------------------------------------------
 
 // x-drift of one (run, tile) item per CTA; one kernel per nx class keeps
-// each instantiation's code and registers small
+// each instantiation's code and registers small.  The tile is nx x W columns
+// (W = 2 SWEEP_BLOCK / G, always whole: nv is a multiple of W); each group of
+// G = nx/R threads transforms one column pair packed as a complex sequence.
+// The lanes of a warp are L different column pairs at the same x (L = 32, or
+// fewer when the tile has fewer pairs), so every global access of the tile
+// is a contiguous row segment; a group's G threads sit in G/(32/L) warps and
+// synchronise by a named barrier of those warps.  The first forward pass
+// reads its elements x = t + i G straight from global memory and the last
+// inverse pass leaves them in registers, which go straight back, so shared
+// memory holds only the passes in between.
+__host__ __device__ constexpr int sweep_col_lanes(int nx) {
+  return (SWEEP_BLOCK / (nx / col32_radix(nx))) < 32 ? SWEEP_BLOCK / (nx / col32_radix(nx)) : 32;
+}
+// stride of the groups' sequences in complex elements: odd, so the L lanes
+// of a pass access (same index, consecutive groups) fall in distinct bank
+// pairs; for nx = 256 (8 lanes of 4 rows) sp_len + 2.  Chosen by counting
+// the wavefronts of every pass and of the rotation.
+__host__ __device__ constexpr int sweep_col_ld(int nx) {
+  return nx == 256 ? sp_len<float>(nx) + 2 : (sp_len<float>(nx) | 1);
+}
 template <int NX>
-__global__ void __launch_bounds__(SWEEP_BLOCK, (NX == 32 ? VG_COL_MIN_BLOCKS_32 : (NX <= 64 ? VG_COL_MIN_BLOCKS_SMALL : 4))) k_sweep_col(const SweepRunDev* __restrict__ runs,
+__global__ void __launch_bounds__(SWEEP_BLOCK, VG_COL_MIN_BLOCKS) k_sweep_col(const SweepRunDev* __restrict__ runs,
                                                               const int2* __restrict__ items, float* g,
                                                               const SweepConsts* __restrict__ scp,
                                                               const cx<float>* __restrict__ tw, float2* dpart) {
   constexpr int R = col32_radix(NX);
+  constexpr int G = NX / R;
   constexpr int W = sweep_col_w(NX);
-  constexpr int LD = sp_len<float>(NX) + COL32_PAD;
+  constexpr int L = sweep_col_lanes(NX);
+  constexpr int SET = G * L;  // threads of the groups that synchronise together
+  constexpr int NSET = SWEEP_BLOCK / SET;
+  constexpr int LDG = sweep_col_ld(NX);
+  static_assert(W == 2 * (SWEEP_BLOCK / G) && SET % 32 == 0 && NSET <= 15, "tile shape");
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int2 it = items[blockIdx.x];
   const SweepRunDev r = runs[it.x];
-  df32* dacc = reinterpret_cast<df32*>(smem_raw + (size_t)(W / 2) * LD * sizeof(cx<float>));
-  for (int x = threadIdx.x; x < NX; x += blockDim.x) dacc[x] = {0.f, 0.f};
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int vr = warp * (32 / L) + lane / L;  // this lane's row slot
+  const int t = vr & (G - 1), set = vr / G;
+  const int grp = (lane & (L - 1)) + L * set;
+  cx<float>* sg = reinterpret_cast<cx<float>*>(smem_raw) + (size_t)grp * LDG;
+  float* red = reinterpret_cast<float*>(smem_raw + (size_t)(SWEEP_BLOCK / G) * LDG * sizeof(cx<float>));
+  const GroupSync sync = {1u + (unsigned)set, (unsigned)SET, 0xffffffffu};
+  const int nv = r.nv;
+  const int c = it.y * W + 2 * grp;  // this group's column pair (c, c + 1)
+  float* gc = g + r.g_off + c;
+  cx<float> io[R];
+#pragma unroll
+  for (int i = 0; i < R; ++i) {
+    const float2 q = *reinterpret_cast<const float2*>(gc + (size_t)(t + i * G) * nv);
+    io[i].x = q.x;
+    io[i].y = q.y;
+  }
+  block_fft_io<float, NX, false, R, 1>(sg, t, tw, sync, io);
+  // theta(m) = m * (-dkx dt) v_col (kx = m dkx on the bins m <= NX/2); the angle
+  // per unit m is the double-float product of kdt = -dkx dt and v (both split)
+  const float2* vhl = scp->rc[r.cls].vhl;
+  const Ang aa = mul_angle(r.kdt, vhl[c]);
+  const Ang ab = mul_angle(r.kdt, vhl[c + 1]);
+  {
+    // phases exp(i m a) for this thread's bins m = t, t+G, ...: one sincos for
+    // the start, one for the step, complex products in between
+    const float scale = 1.f / NX;
+    float sa, ca, sb, cb, sga, cga, sgb, cgb;
+    sincos_m((float)t, aa, sa, ca);
+    sincos_m((float)t, ab, sb, cb);
+    sincos_m((float)G, aa, sga, cga);
+    sincos_m((float)G, ab, sgb, cgb);
+    two_real_rotate<float>(sg, NX, t, G, [&](int, float& pca, float& psa, float& pcb, float& psb) {
+      pca = ca * scale;
+      psa = sa * scale;
+      pcb = cb * scale;
+      psb = sb * scale;
+      const float na = sa * cga + ca * sga, nca = ca * cga - sa * sga;
+      const float nb = sb * cgb + cb * sgb, ncb = cb * cgb - sb * sgb;
+      sa = na;
+      ca = nca;
+      sb = nb;
+      cb = ncb;
+    });
+  }
+  sync();
+  block_fft_io<float, NX, true, R, 2>(sg, t, tw, sync, io);
+#pragma unroll
+  for (int i = 0; i < R; ++i)
+    *reinterpret_cast<float2*>(gc + (size_t)(t + i * G) * nv) = make_float2(io[i].x, io[i].y);
+  // density partials of the tile: trapz weights (1/2 at the two v end
+  // points), summed in FP32 over the L column pairs of a warp row (lanes of
+  // equal row slot), then over the sets in double-float
+  const float wa = (c == 0) ? 0.5f : 1.f, wb = (c + 1 == nv - 1) ? 0.5f : 1.f;
+  float d[R];
+#pragma unroll
+  for (int i = 0; i < R; ++i) d[i] = fmaf(wa, io[i].x, wb * io[i].y);
+#pragma unroll
+  for (int m = 1; m < L; m <<= 1)
+#pragma unroll
+    for (int i = 0; i < R; ++i) d[i] += __shfl_xor_sync(0xffffffffu, d[i], m);
+  if ((lane & (L - 1)) == 0)
+#pragma unroll
+    for (int i = 0; i < R; ++i) red[set * NX + t + i * G] = d[i];
   __syncthreads();
-  col_tile<NX, R>(g + r.g_off, r.nv, it.y * W, W, r.kdt, scp->rc[r.cls].vhl, tw, smem_raw, dacc);
   float2* out = dpart + r.dp_off + (size_t)it.y * NX;
-  for (int x = threadIdx.x; x < NX; x += blockDim.x) out[x] = make_float2(dacc[x].hi, dacc[x].lo);
+  for (int x = threadIdx.x; x < NX; x += SWEEP_BLOCK) {
+    df32 acc = {0.f, 0.f};
+#pragma unroll
+    for (int q = 0; q < NSET; ++q) acc = df_add(acc, {red[q * NX + x], 0.f});
+    out[x] = make_float2(acc.hi, acc.lo);
+  }
 }
 
 // field solve of up to SWEEP_FIELD_BLOCK/G runs of one nx per CTA
@@ -528,8 +616,10 @@ const char* const kSweepNames[SK_COUNT] = {"sweep_kick", "sweep_x_drift", "sweep
 
 template <int NX>
 cudaError_t sweep_col_launch(vg_sweep* s, int c, cudaStream_t st) {
-  constexpr int W = sweep_col_w(NX);
-  const size_t smem = (size_t)(W / 2) * (sp_len<float>(NX) + COL32_PAD) * sizeof(cx<float>) + (size_t)NX * sizeof(df32);
+  constexpr int G = NX / col32_radix(NX);
+  constexpr int SET = G * sweep_col_lanes(NX);
+  const size_t smem = (size_t)(SWEEP_BLOCK / G) * sweep_col_ld(NX) * sizeof(cx<float>) +
+                      (size_t)(SWEEP_BLOCK / SET) * NX * sizeof(float);
   cudaError_t err = ensure_smem((const void*)k_sweep_col<NX>, smem);
   if (err != cudaSuccess) return err;
   k_sweep_col<NX><<<s->col_count[c], SWEEP_BLOCK, smem, st>>>(s->runs, s->col_items + s->col_first[c], s->g,

@@ -56,7 +56,13 @@ __host__ __device__ constexpr int sweep_col_w(int nx) { return 2 * (SWEEP_BLOCK 
 __host__ __device__ constexpr int sweep_row_radix(int nv) {
   return (nv >= 64 && nv <= 4096 && ((VG_SWEEP_R16_MASK >> ilog2(nv)) & 1)) ? 16 : row32_radix(nv);
 }
-__host__ __device__ constexpr int sweep_row_min_blocks(int nv) { return sweep_row_radix(nv) == 16 ? 2 : VG_ROW_MIN_BLOCKS; }
+// CTAs per SM of the radix-16 row kernels (16 elements a thread)
+#ifndef VG_ROW_MIN_BLOCKS_R16
+#define VG_ROW_MIN_BLOCKS_R16 2
+#endif
+__host__ __device__ constexpr int sweep_row_min_blocks(int nv) {
+  return sweep_row_radix(nv) == 16 ? VG_ROW_MIN_BLOCKS_R16 : VG_ROW_MIN_BLOCKS;
+}
 
 struct SweepConsts {
   RowConsts rc[SWEEP_MAX_CLASSES];

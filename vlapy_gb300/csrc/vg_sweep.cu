@@ -41,9 +41,12 @@ constexpr int SWEEP_BLOCK = 256;
 #define VG_ROW_MIN_BLOCKS 4
 #endif
 // nv classes (bit log2 nv) whose row kernel runs radix-16 FFT passes (16
-// elements per thread, one pass fewer for nv = 256 and 1024); build-time knob
+// elements per thread: one pass fewer for nv = 256 and 1024, and for nv = 512
+// a row pair per warp); build-time knob.  On the 4096-run sweep, radix 16 for
+// nv = 256, 512 and 1024 gives the fastest row pass (1.76 ms, against 1.92 ms
+// with nv = 512 on radix 8 and 2.29 ms with nv = 1024 on radix 8)
 #ifndef VG_SWEEP_R16_MASK
-#define VG_SWEEP_R16_MASK 0x500  // nv = 256 and 1024: measured 4.5 % faster row pass
+#define VG_SWEEP_R16_MASK 0x700
 #endif
 // CTAs per SM of the x-drift kernels (64 registers a thread at 4)
 #ifndef VG_COL_MIN_BLOCKS

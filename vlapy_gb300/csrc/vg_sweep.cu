@@ -35,6 +35,12 @@ struct SweepRunDev {
 };
 
 constexpr int SWEEP_BLOCK = 256;
+// threads per CTA of the row kernels (build-time knob; the radix-16 kernels
+// are register-bound, so smaller CTAs give finer occupancy steps)
+#ifndef VG_SWEEP_ROW_BLOCK
+#define VG_SWEEP_ROW_BLOCK 256
+#endif
+constexpr int SWEEP_ROW_BLOCK = VG_SWEEP_ROW_BLOCK;
 // resident CTAs per SM the row and column kernels are compiled for (the
 // register budget per thread follows); build-time tuning knobs
 #ifndef VG_ROW_MIN_BLOCKS
@@ -58,6 +64,11 @@ constexpr int SWEEP_MAX_CLASSES = 6;  // nv in {64, ..., 2048}
 __host__ __device__ constexpr int sweep_col_w(int nx) { return 2 * (SWEEP_BLOCK / (nx / col32_radix(nx))); }
 __host__ __device__ constexpr int sweep_row_radix(int nv) {
   return (nv >= 64 && nv <= 4096 && ((VG_SWEEP_R16_MASK >> ilog2(nv)) & 1)) ? 16 : row32_radix(nv);
+}
+// threads per CTA of the nv-class row kernel: SWEEP_ROW_BLOCK, or one group
+// where a group (nv / radix threads) is larger
+__host__ __device__ constexpr int sweep_row_block(int nv) {
+  return nv / sweep_row_radix(nv) > SWEEP_ROW_BLOCK ? nv / sweep_row_radix(nv) : SWEEP_ROW_BLOCK;
 }
 // CTAs per SM of the radix-16 row kernels (16 elements a thread)
 #ifndef VG_ROW_MIN_BLOCKS_R16
@@ -263,12 +274,14 @@ struct SweepRowArgs {
 
 // one (run, row-pair group) item per CTA; one kernel per nv class
 template <int N>
-__global__ void __launch_bounds__(SWEEP_BLOCK, sweep_row_min_blocks(N)) k_sweep_row(const SweepRunDev* __restrict__ runs,
+__global__ void __launch_bounds__(sweep_row_block(N), sweep_row_min_blocks(N)) k_sweep_row(const SweepRunDev* __restrict__ runs,
                                                               const int2* __restrict__ items, SweepRowArgs sa,
                                                               const SweepConsts* __restrict__ scp) {
   constexpr int R = sweep_row_radix(N);
   constexpr int G = N / R;
-  constexpr int P = SWEEP_BLOCK / G;
+  constexpr int P = sweep_row_block(N) / G;
+  // whole groups; a group of more than a warp takes named barrier 1 + grp
+  static_assert(P * G == sweep_row_block(N) && (G <= 32 || P <= 15), "row-pair groups per CTA");
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int2 it = items[blockIdx.x];
   const SweepRunDev r = runs[it.x];
@@ -639,10 +652,10 @@ cudaError_t sweep_col_launch(vg_sweep* s, int c, cudaStream_t st) {
 template <int N>
 cudaError_t sweep_row_launch(vg_sweep* s, int c, const SweepRowArgs& a, cudaStream_t st) {
   constexpr int R = sweep_row_radix(N);
-  const size_t smem = (size_t)(SWEEP_BLOCK / (N / R)) * row32_group_bytes(N, R);
+  const size_t smem = (size_t)(sweep_row_block(N) / (N / R)) * row32_group_bytes(N, R);
   cudaError_t err = ensure_smem((const void*)k_sweep_row<N>, smem);
   if (err != cudaSuccess) return err;
-  k_sweep_row<N><<<s->row_count[c], SWEEP_BLOCK, smem, st>>>(s->runs, s->row_items + s->row_first[c], a, s->consts);
+  k_sweep_row<N><<<s->row_count[c], sweep_row_block(N), smem, st>>>(s->runs, s->row_items + s->row_first[c], a, s->consts);
   return cudaGetLastError();
 }
 
@@ -828,7 +841,7 @@ int vg_sweep_create(const vg_sweep_desc* d, vg_sweep** out) {
     const SweepRunDev& r = s->runs_h[i];
     for (int t = 0; t < r.ntiles; ++t) col_by[r.nx].push_back(make_int2(i, t));
     const int G = r.nv / sweep_row_radix(r.nv);
-    const int P = SWEEP_BLOCK / G;
+    const int P = sweep_row_block(r.nv) / G;
     for (int pg = 0; pg * P < r.nx / 2; ++pg) row_by[r.nv].push_back(make_int2(i, pg));
     by_nx[r.nx].push_back(i);
   }

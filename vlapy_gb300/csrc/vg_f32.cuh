@@ -137,17 +137,23 @@ __device__ __forceinline__ void group_df_sum(df32 (&v)[NQ], df32* red, int G, in
   }
 }
 
-// ---- tridiagonal solve: partition (interior Thomas) + PCR ---------------
+// ---- tridiagonal solve: partition (interior Thomas) + reduced system -----
 // Solves rows j = 0..N-1: l(j) x[j-1] + b x[j] + u(j) x[j+1] = x_in[j]
 // (l(0) and u(N-1) ignored).  x is one component of a padded complex-float
 // sequence in shared memory (element j at float offset 2*sp<float>(j)); thread
-// t of G owns the contiguous chunk [t*m, t*m+m), m = N/G >= 2.
-// red: shared scratch of 4 * 2G floats.  All threads of the CTA must call it.
+// t of the G threads of a group owns the contiguous chunk [t*M, t*M+M),
+// M >= 2.  Each chunk is reduced by an interior Thomas sweep to two equations
+// in its end values x_s, x_e (the 2G-row boundary system).  One cyclic-
+// reduction step folds the x_s rows into the x_e rows, PCR solves the G
+// remaining rows (one per thread), and the x_s follow by back-substitution.
+// The neighbour rows move by shuffles when the group is one warp or less,
+// otherwise through red (2 x G float4, 16-byte aligned, double-buffered: one
+// group sync per exchange).  All threads of the group must call it.
 // The system is diagonally dominant with pivots of order one, so its divides
 // use the fast intrinsic (__fdividef, within 2 ulp there).
-template <int M, typename LFn, typename UFn, typename Sync = CtaSync>
-__device__ __forceinline__ void partition_solve(float* x, int t, int G, float b, LFn lf, UFn uf,
-                                                float* red, const Sync& sync = Sync()) {
+template <int M, int G, typename LFn, typename UFn, typename Sync = CtaSync>
+__device__ __forceinline__ void partition_solve(float* x, int t, float b, LFn lf, UFn uf, float* red,
+                                                const Sync& sync = Sync()) {
   const int s = t * M, e = s + M - 1;
   float y[M > 2 ? M - 2 : 1], al[M > 2 ? M - 2 : 1], be[M > 2 ? M - 2 : 1];
   float r_s = x[2 * sp<float>(s)], r_e = x[2 * sp<float>(e)];
@@ -196,59 +202,94 @@ __device__ __forceinline__ void partition_solve(float* x, int t, int G, float b,
     RC1 = u_e;
     RD1 = r_e;
   }
-  // PCR on the 2G boundary unknowns (x_s, x_e of every chunk)
-  const int NR = 2 * G;
-  float* A = red;
-  float* B = red + NR;
-  float* C = red + 2 * NR;
-  float* D = red + 3 * NR;
-  A[2 * t] = RA0;
-  B[2 * t] = RB0;
-  C[2 * t] = RC0;
-  D[2 * t] = RD0;
-  A[2 * t + 1] = RA1;
-  B[2 * t + 1] = RB1;
-  C[2 * t + 1] = RC1;
-  D[2 * t + 1] = RD1;
-  sync();
-  for (int st = 1; st < NR; st <<= 1) {
-    float na[2], nb[2], nc[2], nd[2];
-#pragma unroll
-    for (int q = 0; q < 2; ++q) {
-      const int i = 2 * t + q;
-      const int lo = i - st, hi = i + st;
-      float ai = A[i], bi = B[i], ci = C[i], di = D[i];
-      float k1 = 0.f, k2 = 0.f;
-      na[q] = 0.f;
-      nc[q] = 0.f;
-      if (lo >= 0) {
-        k1 = __fdividef(ai, B[lo]);
-        na[q] = -A[lo] * k1;
-        bi -= C[lo] * k1;
-        di -= D[lo] * k1;
-      }
-      if (hi < NR) {
-        k2 = __fdividef(ci, B[hi]);
-        nc[q] = -C[hi] * k2;
-        bi -= A[hi] * k2;
-        di -= D[hi] * k2;
-      }
-      nb[q] = bi;
-      nd[q] = di;
+  // the boundary rows: row 2t (x_s: RA0 x_e(t-1) + RB0 x_s + RC0 x_e = RD0) and
+  // row 2t+1 (x_e: RA1 x_s + RB1 x_e + RC1 x_s(t+1) = RD1)
+  constexpr bool SHFL = G <= 32;
+  const unsigned lane = threadIdx.x & 31u;
+  const unsigned mask = G >= 32 ? 0xffffffffu : (((1u << G) - 1u) << (lane & ~(unsigned)(G - 1)));
+  float4* buf = reinterpret_cast<float4*>(red);
+  int ph = 0;
+  // publish this thread's row, then fetch the row of thread t + d (meaningful
+  // for 0 <= t + d < G); d is the same on every thread of the group
+  auto publish = [&](const float4& v) {
+    if constexpr (!SHFL) {
+      buf[ph * G + t] = v;
+      sync();
     }
-    sync();
-#pragma unroll
-    for (int q = 0; q < 2; ++q) {
-      const int i = 2 * t + q;
-      A[i] = na[q];
-      B[i] = nb[q];
-      C[i] = nc[q];
-      D[i] = nd[q];
+  };
+  auto fetch = [&](const float4& own, int d) -> float4 {
+    if constexpr (SHFL) {
+      float4 r;
+      if (d > 0) {
+        r.x = __shfl_down_sync(mask, own.x, d, G);
+        r.y = __shfl_down_sync(mask, own.y, d, G);
+        r.z = __shfl_down_sync(mask, own.z, d, G);
+        r.w = __shfl_down_sync(mask, own.w, d, G);
+      } else {
+        r.x = __shfl_up_sync(mask, own.x, -d, G);
+        r.y = __shfl_up_sync(mask, own.y, -d, G);
+        r.z = __shfl_up_sync(mask, own.z, -d, G);
+        r.w = __shfl_up_sync(mask, own.w, -d, G);
+      }
+      return r;
+    } else {
+      const int src = t + d;
+      return (src >= 0 && src < G) ? buf[ph * G + src] : own;
     }
-    sync();
+  };
+  auto done = [&]() {
+    if constexpr (!SHFL) ph ^= 1;
+  };
+  // cyclic reduction: row 2t+1 without x_s(t) (own row 2t) and x_s(t+1)
+  // (row 2t+2, thread t+1's first row)
+  float A, B, C, D;
+  {
+    const float4 r0 = make_float4(RA0, RB0, RC0, RD0);
+    publish(r0);
+    const float4 n0 = fetch(r0, 1);
+    done();
+    const bool up = t + 1 < G;
+    const float k1 = __fdividef(RA1, RB0);
+    const float k2 = up ? __fdividef(RC1, n0.y) : 0.f;
+    A = -RA0 * k1;
+    B = RB1 - RC0 * k1 - (up ? n0.x * k2 : 0.f);
+    C = up ? -n0.z * k2 : 0.f;
+    D = RD1 - RD0 * k1 - (up ? n0.w * k2 : 0.f);
   }
-  const float xs = __fdividef(D[2 * t], B[2 * t]);
-  const float xe = __fdividef(D[2 * t + 1], B[2 * t + 1]);
+  // PCR on the G rows in x_e(t)
+#pragma unroll
+  for (int st = 1; st < G; st <<= 1) {
+    const float4 me = make_float4(A, B, C, D);
+    publish(me);
+    const float4 lo = fetch(me, -st), hi = fetch(me, st);
+    done();
+    float nA = 0.f, nC = 0.f, nB = B, nD = D;
+    if (t >= st) {
+      const float k1 = __fdividef(A, lo.y);
+      nA = -lo.x * k1;
+      nB -= lo.z * k1;
+      nD -= lo.w * k1;
+    }
+    if (t + st < G) {
+      const float k2 = __fdividef(C, hi.y);
+      nC = -hi.z * k2;
+      nB -= hi.x * k2;
+      nD -= hi.w * k2;
+    }
+    A = nA;
+    B = nB;
+    C = nC;
+    D = nD;
+  }
+  const float xe = __fdividef(D, B);
+  // back-substitution: x_s(t) from row 2t with x_e(t-1) and x_e(t)
+  float xe_lo;
+  {
+    const float4 v = make_float4(xe, 0.f, 0.f, 0.f);
+    publish(v);
+    xe_lo = fetch(v, -1).x;
+  }
+  const float xs = __fdividef(RD0 - (t > 0 ? RA0 * xe_lo : 0.f) - RC0 * xe, RB0);
   x[2 * sp<float>(s)] = xs;
   x[2 * sp<float>(e)] = xe;
   if (M > 2) {

@@ -257,7 +257,7 @@ __device__ __forceinline__ void collide_row(float* x, int t, const RowConsts& rc
   const float v0 = rc.v0f, dvf = rc.dvf;
   auto lf = [&](int j) { return nu * (Af + (fmaf((float)(j - 1), dvf, v0) - vb) * i2dv); };
   auto uf = [&](int j) { return nu * (Af - (fmaf((float)(j + 1), dvf, v0) - vb) * i2dv); };
-  partition_solve<R>(x, t, G, bdiag, lf, uf, pcr, sync);
+  partition_solve<R, G>(x, t, bdiag, lf, uf, pcr, sync);
 }
 
 // One row-pair group of the row pass: load, [kick dt1], [collide], [moments
@@ -268,8 +268,10 @@ __device__ __forceinline__ void row_pair(const RowArgs& a, int pair, unsigned ch
                                          int P, int grp, int t, const Sync& sync = Sync()) {
   constexpr int G = N / R;
   cx<float>* s = reinterpret_cast<cx<float>*>(grp_base);
-  constexpr size_t seq_bytes = (size_t)sp_len<float>(N) * sizeof(cx<float>) + 16;
-  static_assert(seq_bytes + 8 * G * sizeof(float) + (G / 32 + 1) * 9 * sizeof(df32) == row32_group_bytes(N, R),
+  constexpr size_t seq_bytes = row32_seq_bytes(N);
+  static_assert(seq_bytes % 16 == 0 && row32_group_bytes(N, R) % 16 == 0 &&
+                    seq_bytes + 8 * G * sizeof(float) + round16((G / 32 + 1) * 9 * sizeof(df32)) ==
+                        row32_group_bytes(N, R),
                 "row-pair group layout and its host-side size disagree");
   float* pcr = reinterpret_cast<float*>(grp_base + seq_bytes);
   df32* red = reinterpret_cast<df32*>(grp_base + seq_bytes + 8 * G * sizeof(float));

@@ -77,10 +77,13 @@ __host__ __device__ constexpr int col32_seqs(int nx, int r) {
 }
 __host__ __device__ constexpr int row32_radix(int n) { return n <= 8 ? n : (n <= 4096 ? 8 : 16); }
 __host__ __device__ constexpr int row32_block(int n, int r) { return (n / r) >= 256 ? (n / r) : 256; }
-// per row-pair group: padded sequence (sp_len<float>, the layout the row
-// kernels index), PCR scratch of 4 x 2G floats, double-float reduction slots
+// per row-pair group, each part 16-byte aligned: padded sequence (sp_len,
+// the layout the row kernels index), boundary-solve scratch of 8G floats
+// (2 x G float4), double-float reduction slots
+__host__ __device__ constexpr size_t round16(size_t b) { return (b + 15) & ~(size_t)15; }
+__host__ __device__ constexpr size_t row32_seq_bytes(int n) { return round16((size_t)sp_len<float>(n) * 8 + 16); }
 __host__ __device__ constexpr size_t row32_group_bytes(int n, int r) {
-  return (size_t)sp_len<float>(n) * 8 + 16 + (size_t)8 * (n / r) * 4 + (size_t)((n / r) / 32 + 1) * 9 * 8;
+  return row32_seq_bytes(n) + (size_t)8 * (n / r) * 4 + round16((size_t)((n / r) / 32 + 1) * 9 * 8);
 }
 
 constexpr int F32_MAX_MODES = 4;

@@ -97,9 +97,10 @@ __device__ __forceinline__ void block_df_sum(df32 (&v)[NQ], df32* red) {
 }
 
 // Same, restricted to the G threads of one group (G a multiple of 32 or a
-// divisor of 32); red holds (G/32 rounded up) * NQ entries per group.  Within
-// a warp the partial sums are added in FP32 (a thread's partial covers a few
-// terms, the tree five levels: ~5e-7 relative), across warps in double-float.
+// divisor of 32); red holds (G/32 rounded up) * NQ entries per group (none
+// for G < 32).  Within a warp the partial sums are added in FP32 (a thread's
+// partial covers a few terms, the tree at most five levels: ~5e-7 relative),
+// across warps in double-float.
 // LEADER: only thread 0 of the group needs the totals (the other threads'
 // v are left partial), so only it adds up the warps' sums.
 template <int NQ, bool LEADER = false, typename Sync = CtaSync>
@@ -128,10 +129,16 @@ __device__ __forceinline__ void group_df_sum(df32 (&v)[NQ], df32* red, int G, in
     }
     sync();
   } else {
-    // groups smaller than a warp: shuffle within the aligned sub-warp
+    // groups smaller than a warp: FP32 shuffles within the aligned sub-warp
+    // (at most four levels over per-thread partials, as within a warp above)
 #pragma unroll
-    for (int q = 0; q < NQ; ++q)
-      for (int m = G >> 1; m > 0; m >>= 1) v[q] = df_add(v[q], df_shfl_xor(v[q], m));
+    for (int q = 0; q < NQ; ++q) {
+      float x = v[q].hi + v[q].lo;
+#pragma unroll
+      for (int m = 16; m > 0; m >>= 1)
+        if (m < G) x += __shfl_xor_sync(0xffffffffu, x, m);
+      v[q] = {x, 0.f};
+    }
     sync();
     sync();
   }

@@ -263,7 +263,10 @@ __device__ __forceinline__ void collide_row(float* x, int t, const RowConsts& rc
 // One row-pair group of the row pass: load, [kick dt1], [collide], [moments
 // and x-mode partials], [kick dt2], store.  grp_base: this group's shared
 // memory (row32_group_bytes); macc: the CTA's mode accumulators [n_modes][N].
-template <int N, int R, typename Sync = CtaSync>
+// NPOW: how many power moments sum w g v^p (p < NPOW) the storage needs (6:
+// n, j, T, q, fv4, vN; the batched sweep's series need only p < 3); the
+// slots of the others are left unwritten.
+template <int N, int R, typename Sync = CtaSync, int NPOW = 6>
 __device__ __forceinline__ void row_pair(const RowArgs& a, int pair, unsigned char* grp_base, cx<float>* macc,
                                          int P, int grp, int t, const Sync& sync = Sync()) {
   constexpr int G = N / R;
@@ -303,9 +306,11 @@ __device__ __forceinline__ void row_pair(const RowArgs& a, int pair, unsigned ch
     collide_row<N, R>(sx + 1, t, *a.rc, a.nudt2, a.nudt_f, a.dougherty, red, pcr, sync);
   }
   if (a.want_mom) {
-    // n, j, T, q, fv4, vN (sums of w g v^p), sum w g^2, sum w g f0, sum w f log f
-    df32 mv[9], mw[9];
-    float sa[9] = {0}, sb[9] = {0};
+    // sums of w g v^p (p < NPOW), sum w g^2, sum w g f0, sum w f log f for
+    // both rows: [0, NQ) row a, [NQ, 2 NQ) row b
+    static_assert(NPOW >= 1 && NPOW <= 6, "power moments");
+    constexpr int NQ = NPOW + 3;
+    float sa[NQ] = {0}, sb[NQ] = {0};
 #pragma unroll
     for (int i = 0; i < R; ++i) {
       const int j = t + i * G;  // consecutive threads, consecutive j: coalesced loads
@@ -314,40 +319,63 @@ __device__ __forceinline__ void row_pair(const RowArgs& a, int pair, unsigned ch
       const cx<float> z = s[sp<float>(j)];
       float pa = w * z.x, pb = w * z.y;
 #pragma unroll
-      for (int p = 0; p < 6; ++p) {
+      for (int p = 0; p < NPOW; ++p) {
         sa[p] += pa;
         sb[p] += pb;
-        pa *= vj;
-        pb *= vj;
+        if (p + 1 < NPOW) {
+          pa *= vj;
+          pb *= vj;
+        }
       }
-      sa[6] = fmaf(w * z.x, z.x, sa[6]);
-      sb[6] = fmaf(w * z.y, z.y, sb[6]);
-      sa[7] = fmaf(w * z.x, f0j, sa[7]);
-      sb[7] = fmaf(w * z.y, f0j, sb[7]);
+      sa[NPOW] = fmaf(w * z.x, z.x, sa[NPOW]);
+      sb[NPOW] = fmaf(w * z.y, z.y, sb[NPOW]);
+      sa[NPOW + 1] = fmaf(w * z.x, f0j, sa[NPOW + 1]);
+      sb[NPOW + 1] = fmaf(w * z.y, f0j, sb[NPOW + 1]);
       // f log f by the fast logarithm (3 ulp; NaN for f < 0 as in FP64)
       const float fa = z.x + f0j, fb = z.y + f0j;
-      sa[8] = fmaf(w * fa, __logf(fa), sa[8]);
-      sb[8] = fmaf(w * fb, __logf(fb), sb[8]);
+      sa[NPOW + 2] = fmaf(w * fa, __logf(fa), sa[NPOW + 2]);
+      sb[NPOW + 2] = fmaf(w * fb, __logf(fb), sb[NPOW + 2]);
     }
+    df32 m2[2 * NQ];
 #pragma unroll
-    for (int q = 0; q < 9; ++q) {
-      mv[q] = {sa[q], 0.f};
-      mw[q] = {sb[q], 0.f};
+    for (int q = 0; q < NQ; ++q) {
+      m2[q] = {sa[q], 0.f};
+      m2[NQ + q] = {sb[q], 0.f};
     }
-    group_df_sum<9, true>(mv, red, G, t, sync);
-    group_df_sum<9, true>(mw, red, G, t, sync);
+    // one reduction of both rows where red has the room (9 slots per warp
+    // and one more warp's worth; a group inside one warp needs none), else
+    // one per row
+    constexpr int NW = G >= 32 ? G / 32 : 1;
+    if constexpr (G < 32 || 2 * NQ * NW <= 9 * (G / 32 + 1)) {
+      group_df_sum<2 * NQ, true>(m2, red, G, t, sync);
+    } else {
+      df32 ma[NQ], mb[NQ];
+#pragma unroll
+      for (int q = 0; q < NQ; ++q) {
+        ma[q] = m2[q];
+        mb[q] = m2[NQ + q];
+      }
+      group_df_sum<NQ, true>(ma, red, G, t, sync);
+      group_df_sum<NQ, true>(mb, red, G, t, sync);
+#pragma unroll
+      for (int q = 0; q < NQ; ++q) {
+        m2[q] = ma[q];
+        m2[NQ + q] = mb[q];
+      }
+    }
     if (t == 0) {
       // raw sums; the storage kernels form dv * sum + trapz(f0 ...) in FP64.
       // Each array is indexed by constants only, so it stays in registers.
-      auto put = [&](const df32 (&m)[9], int row) {
+      auto put = [&](int o, int row) {
         df32* out = reinterpret_cast<df32*>(a.mom + (size_t)row * MOM_STRIDE);
 #pragma unroll
-        for (int p = 0; p < 6; ++p) out[p] = m[p];
-        out[6] = df_add(m[6], {2.f * m[7].hi, 2.f * m[7].lo});  // sum w (g^2 + 2 g f0)
-        out[7] = m[8];
+        for (int p = 0; p < NPOW; ++p) out[p] = m2[o + p];
+        // sum w (g^2 + 2 g f0)
+        out[6] = df_add(m2[o + NPOW], {2.f * m2[o + NPOW + 1].hi, 2.f * m2[o + NPOW + 1].lo});
+        out[7] = m2[o + NPOW + 2];
       };
-      if (va) put(mv, ra);
-      if (vb) put(mw, rb);
+      if (va) put(0, ra);
+      if (vb) put(NQ, rb);
     }
     // x-Fourier modes of f (the f0 part of mode 0 is added in the reduction);
     // the groups of a CTA hold different rows but add into the same bins,

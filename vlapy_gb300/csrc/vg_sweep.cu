@@ -306,8 +306,9 @@ __global__ void __launch_bounds__(sweep_row_block(N), sweep_row_min_blocks(N)) k
   a.tw = sa.tw;
   a.rc = &scp->rc[r.cls];
   // the row-pair groups of a CTA are independent: each synchronises alone
-  row_pair<N, R>(a, it.y * P + grp, smem_raw + (size_t)grp * row32_group_bytes(N, R), nullptr, P, grp, t,
-                 GroupSync::of(grp, G));
+  // the sweep's series use the power moments p = 0, 1, 2 only
+  row_pair<N, R, GroupSync, 3>(a, it.y * P + grp, smem_raw + (size_t)grp * row32_group_bytes(N, R), nullptr, P,
+                               grp, t, GroupSync::of(grp, G));
 }
 
 // e history row and the seven series of every run (one CTA per run)

@@ -87,6 +87,20 @@ template <typename T>
 __device__ __forceinline__ int sp(int i) { return i + (i >> pad_shift<T>()); }
 template <typename T>
 __host__ __device__ constexpr int sp_len(int n) { return n + (n >> pad_shift<T>()); }
+// Padded offset of element base + m * S, m = 0..r-1, as sp(base) plus a
+// compile-time constant per m wherever the pad pattern allows (CASE):
+//  1: S a multiple of the pad period P: sp(base) + m (S + S/P);
+//  2: base mod P < S (with S | P), or S = 1 and base a multiple of r (r | P):
+//     no pad boundary falls between base and base + m S other than those
+//     of m S itself, so sp(base) + m S + (m S) / P;
+//  0: otherwise the element's own sp().
+template <typename T, int S, int CASE>
+__device__ __forceinline__ int sp_step(int spbase, int base, int m) {
+  constexpr int P = 1 << pad_shift<T>();
+  if constexpr (CASE == 1) return spbase + m * (S + S / P);
+  else if constexpr (CASE == 2) return spbase + m * S + ((m * S) >> pad_shift<T>());
+  else return sp<T>(base + m * S);
+}
 
 // multiply by exp(-+2 pi i k / R), forward sign '-' unless INV
 template <typename T, int R, bool INV>
@@ -167,15 +181,23 @@ struct StockhamPass {
     constexpr bool from_regs = (IO & 1) && NS == 1;
     constexpr bool to_regs = (IO & 2) && NS * r == N;
     static_assert(!from_regs || (BPT == 1 && r == R), "the first pass reads one radix-R butterfly per thread");
+    constexpr int PP = 1 << pad_shift<T>();
+    // loads: element j + m NB; NB a multiple of the pad period makes the
+    // offsets constant past sp(j)
+    constexpr int LCASE = (NB % PP == 0) ? 1 : 0;
+    // stores: element base + m NS with base = (j - k) r + k: for NS = 1 base
+    // is a multiple of r; for NS r >= P, base mod P = k < NS
+    constexpr int SCASE = (NS % PP == 0) ? 1 : ((NS == 1 && PP % r == 0) || (PP % NS == 0 && NS * r >= PP)) ? 2 : 0;
     cx<T> a[BPT][r];
 #pragma unroll
     for (int b = 0; b < BPT; ++b) {
       const int j = t + b * G;
       const int k = j & (NS - 1);
+      const int spj = sp<T>(j);
 #pragma unroll
       for (int m = 0; m < r; ++m) {
         if constexpr (from_regs) a[b][m] = io[m];
-        else a[b][m] = s[sp<T>(j + m * NB)];
+        else a[b][m] = s[sp_step<T, NB, LCASE>(spj, j, m)];
       }
       if (NS > 1) {
         // twiddles w^m: the power-of-two m from the table, the others as
@@ -204,8 +226,9 @@ struct StockhamPass {
         const int j = t + b * G;
         const int k = j & (NS - 1);
         const int base = (j - k) * r + k;
+        const int spb = sp<T>(base);
 #pragma unroll
-        for (int m = 0; m < r; ++m) s[sp<T>(base + m * NS)] = a[b][m];
+        for (int m = 0; m < r; ++m) s[sp_step<T, NS, SCASE>(spb, base, m)] = a[b][m];
       }
       sync();
       StockhamPass<T, N, R, INV, NS * r, IO>::run(s, t, tw, sync, io);

@@ -54,14 +54,28 @@ constexpr int SWEEP_ROW_BLOCK = VG_SWEEP_ROW_BLOCK;
 #ifndef VG_SWEEP_R16_MASK
 #define VG_SWEEP_R16_MASK 0x700
 #endif
-// CTAs per SM of the x-drift kernels (64 registers a thread at 4)
+// CTAs per SM of the x-drift kernels (64 registers a thread at 4; the
+// radix-16 ones hold 16 elements a thread)
 #ifndef VG_COL_MIN_BLOCKS
 #define VG_COL_MIN_BLOCKS 4
+#endif
+// (3: a small spill, but on the 4096-run sweep the nx = 128 x-drift takes
+// 0.43 ms against 0.46 ms at 2 CTAs and at radix 8)
+#ifndef VG_COL_MIN_BLOCKS_R16
+#define VG_COL_MIN_BLOCKS_R16 3
 #endif
 constexpr int SWEEP_FIELD_BLOCK = 128;
 constexpr int SWEEP_MAX_CLASSES = 6;  // nv in {64, ..., 2048}
 
-__host__ __device__ constexpr int sweep_col_w(int nx) { return 2 * (SWEEP_BLOCK / (nx / col32_radix(nx))); }
+// FFT radix of the sweep's x-drift: radix 16 where it saves a pass (nx in
+// the build-time mask, bit log2 nx: 128 = 16 x 8 instead of 8 x 8 x 2)
+#ifndef VG_SWEEP_COL_R16_MASK
+#define VG_SWEEP_COL_R16_MASK 0x80
+#endif
+__host__ __device__ constexpr int sweep_col_radix(int nx) {
+  return (nx >= 32 && nx <= 256 && ((VG_SWEEP_COL_R16_MASK >> ilog2(nx)) & 1)) ? 16 : col32_radix(nx);
+}
+__host__ __device__ constexpr int sweep_col_w(int nx) { return 2 * (SWEEP_BLOCK / (nx / sweep_col_radix(nx))); }
 __host__ __device__ constexpr int sweep_row_radix(int nv) {
   return (nv >= 64 && nv <= 4096 && ((VG_SWEEP_R16_MASK >> ilog2(nv)) & 1)) ? 16 : row32_radix(nv);
 }
@@ -101,7 +115,7 @@ struct SweepConsts {
 // inverse pass leaves them in registers, which go straight back, so shared
 // memory holds only the passes in between.
 __host__ __device__ constexpr int sweep_col_lanes(int nx) {
-  return (SWEEP_BLOCK / (nx / col32_radix(nx))) < 32 ? SWEEP_BLOCK / (nx / col32_radix(nx)) : 32;
+  return (SWEEP_BLOCK / (nx / sweep_col_radix(nx))) < 32 ? SWEEP_BLOCK / (nx / sweep_col_radix(nx)) : 32;
 }
 // stride of the groups' sequences in complex elements: odd, so the L lanes
 // of a pass access (same index, consecutive groups) fall in distinct bank
@@ -111,11 +125,11 @@ __host__ __device__ constexpr int sweep_col_ld(int nx) {
   return nx == 256 ? sp_len<float>(nx) + 2 : (sp_len<float>(nx) | 1);
 }
 template <int NX>
-__global__ void __launch_bounds__(SWEEP_BLOCK, VG_COL_MIN_BLOCKS) k_sweep_col(const SweepRunDev* __restrict__ runs,
+__global__ void __launch_bounds__(SWEEP_BLOCK, sweep_col_radix(NX) == 16 ? VG_COL_MIN_BLOCKS_R16 : VG_COL_MIN_BLOCKS) k_sweep_col(const SweepRunDev* __restrict__ runs,
                                                               const int2* __restrict__ items, float* g,
                                                               const SweepConsts* __restrict__ scp,
                                                               const cx<float>* __restrict__ tw, float2* dpart) {
-  constexpr int R = col32_radix(NX);
+  constexpr int R = sweep_col_radix(NX);
   constexpr int G = NX / R;
   constexpr int W = sweep_col_w(NX);
   constexpr int L = sweep_col_lanes(NX);
@@ -639,7 +653,7 @@ const char* const kSweepNames[SK_COUNT] = {"sweep_kick", "sweep_x_drift", "sweep
 
 template <int NX>
 cudaError_t sweep_col_launch(vg_sweep* s, int c, cudaStream_t st) {
-  constexpr int G = NX / col32_radix(NX);
+  constexpr int G = NX / sweep_col_radix(NX);
   constexpr int SET = G * sweep_col_lanes(NX);
   const size_t smem = (size_t)(SWEEP_BLOCK / G) * sweep_col_ld(NX) * sizeof(cx<float>) +
                       (size_t)(SWEEP_BLOCK / SET) * NX * sizeof(float);

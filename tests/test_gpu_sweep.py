@@ -228,3 +228,49 @@ def test_sweep_lenard_bernstein_matches_oracle():
         f_ref, _, f0 = oracle_run(r, 10, operator="lb")
         f = sw.read_run(i)[0].cpu().numpy()
         assert np.linalg.norm(f - f_ref) / np.linalg.norm(f_ref - f0[None, :]) <= 1e-4, (i, r)
+
+
+def test_sweep_full_size_properties():
+    """The default workload at its full size (4096 runs, 1.8e8 cells), through
+    properties that do not depend on the size: everything finite, each run's
+    density conserved, each run's result independent of the batch it ran in
+    (bit for bit), and one run of each shape class against the oracle."""
+    from vlapy_gb300.sweep import Sweep, sweep_config
+    runs = sweep_config(4096, 20261203)
+    nsteps = 20
+    sw = Sweep(runs)
+    sw.reset()
+    eh, sh = sw.history(nsteps)
+    sw.run_steps(nsteps, eh, sh)
+    torch.cuda.synchronize()
+    assert torch.isfinite(eh).all() and torch.isfinite(sh[:, :, :4]).all()
+    # density (n ~ 1): kicks and drifts keep it exactly, the collision keeps it
+    # discretely; FP32 delta-f rounding (~1e-7 of |g| <= 1e-2 a step) moves it
+    # by ~1e-9 over these steps
+    n = sh[:, :, 0].cpu().numpy()
+    assert np.abs(n - n[:1]).max() <= 1e-8
+    # batching independence: every 7th run in a sweep of its own
+    idx = list(range(0, len(runs), 7))
+    sub = Sweep([runs[i] for i in idx])
+    sub.reset()
+    eb, sb = sub.history(nsteps)
+    sub.run_steps(nsteps, eb, sb)
+    torch.cuda.synchronize()
+    # (mean f log f is NaN where f < 0 in the far tails, as in the reference)
+    torch.testing.assert_close(sh[:, idx, :], sb, rtol=0, atol=0, equal_nan=True)
+    for j, i in enumerate(idx[::37]):
+        assert torch.equal(sw.e_of(eh, i), sub.e_of(eb, j * 37))
+        assert torch.equal(sw.read_run(i)[0], sub.read_run(j * 37)[0])
+    # one run of each (nx, nv) class against the FP64 oracle
+    seen = set()
+    for i, r in enumerate(runs):
+        key = (r["nx"], r["nv"])
+        if key in seen:
+            continue
+        seen.add(key)
+        f_ref, e_ref, f0 = oracle_run(r, nsteps)
+        f = sw.read_run(i)[0].cpu().numpy()
+        assert np.linalg.norm(f - f_ref) / np.linalg.norm(f_ref - f0[None, :]) <= 1e-4, (i, r)
+        e_hist = sw.e_of(eh, i).cpu().numpy()
+        assert np.linalg.norm(e_hist - e_ref) / np.linalg.norm(e_ref) <= 1e-4, (i, r)
+    assert len(seen) == 9

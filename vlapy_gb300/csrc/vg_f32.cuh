@@ -74,6 +74,42 @@ __device__ __forceinline__ void sincos_m(float m, Ang a, float& s, float& c) {
   c = fmaf(-s0, e, c0);
 }
 
+// ---- sums over the lanes of a warp row by transposition -----------------
+// d[0..R) on each of the L lanes of a row (L a power of two <= 32, rows the
+// aligned L-lane blocks of the warp): after the call the lanes hold the row
+// totals of d[IDX..IDX+CNT), CNT = max(1, R / L), with IDX returned through
+// idx.  Each level sends half of the remaining values to the partner lane
+// and keeps the other half (R/2 + R/4 + ... shuffles instead of R log2 L);
+// once one value is left the levels are plain butterflies, whose duplicate
+// lanes clear `writer`, so exactly one lane of a row holds each total with
+// writer set.  All 32 lanes of the warp must call it.
+template <int R, int L>
+__device__ __forceinline__ void lane_transpose_sum(float (&d)[R], int lane, int& idx, bool& writer) {
+  idx = 0;
+  writer = true;
+  int cnt = R;
+#pragma unroll
+  for (int m = L / 2; m >= 1; m >>= 1) {
+    const bool hi = (lane & m) != 0;
+    if (cnt > 1) {
+      const int h = cnt / 2;
+#pragma unroll
+      for (int q = 0; q < R / 2; ++q) {
+        if (q < h) {
+          const float send = hi ? d[q] : d[q + h];
+          const float keep = hi ? d[q + h] : d[q];
+          d[q] = keep + __shfl_xor_sync(0xffffffffu, send, m);
+        }
+      }
+      if (hi) idx += h;
+      cnt = h;
+    } else {
+      d[0] += __shfl_xor_sync(0xffffffffu, d[0], m);
+      if (hi) writer = false;
+    }
+  }
+}
+
 // ---- CTA-wide reductions of NQ double-float values ----------------------
 // red: shared scratch of (blockDim.x / 32) * NQ df32.  Every thread gets the
 // totals.  Must be called by all threads of the CTA.

@@ -192,18 +192,18 @@ __global__ void __launch_bounds__(SWEEP_BLOCK, sweep_col_radix(NX) == 16 ? VG_CO
     *reinterpret_cast<float2*>(gc + (size_t)(t + i * G) * nv) = make_float2(io[i].x, io[i].y);
   // density partials of the tile: trapz weights (1/2 at the two v end
   // points), summed in FP32 over the L column pairs of a warp row (lanes of
-  // equal row slot), then over the sets in double-float
+  // equal row slot, by transposition), then over the sets in double-float
   const float wa = (c == 0) ? 0.5f : 1.f, wb = (c + 1 == nv - 1) ? 0.5f : 1.f;
   float d[R];
 #pragma unroll
   for (int i = 0; i < R; ++i) d[i] = fmaf(wa, io[i].x, wb * io[i].y);
+  int idx;
+  bool writer;
+  lane_transpose_sum<R, L>(d, lane, idx, writer);
+  constexpr int CNT = R > L ? R / L : 1;
+  if (writer)
 #pragma unroll
-  for (int m = 1; m < L; m <<= 1)
-#pragma unroll
-    for (int i = 0; i < R; ++i) d[i] += __shfl_xor_sync(0xffffffffu, d[i], m);
-  if ((lane & (L - 1)) == 0)
-#pragma unroll
-    for (int i = 0; i < R; ++i) red[set * NX + t + i * G] = d[i];
+    for (int q = 0; q < CNT; ++q) red[set * NX + t + (idx + q) * G] = d[q];
   __syncthreads();
   float2* out = dpart + r.dp_off + (size_t)it.y * NX;
   for (int x = threadIdx.x; x < NX; x += SWEEP_BLOCK) {

@@ -192,72 +192,106 @@ __device__ __forceinline__ void kick(cx<float>* s, int t, float hk, float ea, fl
   kick_io<N, R, 0>(s, t, hk, ea, eb, F0, tw, sync, none);
 }
 
-// Fokker-Planck step of one row stored at x (stride 2 floats) in delta-f form.
+// Per-row collision scalars from the row's raw moment sums (sum w g v^p,
+// p = 0, 1, 2), in double-float; each FP32 coefficient is rounded once:
+// out = {-vth/dv^2, 1 + 2 nudt vth/dv^2, vbar, nudt vth, nudt vbar}.
+__device__ __forceinline__ void collision_scalars(const RowConsts& rc, float2 nudt2, int dougherty, df32 s0,
+                                                  df32 s1, df32 s2, float* out) {
+  const df32 dv = {rc.dv2f.x, rc.dv2f.y};
+  const df32 M0 = df_add(df_mul(dv, s0), {rc.f0m2f[0].x, rc.f0m2f[0].y});
+  const df32 M1 = df_add(df_mul(dv, s1), {rc.f0m2f[1].x, rc.f0m2f[1].y});
+  const df32 M2 = df_add(df_mul(dv, s2), {rc.f0m2f[2].x, rc.f0m2f[2].y});
+  // DG: vbar = trapz(f v), v0t^2 = trapz(f (v - vbar)^2) = M2 + vbar^2 (M0 - 2)
+  // LB: v0t^2 = trapz(f v^2), no drift
+  const df32 vbar = dougherty ? M1 : df32{0.f, 0.f};
+  const df32 vth = dougherty ? df_add(M2, df_mul(df_mul(vbar, vbar), df_add(M0, {-2.f, 0.f}))) : M2;
+  const df32 nd = {nudt2.x, nudt2.y};
+  const df32 a = df_mul(vth, {rc.idv2f.x, rc.idv2f.y});  // vth / dv^2
+  const df32 na = df_mul(nd, a);
+  out[0] = -df_round(a);
+  out[1] = df_round(df_add({1.f, 0.f}, {2.f * na.hi, 2.f * na.lo}));
+  out[2] = df_round(vbar);
+  out[3] = df_round(df_mul(nd, vth));
+  out[4] = df_round(df_mul(nd, vbar));
+}
+
+// Fokker-Planck step, in delta-f form, of both rows of a packed pair (row a
+// in the real parts of s, row b in the imaginary parts).  The moments and the
+// right-hand sides of the two rows share one pass over the pair (one 8-byte
+// access per element, one load of each constant) and one reduction; the two
+// tridiagonal solves run one after the other.
 template <int N, int R, typename Sync = CtaSync>
-__device__ __forceinline__ void collide_row(float* x, int t, const RowConsts& rc, float2 nudt2, float nudt_f,
-                                            int dougherty, df32* red, float* pcr, const Sync& sync = Sync()) {
+__device__ __forceinline__ void collide_pair(cx<float>* s, int t, const RowConsts& rc, float2 nudt2, float nudt_f,
+                                             int dougherty, df32* red, float* pcr, const Sync& sync = Sync()) {
   constexpr int G = N / R;
-  // moments of g: sum w g, sum w g v, sum w g v^2.  The elementwise parts
-  // give consecutive threads consecutive j, so the constant vectors load
-  // coalesced; only the tridiagonal solve works on contiguous chunks
-  df32 mv[3];
+  // moments of g: sum w g, sum w g v, sum w g v^2 of each row.  The
+  // elementwise parts give consecutive threads consecutive j, so the constant
+  // vectors load coalesced; only the tridiagonal solves work on chunks
+  df32 mv[6];
   {
-    float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+    float m[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
 #pragma unroll
     for (int i = 0; i < R; ++i) {
       const int j = t + i * G;
       const float w = (j == 0 || j == N - 1) ? 0.5f : 1.f;
-      const float gv = w * x[2 * sp<float>(j)];
+      const cx<float> z = s[sp<float>(j)];
       const float vj = rc.v[j];
-      a0 += gv;
-      a1 = fmaf(gv, vj, a1);
-      a2 = fmaf(gv * vj, vj, a2);
+      const float ga = w * z.x, gb = w * z.y;
+      m[0] += ga;
+      m[1] = fmaf(ga, vj, m[1]);
+      m[2] = fmaf(ga * vj, vj, m[2]);
+      m[3] += gb;
+      m[4] = fmaf(gb, vj, m[4]);
+      m[5] = fmaf(gb * vj, vj, m[5]);
     }
-    mv[0] = {a0, 0.f};
-    mv[1] = {a1, 0.f};
-    mv[2] = {a2, 0.f};
+#pragma unroll
+    for (int q = 0; q < 6; ++q) mv[q] = {m[q], 0.f};
   }
-  group_df_sum<3, true>(mv, red, G, t, sync);
+  group_df_sum<6, true>(mv, red, G, t, sync);
   // per-row scalars in double-float by one thread; the group reads them back
-  // as FP32 coefficients, each rounded once
   float* sc = reinterpret_cast<float*>(red);
   if (t == 0) {
-    const df32 dv = {rc.dv2f.x, rc.dv2f.y};
-    const df32 M0 = df_add(df_mul(dv, mv[0]), {rc.f0m2f[0].x, rc.f0m2f[0].y});
-    const df32 M1 = df_add(df_mul(dv, mv[1]), {rc.f0m2f[1].x, rc.f0m2f[1].y});
-    const df32 M2 = df_add(df_mul(dv, mv[2]), {rc.f0m2f[2].x, rc.f0m2f[2].y});
-    // DG: vbar = trapz(f v), v0t^2 = trapz(f (v - vbar)^2) = M2 + vbar^2 (M0 - 2)
-    // LB: v0t^2 = trapz(f v^2), no drift
-    const df32 vbar = dougherty ? M1 : df32{0.f, 0.f};
-    const df32 vth = dougherty ? df_add(M2, df_mul(df_mul(vbar, vbar), df_add(M0, {-2.f, 0.f}))) : M2;
-    const df32 nd = {nudt2.x, nudt2.y};
-    const df32 a = df_mul(vth, {rc.idv2f.x, rc.idv2f.y});  // vth / dv^2
-    const df32 na = df_mul(nd, a);
-    sc[0] = -df_round(a);
-    sc[1] = df_round(df_add({1.f, 0.f}, {2.f * na.hi, 2.f * na.lo}));
-    sc[2] = df_round(vbar);
-    sc[3] = df_round(df_mul(nd, vth));
-    sc[4] = df_round(df_mul(nd, vbar));
+    collision_scalars(rc, nudt2, dougherty, mv[0], mv[1], mv[2], sc);
+    collision_scalars(rc, nudt2, dougherty, mv[3], mv[4], mv[5], sc + 5);
   }
   sync();
-  const float Af = sc[0], bdiag = sc[1], vb = sc[2], cs = sc[3], cd = sc[4];
+  float sa[5], sb[5];
+#pragma unroll
+  for (int q = 0; q < 5; ++q) {
+    sa[q] = sc[q];
+    sb[q] = sc[5 + q];
+  }
   const float nu = nudt_f;
   const float cm = nu;
   const float i2dv = rc.i2dv;
   sync();
-  // right-hand side: g - (A - I) f0 with (A - I) f0 = nudt (-vth S + Mv - vbar D)
+  // right-hand sides: g - (A - I) f0 with (A - I) f0 = nudt (-vth S + Mv - vbar D)
 #pragma unroll
   for (int i = 0; i < R; ++i) {
     const int j = t + i * G;
-    x[2 * sp<float>(j)] -= -cs * rc.S[j] + cm * rc.Mv[j] - cd * rc.D[j];
+    const float S = rc.S[j], Mv = rc.Mv[j], D = rc.D[j];
+    cx<float> z = s[sp<float>(j)];
+    z.x -= -sa[3] * S + cm * Mv - sa[4] * D;
+    z.y -= -sb[3] * S + cm * Mv - sb[4] * D;
+    s[sp<float>(j)] = z;
   }
   sync();
   // off-diagonals at v[j -+ 1] of the uniform grid v[j] = v[0] + j dv,
   // formed in registers (within an FP32 ulp of the tabulated grid)
   const float v0 = rc.v0f, dvf = rc.dvf;
-  auto lf = [&](int j) { return nu * (Af + (fmaf((float)(j - 1), dvf, v0) - vb) * i2dv); };
-  auto uf = [&](int j) { return nu * (Af - (fmaf((float)(j + 1), dvf, v0) - vb) * i2dv); };
-  partition_solve<R, G>(x, t, bdiag, lf, uf, pcr, sync);
+  float* x = reinterpret_cast<float*>(s);
+  {
+    const float Af = sa[0], vb = sa[2];
+    auto lf = [&](int j) { return nu * (Af + (fmaf((float)(j - 1), dvf, v0) - vb) * i2dv); };
+    auto uf = [&](int j) { return nu * (Af - (fmaf((float)(j + 1), dvf, v0) - vb) * i2dv); };
+    partition_solve<R, G>(x, t, sa[1], lf, uf, pcr, sync);
+  }
+  {
+    const float Af = sb[0], vb = sb[2];
+    auto lf = [&](int j) { return nu * (Af + (fmaf((float)(j - 1), dvf, v0) - vb) * i2dv); };
+    auto uf = [&](int j) { return nu * (Af - (fmaf((float)(j + 1), dvf, v0) - vb) * i2dv); };
+    partition_solve<R, G>(x + 1, t, sb[1], lf, uf, pcr, sync);
+  }
 }
 
 // One row-pair group of the row pass: load, [kick dt1], [collide], [moments
@@ -300,10 +334,8 @@ __device__ __forceinline__ void row_pair(const RowArgs& a, int pair, unsigned ch
     for (int i = 0; i < R; ++i) s[sp<float>(t + i * G)] = io[i];
     sync();
   }
-  float* sx = reinterpret_cast<float*>(s);
   if (a.fp) {
-    collide_row<N, R>(sx, t, *a.rc, a.nudt2, a.nudt_f, a.dougherty, red, pcr, sync);
-    collide_row<N, R>(sx + 1, t, *a.rc, a.nudt2, a.nudt_f, a.dougherty, red, pcr, sync);
+    collide_pair<N, R>(s, t, *a.rc, a.nudt2, a.nudt_f, a.dougherty, red, pcr, sync);
   }
   if (a.want_mom) {
     // sums of w g v^p (p < NPOW), sum w g^2, sum w g f0, sum w f log f for

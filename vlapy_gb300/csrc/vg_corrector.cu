@@ -625,10 +625,21 @@ constexpr int TC_THREADS = TC_SLOTS * 128;               // 4 warps per slot
 constexpr int TC_TILE_ROWS = CROWS;                      // 132
 constexpr int TC_LBO_ACT = 16 * TC_TILE_ROWS;            // 2112 B
 constexpr int TC_ACT_BYTES = 8 * TC_LBO_ACT;             // 64 channels
-constexpr int TC_W1_TAP = HID * L1_IN * 2, TC_W2_TAP = HID * HID * 2, TC_W4_TAP = 16 * HID * 2;
-constexpr int TC_W_BYTES = 5 * (TC_W1_TAP + 2 * TC_W2_TAP + TC_W4_TAP);  // 102400
+// the first layer folds its taps into K (im2col): K = 5 taps x 4 real input
+// channels = 20, padded to 32, so it is 2 MMAs where 5 taps x one 16-channel
+// K-step were 5; its B operand is [64 outputs][32] with k = 4 t + c
+constexpr int L1_REAL = 4, TC_K1 = 32;
+constexpr int TC_W1_BYTES = HID * TC_K1 * 2, TC_W2_TAP = HID * HID * 2;
+// the last layer (one output channel) puts its five taps in N instead: one
+// 16 x 64 B operand whose row t is tap t (rows 5..15 zero), so that the
+// layer is 4 MMAs (K = 64) of M = 128, N = 16, D4[p][t] = sum_c h3[p][c] w4[t][c],
+// and the epilogue adds out[p] = sum_t D4[p + t - 2][t]; at N = 16 an MMA
+// costs about as much as at N = 64, so this is 4 MMAs where 5 taps x 4
+// K-steps were 20
+constexpr int TC_W4_BYTES = 16 * HID * 2;
+constexpr int TC_W_BYTES = TC_W1_BYTES + 2 * 5 * TC_W2_TAP + TC_W4_BYTES;  // 88064
 constexpr int TC_OFF_W1 = 0;
-constexpr int TC_OFF_W2 = TC_OFF_W1 + 5 * TC_W1_TAP;
+constexpr int TC_OFF_W2 = TC_OFF_W1 + TC_W1_BYTES;
 constexpr int TC_OFF_W3 = TC_OFF_W2 + 5 * TC_W2_TAP;
 constexpr int TC_OFF_W4 = TC_OFF_W3 + 5 * TC_W2_TAP;
 // per slot one tile of 64 channels, updated in place: a layer's epilogue
@@ -637,8 +648,9 @@ constexpr int TC_OFF_W4 = TC_OFF_W3 + 5 * TC_W2_TAP;
 // of the first layer is the tile's first two channel groups
 constexpr int TC_OFF_SLOT = TC_W_BYTES;
 constexpr int TC_SLOT_BYTES = TC_ACT_BYTES;
-constexpr int TC_OFF_F = TC_OFF_SLOT + TC_SLOTS * TC_SLOT_BYTES;  // floats: bias[256], red[slots][128]
-constexpr int TC_NF = 256 + TC_SLOTS * 128;
+// floats: bias[256], red[slots][128], the last layer's tap sums xch[slots][5][128]
+constexpr int TC_OFF_F = TC_OFF_SLOT + TC_SLOTS * TC_SLOT_BYTES;
+constexpr int TC_NF = 256 + TC_SLOTS * 128 + TC_SLOTS * 5 * CP;
 constexpr int TC_OFF_BAR = TC_OFF_F + TC_NF * 4;         // done[slots] mbarriers, TMEM address
 constexpr int TC_SMEM = TC_OFF_BAR + 8 * TC_SLOTS + 16;
 constexpr int TC_TMEM_COLS = 512;                        // 64 per slot, rounded up to a power of two
@@ -750,6 +762,35 @@ __device__ __forceinline__ void tc_layer_issue(uint32_t tmem, uint32_t act, uint
   }
 }
 
+// issue the first layer: 2 K-steps of M = 128, N = 64 over the im2col rows
+// (position p at tile row p + 2, K = 32) against the folded weights at w
+__device__ __forceinline__ void tc_first_issue(uint32_t tmem, uint32_t act, uint32_t w) {
+  constexpr uint32_t idesc = tc_idesc(128, HID);
+  const uint64_t a0 = tc_desc(act, TC_LBO_ACT, 128);
+  const uint64_t b0 = tc_desc(w, 16 * HID, 128);
+#pragma unroll
+  for (int kc = 0; kc < TC_K1 / 16; ++kc) {
+    const uint64_t a = a0 + (uint64_t)((16 * CHALO + 2 * kc * TC_LBO_ACT) >> 4);
+    const uint64_t b = b0 + (uint64_t)((2 * kc * (16 * HID)) >> 4);
+    tc_mma(tmem, a, b, idesc, kc > 0 ? 1 : 0);
+  }
+}
+
+// issue the last layer: 4 K-steps of M = 128, N = 16 over the tile's own
+// rows (positions 0..127 at tile rows 2..129: the tap-2 start) against the
+// taps-as-rows weight operand at w
+__device__ __forceinline__ void tc_last_issue(uint32_t tmem, uint32_t act, uint32_t w) {
+  constexpr uint32_t idesc = tc_idesc(128, 16);
+  const uint64_t a0 = tc_desc(act, TC_LBO_ACT, 128);
+  const uint64_t b0 = tc_desc(w, 16 * 16, 128);
+#pragma unroll
+  for (int kc = 0; kc < HID / 16; ++kc) {
+    const uint64_t a = a0 + (uint64_t)((16 * CHALO + 2 * kc * TC_LBO_ACT) >> 4);
+    const uint64_t b = b0 + (uint64_t)((2 * kc * (16 * 16)) >> 4);
+    tc_mma(tmem, a, b, idesc, kc > 0 ? 1 : 0);
+  }
+}
+
 // epilogue of a hidden layer: TMEM (this thread's position, 64 channels) +
 // bias, ReLU, BF16 into row p + 2 of the next tile; two halves of 32
 // columns, each with its two 16-column loads in flight together (the
@@ -850,6 +891,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   const int p = 32 * quarter + lane;     // position = TMEM lane
   const bool issuer = (p == 0);          // the slot's MMA issuer
   float* red = bias + 256 + 128 * slot;
+  float* xch = bias + 256 + 128 * TC_SLOTS + 5 * CP * slot;  // [5][128]
   unsigned char* tile = smem + TC_OFF_SLOT + slot * TC_SLOT_BYTES;
   const uint32_t tile_s = s_base + TC_OFF_SLOT + slot * TC_SLOT_BYTES;
   const uint32_t td = tmem + 64 * slot, lane_base = (uint32_t)(quarter * 32) << 16;
@@ -883,10 +925,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     if (issuer) {
       tc_fence_after();
       switch (L) {
-        case 0: tc_layer_issue<L1_IN, HID>(td, tile_s, s_base + TC_OFF_W1); break;
+        case 0: tc_first_issue(td, tile_s, s_base + TC_OFF_W1); break;
         case 1: tc_layer_issue<HID, HID>(td, tile_s, s_base + TC_OFF_W2); break;
         case 2: tc_layer_issue<HID, HID>(td, tile_s, s_base + TC_OFF_W3); break;
-        default: tc_layer_issue<HID, 16>(td, tile_s, s_base + TC_OFF_W4); break;
+        default: tc_last_issue(td, tile_s, s_base + TC_OFF_W4); break;
       }
       tc_commit(bar);
     }
@@ -916,11 +958,23 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     slot_sync(slot);
     const float s = sqrtf(red[CP - 1] / CP) + 1e-30f;
     {
+      // im2col of the first layer: this position's 4 features go to channels
+      // 4t..4t+3 of the output position q = p - t + 2 that reads it at tap t;
+      // the owner of each row zeroes the taps that fall outside the row and
+      // channels 20..31 (rows 2..129 only: the halo rows stay zero)
       const __nv_bfloat162 c01 = __floats2bfloat162_rn(d / s, vfeat);
       const __nv_bfloat162 c23 = __floats2bfloat162_rn(feat, dp / s);
-      *reinterpret_cast<uint4*>(tile + tc_off(p + CHALO, 0, TC_LBO_ACT)) =
-          make_uint4(*reinterpret_cast<const uint32_t*>(&c01), *reinterpret_cast<const uint32_t*>(&c23), 0u, 0u);
-      *reinterpret_cast<uint4*>(tile + tc_off(p + CHALO, 8, TC_LBO_ACT)) = make_uint4(0, 0, 0, 0);
+      const uint2 fv = make_uint2(*reinterpret_cast<const uint32_t*>(&c01), *reinterpret_cast<const uint32_t*>(&c23));
+#pragma unroll
+      for (int t = 0; t < 5; ++t) {
+        const int q = p - t + CHALO;
+        if (q >= 0 && q < CP) *reinterpret_cast<uint2*>(tile + tc_off(q + CHALO, 4 * t, TC_LBO_ACT)) = fv;
+        const int src = p + t - CHALO;
+        if (src < 0 || src >= CP)
+          *reinterpret_cast<uint2*>(tile + tc_off(p + CHALO, 4 * t, TC_LBO_ACT)) = make_uint2(0u, 0u);
+      }
+      *reinterpret_cast<uint2*>(tile + tc_off(p + CHALO, 20, TC_LBO_ACT)) = make_uint2(0u, 0u);
+      *reinterpret_cast<uint4*>(tile + tc_off(p + CHALO, 24, TC_LBO_ACT)) = make_uint4(0u, 0u, 0u, 0u);
     }
     issue(0);
     float pred = 0.f;
@@ -936,9 +990,19 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         tc_hidden_epilogue(td, quarter, p, bias + HID * L, tile);
         issue(L + 1);
       } else {
+        // D4[p][t] (t < 5) of this position; out[p] = sum_t D4[p + t - 2][t]
+        // over the positions inside the row (the halo rows are zero)
         float v[16];
         tc_ld16(td + lane_base, v);
-        pred = v[0] + bias[3 * HID];
+#pragma unroll
+        for (int t = 0; t < 5; ++t) xch[t * CP + p] = v[t];
+        slot_sync(slot);
+        pred = bias[3 * HID];
+#pragma unroll
+        for (int t = 0; t < 5; ++t) {
+          const int q = p + t - CHALO;
+          if (q >= 0 && q < CP) pred += xch[t * CP + q];
+        }
       }
     }
     if (!ok) break;
@@ -962,18 +1026,27 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 // the four layers' BF16 weights in the fused kernel's shared-memory image
 __global__ void k_pack_tc(const float* __restrict__ w, __nv_bfloat16* __restrict__ img) {
   // layer l: (offset in params, cout real, cin, N padded, byte offset in the image)
-  const int n_total = 5 * (HID * L1_IN + 2 * HID * HID + 16 * HID);
+  const int n_total = HID * TC_K1 + 2 * 5 * HID * HID + 16 * HID;
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n_total; q += gridDim.x * blockDim.x) {
     int r = q, off, cout, cin, np, base;
-    if (r < 5 * HID * L1_IN) {
-      off = OFF_W1; cout = HID; cin = L1_IN; np = HID; base = TC_OFF_W1;
-    } else if ((r -= 5 * HID * L1_IN) < 5 * HID * HID) {
+    if (r < HID * TC_K1) {
+      // first layer, taps folded into K: k = 4 t + c (c < 4 real channels;
+      // channels 4..15 of the first layer only ever meet zero inputs)
+      const int o = r / TC_K1, k = r % TC_K1;
+      const float val = k < 5 * L1_REAL ? w[OFF_W1 + ((size_t)o * L1_IN + k % L1_REAL) * 5 + k / L1_REAL] : 0.f;
+      img[(TC_OFF_W1 + tc_off(o, k, 16 * HID)) / 2] = __float2bfloat16(val);
+      continue;
+    } else if ((r -= HID * TC_K1) < 5 * HID * HID) {
       off = OFF_W2; cout = HID; cin = HID; np = HID; base = TC_OFF_W2;
     } else if ((r -= 5 * HID * HID) < 5 * HID * HID) {
       off = OFF_W3; cout = HID; cin = HID; np = HID; base = TC_OFF_W3;
     } else {
+      // last layer: row t of the 16 x 64 operand is tap t of the one output
       r -= 5 * HID * HID;
-      off = OFF_W4; cout = 1; cin = HID; np = 16; base = TC_OFF_W4;
+      const int t = r / HID, c = r % HID;
+      const float val = t < 5 ? w[OFF_W4 + (size_t)c * 5 + t] : 0.f;
+      img[(TC_OFF_W4 + tc_off(t, c, 16 * 16)) / 2] = __float2bfloat16(val);
+      continue;
     }
     const int t = r / (np * cin), o = (r / cin) % np, c = r % cin;
     const float val = o < cout ? w[off + ((size_t)o * cin + c) * 5 + t] : 0.f;

@@ -800,7 +800,7 @@ __device__ __forceinline__ void tc_last_issue(uint32_t tmem, uint32_t act, uint3
 // epilogue of a hidden layer: TMEM (this thread's position, 64 channels) +
 // bias, ReLU, BF16 into row p + 2 of the next tile; two halves of 32
 // columns, each with its two 16-column loads in flight together (the
-// register budget of six slots per CTA)
+// register budget of TC_SLOTS slots per CTA)
 __device__ __forceinline__ void tc_hidden_epilogue(uint32_t tmem, int quarter, int p, const float* bias,
                                                    unsigned char* out_tile) {
   const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;

@@ -173,7 +173,7 @@ void free_plan(vg_plan* p) {
   delete static_cast<ProfState*>(p->prof);
   if (p->f32) {
     F32Plan* q = p->f32;
-    void* qp[] = {q->F0, q->v32, q->f0_32, q->S, q->Mv, q->D, q->dpart, q->mpart, q->vhl, q->e32, q->rc_dev};
+    void* qp[] = {q->F0, q->v32, q->f0_32, q->S, q->Mv, q->D, q->dpart, q->mpart, q->spart, q->vhl, q->e32, q->rc_dev};
     for (void* x : qp)
       if (x) cudaFree(x);
     delete q;
@@ -437,6 +437,7 @@ int setup_f32(vg_plan* p, const vg_run_desc* d) {
   q->row_grid_max = 8 * nsm;
   VG_CHECK(dev_copy<float2>(&q->dpart, nullptr, (size_t)q->col_grid_max * nx, "density partials"));
   VG_CHECK(dev_copy<cx<float>>(&q->mpart, nullptr, (size_t)q->row_grid_max * F32_MAX_MODES * nv, "mode partials"));
+  VG_CHECK(dev_copy<float2>(&q->spart, nullptr, (size_t)F32_STORE_MAX_CTAS * 7, "series partials"));
   return VG_OK;
 }
 

@@ -60,6 +60,7 @@ struct F32Plan {
   float2* dpart;       // [max col grid][nx] density partials (hi, lo)
   int npart;
   cx<float>* mpart;    // [max row grid][4][nv]
+  float2* spart;       // [F32_STORE_MAX_CTAS][7] per-CTA series partials (hi, lo) of the store
   int mgrid;
   int col_grid_max, row_grid_max, col_grid, row_grid;
   int n_sm;
@@ -87,6 +88,7 @@ __host__ __device__ constexpr size_t row32_group_bytes(int n, int r) {
 }
 
 constexpr int F32_MAX_MODES = 4;
+constexpr int F32_STORE_MAX_CTAS = 64;  // CTAs of the per-step fields/series pass
 
 // (hi, lo) FP32 split of an FP64 value
 inline float2 split_f2(double a) {

@@ -10,6 +10,8 @@
 // The first half kick of a batch runs once as a row pass of its own; the
 // last step of a batch skips the trailing kick, so the state handed back is
 // the reference's f after its collision step.
+#include <algorithm>
+
 #include "vg_f32_body.cuh"
 #include "vg_internal.cuh"
 
@@ -135,13 +137,17 @@ __global__ void __launch_bounds__(row32_block(N, R)) k_row_f32(RowArgs a) {
 // storage of one step: fields, series and stored modes
 // ---------------------------------------------------------------------------
 
+// fields of one step and the series partial sums of this CTA's rows (rows
+// blockIdx.x * blockDim.x + threadIdx.x, stride the whole grid); spart[b][q]
+// is CTA b's double-float partial of series q
 __global__ void k_store_fields_f32(const double* __restrict__ mom, RowConsts rc, const double* __restrict__ e,
-                                   const double* __restrict__ de, int nx, int i, vg_history h) {
+                                   const double* __restrict__ de, int nx, int i, vg_history h,
+                                   float2* __restrict__ spart) {
   __shared__ df32 red[32 * 7];
   const size_t off = (size_t)i * nx;
   df32 acc[7];
   for (int q = 0; q < 7; ++q) acc[q] = {0.f, 0.f};
-  for (int n = threadIdx.x; n < nx; n += blockDim.x) {
+  for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < nx; n += gridDim.x * blockDim.x) {
     const double* slots = mom + (size_t)n * MOM_STRIDE;
     double m[8];
     for (int q = 0; q < 8; ++q) m[q] = row_moment(slots, q, rc);
@@ -156,29 +162,53 @@ __global__ void k_store_fields_f32(const double* __restrict__ mom, RowConsts rc,
     }
   }
   block_df_sum<7>(acc, red);
-  if (threadIdx.x < 7 && h.series[threadIdx.x]) h.series[threadIdx.x][i] = df_to_double(acc[threadIdx.x]) / nx;
+  if (threadIdx.x < 7) spart[blockIdx.x * 7 + threadIdx.x] = make_float2(acc[threadIdx.x].hi, acc[threadIdx.x].lo);
 }
 
+// the series of one step: the CTAs' partials added in CTA order (one thread
+// per series, so the sum is the same on every run)
+__global__ void k_store_series_f32(const float2* __restrict__ spart, int nb, int nx, int i, vg_history h) {
+  const int q = threadIdx.x;
+  if (q >= 7 || !h.series[q]) return;
+  df32 acc = {0.f, 0.f};
+  for (int b = 0; b < nb; ++b) acc = df_add(acc, {spart[b * 7 + q].x, spart[b * 7 + q].y});
+  h.series[q][i] = df_to_double(acc) / nx;
+}
+
+// stored x-modes of one step: thread (j, m) adds mode m of velocity j over
+// the row kernel's per-CTA partials, in four interleaved double-float chains
+// (partials p = 0, 4, 8, ... in the first, and so on) joined in a fixed order
 __global__ void k_store_modes_f32(const cx<float>* __restrict__ mpart, int npart, int nm, int nv, int nx,
                                   const double* __restrict__ f0, int n_slots, int i, cx<float>* __restrict__ out) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= nv) return;
+  const int m = blockIdx.y;
+  if (j >= nv || m >= nm || m >= n_slots) return;
   cx<float>* dst = out + (size_t)i * n_slots * nv;
-  for (int m = 0; m < nm && m < n_slots; ++m) {
-    df32 re = {0.f, 0.f}, im = {0.f, 0.f};
-    for (int p = 0; p < npart; ++p) {
-      const cx<float> z = mpart[((size_t)p * nm + m) * nv + j];
-      re = df_add(re, {z.x, 0.f});
-      im = df_add(im, {z.y, 0.f});
+  df32 re[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+  df32 im[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+  int p = 0;
+  for (; p + 4 <= npart; p += 4) {
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const cx<float> z = mpart[((size_t)(p + u) * nm + m) * nv + j];
+      re[u] = df_add(re[u], {z.x, 0.f});
+      im[u] = df_add(im[u], {z.y, 0.f});
     }
-    double zr = df_to_double(re), zi = df_to_double(im);
-    if (m == 0) zr += (double)nx * f0[j];
-    const cx<float> z = {(float)zr, (float)zi};
-    if (nm == 1) {
-      for (int sl = 0; sl < n_slots; ++sl) dst[(size_t)sl * nv + j] = z;
-    } else {
-      dst[(size_t)m * nv + j] = z;
-    }
+  }
+  for (int u = 0; p < npart; ++p, ++u) {
+    const cx<float> z = mpart[((size_t)p * nm + m) * nv + j];
+    re[u] = df_add(re[u], {z.x, 0.f});
+    im[u] = df_add(im[u], {z.y, 0.f});
+  }
+  const df32 rs = df_add(df_add(re[0], re[1]), df_add(re[2], re[3]));
+  const df32 is = df_add(df_add(im[0], im[1]), df_add(im[2], im[3]));
+  double zr = df_to_double(rs), zi = df_to_double(is);
+  if (m == 0) zr += (double)nx * f0[j];
+  const cx<float> z = {(float)zr, (float)zi};
+  if (nm == 1) {
+    for (int sl = 0; sl < n_slots; ++sl) dst[(size_t)sl * nv + j] = z;
+  } else {
+    dst[(size_t)m * nv + j] = z;
   }
 }
 
@@ -352,8 +382,12 @@ cudaError_t launch_row_f32(const vg_plan& p, float* g, const double* e, double d
 
 cudaError_t launch_store_f32(const vg_plan& p, const float* g, const double* e, const double* de,
                              const vg_history& h, int i, int n_modes, cudaStream_t s) {
-  k_store_fields_f32<<<1, 256, 0, s>>>(p.mom, p.f32->rc, e, de, p.nx, i, h);
+  const int nb = std::min(F32_STORE_MAX_CTAS, (p.nx + 255) / 256);
+  k_store_fields_f32<<<nb, 256, 0, s>>>(p.mom, p.f32->rc, e, de, p.nx, i, h, p.f32->spart);
   cudaError_t err = cudaGetLastError();
+  if (err != cudaSuccess) return err;
+  k_store_series_f32<<<1, 32, 0, s>>>(p.f32->spart, nb, p.nx, i, h);
+  err = cudaGetLastError();
   if (err != cudaSuccess) return err;
   if (h.stored_f && h.store_all) {
     const size_t n = (size_t)p.nx * p.nv;
@@ -362,8 +396,8 @@ cudaError_t launch_store_f32(const vg_plan& p, const float* g, const double* e, 
     return cudaGetLastError();
   }
   if (h.stored_f && !h.store_all && n_modes > 0) {
-    k_store_modes_f32<<<div_up(p.nv, 128), 128, 0, s>>>(p.f32->mpart, p.f32->mgrid, n_modes, p.nv, p.nx, p.f_bg,
-                                                        h.n_slots, i, static_cast<cx<float>*>(h.stored_f));
+    k_store_modes_f32<<<dim3(div_up(p.nv, 128), n_modes), 128, 0, s>>>(
+        p.f32->mpart, p.f32->mgrid, n_modes, p.nv, p.nx, p.f_bg, h.n_slots, i, static_cast<cx<float>*>(h.stored_f));
     err = cudaGetLastError();
   }
   return err;

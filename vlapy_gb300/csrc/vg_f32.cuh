@@ -110,6 +110,36 @@ __device__ __forceinline__ void lane_transpose_sum(float (&d)[R], int lane, int&
   }
 }
 
+// The same for R double-float values over the whole warp (L = 32): the
+// writer lane with index idx holds the warp total of d[idx] in d[0] (R a
+// power of two <= 32).
+template <int R>
+__device__ __forceinline__ void warp_transpose_sum_df(df32 (&d)[R], int lane, int& idx, bool& writer) {
+  idx = 0;
+  writer = true;
+  int cnt = R;
+#pragma unroll
+  for (int m = 16; m >= 1; m >>= 1) {
+    const bool hi = (lane & m) != 0;
+    if (cnt > 1) {
+      const int h = cnt / 2;
+#pragma unroll
+      for (int q = 0; q < R / 2; ++q) {
+        if (q < h) {
+          const df32 send = hi ? d[q] : d[q + h];
+          const df32 keep = hi ? d[q + h] : d[q];
+          d[q] = df_add(keep, df_shfl_xor(send, m));
+        }
+      }
+      if (hi) idx += h;
+      cnt = h;
+    } else {
+      d[0] = df_add(d[0], df_shfl_xor(d[0], m));
+      if (hi) writer = false;
+    }
+  }
+}
+
 // ---- CTA-wide reductions of NQ double-float values ----------------------
 // red: shared scratch of (blockDim.x / 32) * NQ df32.  Every thread gets the
 // totals.  Must be called by all threads of the CTA.

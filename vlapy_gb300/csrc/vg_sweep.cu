@@ -325,29 +325,42 @@ __global__ void __launch_bounds__(sweep_row_block(N), sweep_row_min_blocks(N)) k
                                grp, t, GroupSync::of(grp, G));
 }
 
-// e history row and the seven series of every run (one CTA per run)
+// e history row and the seven series of every run (one CTA per run, one
+// row per thread): each warp adds its rows' double-float sums by
+// transposition, then seven threads add the four warps' totals in order
 __global__ void __launch_bounds__(128) k_sweep_store(const SweepRunDev* __restrict__ runs, int n_runs,
                                                      const SweepConsts* __restrict__ scp,
                                                      const double* __restrict__ mom, const double* __restrict__ e,
                                                      double* __restrict__ e_row, double* __restrict__ s_row) {
-  __shared__ df32 red[4 * 7];
+  __shared__ df32 red[4][8];
   const SweepRunDev r = runs[blockIdx.x];
-  df32 acc[7];
-  for (int q = 0; q < 7; ++q) acc[q] = {0.f, 0.f};
+  const RowConsts& rc = scp->rc[r.cls];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  df32 acc[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) acc[q] = {0.f, 0.f};
   for (int x = threadIdx.x; x < r.nx; x += blockDim.x) {
     const double ex = e[r.x_off + x];
     if (e_row) e_row[r.x_off + x] = ex;
     const double* slots = mom + (size_t)(r.x_off + x) * MOM_STRIDE;
-    const RowConsts& rc = scp->rc[r.cls];
     const double src[7] = {row_moment(slots, 0, rc), row_moment(slots, 1, rc), row_moment(slots, 2, rc), ex * ex,
                            0.0, row_moment(slots, 6, rc), row_moment(slots, 7, rc)};
+#pragma unroll
     for (int q = 0; q < 7; ++q) {
       const float hi = (float)src[q];
       acc[q] = df_add(acc[q], {hi, (float)(src[q] - (double)hi)});
     }
   }
-  block_df_sum<7>(acc, red);
-  if (s_row && threadIdx.x < 7) s_row[(size_t)blockIdx.x * 7 + threadIdx.x] = df_to_double(acc[threadIdx.x]) / r.nx;
+  int idx;
+  bool writer;
+  warp_transpose_sum_df<8>(acc, lane, idx, writer);
+  if (writer) red[warp][idx] = acc[0];
+  __syncthreads();
+  if (s_row && threadIdx.x < 7) {
+    df32 t = red[0][threadIdx.x];
+    for (int w = 1; w < 4; ++w) t = df_add(t, red[w][threadIdx.x]);
+    s_row[(size_t)blockIdx.x * 7 + threadIdx.x] = df_to_double(t) / r.nx;
+  }
 }
 
 // initial state g = A cos(k x_j) M(v) (the x-mean of f = M (1 + A cos k x) is M)

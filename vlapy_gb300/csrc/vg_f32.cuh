@@ -228,7 +228,13 @@ template <int M, int G, typename LFn, typename UFn, typename Sync = CtaSync>
 __device__ __forceinline__ void partition_solve(float* x, int t, float b, LFn lf, UFn uf, float* red,
                                                 const Sync& sync = Sync()) {
   const int s = t * M, e = s + M - 1;
-  float y[M > 2 ? M - 2 : 1], al[M > 2 ? M - 2 : 1], be[M > 2 ? M - 2 : 1];
+  // the x_e influence vector needs no array: its source is the last interior
+  // row only, so the forward sweep leaves it zero above that row and
+  // back-substitution makes it be[i] = -cp[i] be[i+1] from be_last.  The
+  // data solution y lives in place of the right-hand side in x (registers
+  // hold the x_s influence al and the pivots cp).
+  float al[M > 2 ? M - 2 : 1], cp[M > 2 ? M - 2 : 1];
+  float be_last = 0.f, be0 = 0.f, y_last = 0.f, y0 = 0.f;
   float r_s = x[2 * sp<float>(s)], r_e = x[2 * sp<float>(e)];
   float RA0, RB0, RC0, RD0, RA1, RB1, RC1, RD1;
   const float l_s = (s == 0) ? 0.f : lf(s);
@@ -237,7 +243,6 @@ __device__ __forceinline__ void partition_solve(float* x, int t, float b, LFn lf
   const float u_e = (e == G * M - 1) ? 0.f : uf(e);
   if (M > 2) {
     // interior Thomas with three right-hand sides: data, x_s influence, x_e influence
-    float cp[M > 2 ? M - 2 : 1];
 #pragma unroll
     for (int i = 0; i < M - 2; ++i) {
       const int j = s + 1 + i;
@@ -246,25 +251,29 @@ __device__ __forceinline__ void partition_solve(float* x, int t, float b, LFn lf
       const float inv = __fdividef(1.f, den);
       cp[i] = uj * inv;
       const float rj = x[2 * sp<float>(j)];
-      y[i] = (i == 0) ? rj * inv : (rj - lj * y[i - 1]) * inv;
+      y_last = (i == 0) ? rj * inv : (rj - lj * y_last) * inv;
+      x[2 * sp<float>(j)] = y_last;
       al[i] = (i == 0) ? -lj * inv : (-lj * al[i - 1]) * inv;
-      const float bsrc = (i == M - 3) ? -uj : 0.f;
-      be[i] = (i == 0) ? bsrc * inv : (bsrc - lj * be[i - 1]) * inv;
+      if (i == M - 3) be_last = -uj * inv;
     }
+    be0 = be_last;
+    y0 = y_last;
 #pragma unroll
     for (int i = M - 4; i >= 0; --i) {
-      y[i] -= cp[i] * y[i + 1];
+      float* xj = x + 2 * sp<float>(s + 1 + i);
+      y0 = *xj - cp[i] * y0;
+      *xj = y0;
       al[i] -= cp[i] * al[i + 1];
-      be[i] -= cp[i] * be[i + 1];
+      be0 = -cp[i] * be0;
     }
     RA0 = l_s;
     RB0 = b + u_s * al[0];
-    RC0 = u_s * be[0];
-    RD0 = r_s - u_s * y[0];
+    RC0 = u_s * be0;
+    RD0 = r_s - u_s * y0;
     RA1 = l_e * al[M - 3];
-    RB1 = b + l_e * be[M - 3];
+    RB1 = b + l_e * be_last;
     RC1 = u_e;
-    RD1 = r_e - l_e * y[M - 3];
+    RD1 = r_e - l_e * y_last;
   } else {
     RA0 = l_s;
     RB0 = b;
@@ -366,8 +375,13 @@ __device__ __forceinline__ void partition_solve(float* x, int t, float b, LFn lf
   x[2 * sp<float>(s)] = xs;
   x[2 * sp<float>(e)] = xe;
   if (M > 2) {
+    float bi = be_last;
 #pragma unroll
-    for (int i = 0; i < M - 2; ++i) x[2 * sp<float>(s + 1 + i)] = y[i] + al[i] * xs + be[i] * xe;
+    for (int i = M - 3; i >= 0; --i) {
+      if (i < M - 3) bi = -cp[i] * bi;
+      float* xj = x + 2 * sp<float>(s + 1 + i);
+      *xj = *xj + al[i] * xs + bi * xe;
+    }
   }
   sync();
 }

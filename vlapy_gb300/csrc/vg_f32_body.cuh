@@ -317,135 +317,148 @@ __device__ __forceinline__ void row_pair(const RowArgs& a, int pair, unsigned ch
   const bool va = ra < a.nx, vb = rb < a.nx;
   float* ga = a.g + (size_t)ra * N;
   float* gbp = a.g + (size_t)rb * N;
-  // the pair's elements t + i G: exactly what the first FFT pass of the kick
-  // reads, so they go from global memory straight into that pass
-  cx<float> io[R];
-#pragma unroll
-  for (int i = 0; i < R; ++i) {
-    const int n = t + i * G;
-    io[i] = {va ? ga[n] : 0.f, vb ? gbp[n] : 0.f};
-  }
   const bool kicks = a.hk1 != 0.f || a.hk2 != 0.f;
   const float ea = (kicks && va) ? a.e32[ra] : 0.f, eb = (kicks && vb) ? a.e32[rb] : 0.f;
-  if (a.hk1 != 0.f) {
-    kick_io<N, R, 1>(s, t, a.hk1, ea, eb, a.F0, a.tw, sync, io);
-  } else {
+  // both kicks run the same code (registers in, registers out), once each in
+  // a loop the compiler keeps rolled, so the kernel holds one copy of the
+  // kick's FFTs instead of four differently specialised ones (instruction-
+  // cache pressure); the collision and the moments sit between the two
+#pragma unroll 1
+  for (int kpass = 0; kpass < 2; ++kpass) {
+    const float hk = kpass == 0 ? a.hk1 : a.hk2;
+    // the pair's elements t + i G, exactly what the first FFT pass reads: from
+    // global memory before the first kick, from shared memory before the
+    // second (io is defined afresh in every pass, so it is dead in between)
+    cx<float> io[R];
+    if (kpass == 0) {
+#pragma unroll
+      for (int i = 0; i < R; ++i) {
+        const int n = t + i * G;
+        io[i] = {va ? ga[n] : 0.f, vb ? gbp[n] : 0.f};
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < R; ++i) io[i] = s[sp<float>(t + i * G)];
+    }
+    if (hk != 0.f) {
+      kick_io<N, R, 3>(s, t, hk, ea, eb, a.F0, a.tw, sync, io);
+    }
+    if (kpass == 1) {
+      // the last FFT pass left elements t + i G in registers: the store
+      // pattern, so they go straight back to global memory
+#pragma unroll
+      for (int i = 0; i < R; ++i) {
+        const int n = t + i * G;
+        if (va) ga[n] = io[i].x;
+        if (vb) gbp[n] = io[i].y;
+      }
+      break;
+    }
+    // the pair into shared memory for the collision and the moments (after
+    // every thread's last kick pass has read it)
+    sync();
 #pragma unroll
     for (int i = 0; i < R; ++i) s[sp<float>(t + i * G)] = io[i];
     sync();
-  }
-  if (a.fp) {
-    collide_pair<N, R>(s, t, *a.rc, a.nudt2, a.nudt_f, a.dougherty, red, pcr, sync);
-  }
-  if (a.want_mom) {
-    // sums of w g v^p (p < NPOW), sum w g^2, sum w g f0, sum w f log f for
-    // both rows: [0, NQ) row a, [NQ, 2 NQ) row b
-    static_assert(NPOW >= 1 && NPOW <= 6, "power moments");
-    constexpr int NQ = NPOW + 3;
-    float sa[NQ] = {0}, sb[NQ] = {0};
-#pragma unroll
-    for (int i = 0; i < R; ++i) {
-      const int j = t + i * G;  // consecutive threads, consecutive j: coalesced loads
-      const float w = (j == 0 || j == N - 1) ? 0.5f : 1.f;
-      const float vj = a.rc->v[j], f0j = a.rc->f0[j];
-      const cx<float> z = s[sp<float>(j)];
-      float pa = w * z.x, pb = w * z.y;
-#pragma unroll
-      for (int p = 0; p < NPOW; ++p) {
-        sa[p] += pa;
-        sb[p] += pb;
-        if (p + 1 < NPOW) {
-          pa *= vj;
-          pb *= vj;
-        }
-      }
-      sa[NPOW] = fmaf(w * z.x, z.x, sa[NPOW]);
-      sb[NPOW] = fmaf(w * z.y, z.y, sb[NPOW]);
-      sa[NPOW + 1] = fmaf(w * z.x, f0j, sa[NPOW + 1]);
-      sb[NPOW + 1] = fmaf(w * z.y, f0j, sb[NPOW + 1]);
-      // f log f by the fast logarithm (3 ulp; NaN for f < 0 as in FP64)
-      const float fa = z.x + f0j, fb = z.y + f0j;
-      sa[NPOW + 2] = fmaf(w * fa, __logf(fa), sa[NPOW + 2]);
-      sb[NPOW + 2] = fmaf(w * fb, __logf(fb), sb[NPOW + 2]);
+    if (a.fp) {
+      collide_pair<N, R>(s, t, *a.rc, a.nudt2, a.nudt_f, a.dougherty, red, pcr, sync);
     }
-    df32 m2[2 * NQ];
-#pragma unroll
-    for (int q = 0; q < NQ; ++q) {
-      m2[q] = {sa[q], 0.f};
-      m2[NQ + q] = {sb[q], 0.f};
-    }
-    // one reduction of both rows where red has the room (9 slots per warp
-    // and one more warp's worth; a group inside one warp needs none), else
-    // one per row
-    constexpr int NW = G >= 32 ? G / 32 : 1;
-    if constexpr (G < 32 || 2 * NQ * NW <= 9 * (G / 32 + 1)) {
-      group_df_sum<2 * NQ, true>(m2, red, G, t, sync);
-    } else {
-      df32 ma[NQ], mb[NQ];
-#pragma unroll
-      for (int q = 0; q < NQ; ++q) {
-        ma[q] = m2[q];
-        mb[q] = m2[NQ + q];
-      }
-      group_df_sum<NQ, true>(ma, red, G, t, sync);
-      group_df_sum<NQ, true>(mb, red, G, t, sync);
-#pragma unroll
-      for (int q = 0; q < NQ; ++q) {
-        m2[q] = ma[q];
-        m2[NQ + q] = mb[q];
-      }
-    }
-    if (t == 0) {
-      // raw sums; the storage kernels form dv * sum + trapz(f0 ...) in FP64.
-      // Each array is indexed by constants only, so it stays in registers.
-      auto put = [&](int o, int row) {
-        df32* out = reinterpret_cast<df32*>(a.mom + (size_t)row * MOM_STRIDE);
-#pragma unroll
-        for (int p = 0; p < NPOW; ++p) out[p] = m2[o + p];
-        // sum w (g^2 + 2 g f0)
-        out[6] = df_add(m2[o + NPOW], {2.f * m2[o + NPOW + 1].hi, 2.f * m2[o + NPOW + 1].lo});
-        out[7] = m2[o + NPOW + 2];
-      };
-      if (va) put(0, ra);
-      if (vb) put(NQ, rb);
-    }
-    // x-Fourier modes of f (the f0 part of mode 0 is added in the reduction);
-    // the groups of a CTA hold different rows but add into the same bins,
-    // so they take turns
-    // (only with a CTA-wide sync: the turns are CTA barriers)
-    if (Sync::cta_wide && nm > 0) {
-      for (int gq = 0; gq < P; ++gq) {
-        if (gq == grp) {
-          for (int mq = 0; mq < nm; ++mq) {
-            float swa = 0.f, cwa = 0.f, swb = 0.f, cwb = 0.f;
-            if (va) sincospif(-2.f * (float)((mq * ra) % a.nx) / (float)a.nx, &swa, &cwa);
-            if (vb) sincospif(-2.f * (float)((mq * rb) % a.nx) / (float)a.nx, &swb, &cwb);
-            for (int i = 0; i < R; ++i) {
-              const int n = t + i * G;
-              const cx<float> z = s[sp<float>(n)];
-              cx<float>& acc = macc[(size_t)mq * N + n];
-              acc.x += z.x * cwa + z.y * cwb;
-              acc.y += z.x * swa + z.y * swb;
-            }
+    if (a.want_mom) {
+      // sums of w g v^p (p < NPOW), sum w g^2, sum w g f0, sum w f log f for
+      // both rows: [0, NQ) row a, [NQ, 2 NQ) row b
+      static_assert(NPOW >= 1 && NPOW <= 6, "power moments");
+      constexpr int NQ = NPOW + 3;
+      float sa[NQ] = {0}, sb[NQ] = {0};
+  #pragma unroll
+      for (int i = 0; i < R; ++i) {
+        const int j = t + i * G;  // consecutive threads, consecutive j: coalesced loads
+        const float w = (j == 0 || j == N - 1) ? 0.5f : 1.f;
+        const float vj = a.rc->v[j], f0j = a.rc->f0[j];
+        const cx<float> z = s[sp<float>(j)];
+        float pa = w * z.x, pb = w * z.y;
+  #pragma unroll
+        for (int p = 0; p < NPOW; ++p) {
+          sa[p] += pa;
+          sb[p] += pb;
+          if (p + 1 < NPOW) {
+            pa *= vj;
+            pb *= vj;
           }
         }
-        __syncthreads();
+        sa[NPOW] = fmaf(w * z.x, z.x, sa[NPOW]);
+        sb[NPOW] = fmaf(w * z.y, z.y, sb[NPOW]);
+        sa[NPOW + 1] = fmaf(w * z.x, f0j, sa[NPOW + 1]);
+        sb[NPOW + 1] = fmaf(w * z.y, f0j, sb[NPOW + 1]);
+        // f log f by the fast logarithm (3 ulp; NaN for f < 0 as in FP64)
+        const float fa = z.x + f0j, fb = z.y + f0j;
+        sa[NPOW + 2] = fmaf(w * fa, __logf(fa), sa[NPOW + 2]);
+        sb[NPOW + 2] = fmaf(w * fb, __logf(fb), sb[NPOW + 2]);
+      }
+      df32 m2[2 * NQ];
+  #pragma unroll
+      for (int q = 0; q < NQ; ++q) {
+        m2[q] = {sa[q], 0.f};
+        m2[NQ + q] = {sb[q], 0.f};
+      }
+      // one reduction of both rows where red has the room (9 slots per warp
+      // and one more warp's worth; a group inside one warp needs none), else
+      // one per row
+      constexpr int NW = G >= 32 ? G / 32 : 1;
+      if constexpr (G < 32 || 2 * NQ * NW <= 9 * (G / 32 + 1)) {
+        group_df_sum<2 * NQ, true>(m2, red, G, t, sync);
+      } else {
+        df32 ma[NQ], mb[NQ];
+  #pragma unroll
+        for (int q = 0; q < NQ; ++q) {
+          ma[q] = m2[q];
+          mb[q] = m2[NQ + q];
+        }
+        group_df_sum<NQ, true>(ma, red, G, t, sync);
+        group_df_sum<NQ, true>(mb, red, G, t, sync);
+  #pragma unroll
+        for (int q = 0; q < NQ; ++q) {
+          m2[q] = ma[q];
+          m2[NQ + q] = mb[q];
+        }
+      }
+      if (t == 0) {
+        // raw sums; the storage kernels form dv * sum + trapz(f0 ...) in FP64.
+        // Each array is indexed by constants only, so it stays in registers.
+        auto put = [&](int o, int row) {
+          df32* out = reinterpret_cast<df32*>(a.mom + (size_t)row * MOM_STRIDE);
+  #pragma unroll
+          for (int p = 0; p < NPOW; ++p) out[p] = m2[o + p];
+          // sum w (g^2 + 2 g f0)
+          out[6] = df_add(m2[o + NPOW], {2.f * m2[o + NPOW + 1].hi, 2.f * m2[o + NPOW + 1].lo});
+          out[7] = m2[o + NPOW + 2];
+        };
+        if (va) put(0, ra);
+        if (vb) put(NQ, rb);
+      }
+      // x-Fourier modes of f (the f0 part of mode 0 is added in the reduction);
+      // the groups of a CTA hold different rows but add into the same bins,
+      // so they take turns
+      // (only with a CTA-wide sync: the turns are CTA barriers)
+      if (Sync::cta_wide && nm > 0) {
+        for (int gq = 0; gq < P; ++gq) {
+          if (gq == grp) {
+            for (int mq = 0; mq < nm; ++mq) {
+              float swa = 0.f, cwa = 0.f, swb = 0.f, cwb = 0.f;
+              if (va) sincospif(-2.f * (float)((mq * ra) % a.nx) / (float)a.nx, &swa, &cwa);
+              if (vb) sincospif(-2.f * (float)((mq * rb) % a.nx) / (float)a.nx, &swb, &cwb);
+              for (int i = 0; i < R; ++i) {
+                const int n = t + i * G;
+                const cx<float> z = s[sp<float>(n)];
+                cx<float>& acc = macc[(size_t)mq * N + n];
+                acc.x += z.x * cwa + z.y * cwb;
+                acc.y += z.x * swa + z.y * swb;
+              }
+            }
+          }
+          __syncthreads();
+        }
       }
     }
-  }
-  // the last FFT pass of the kick leaves elements t + i G in registers: the
-  // store pattern, so they go straight back to global memory
-  if (a.hk2 != 0.f) {
-    kick_io<N, R, 2>(s, t, a.hk2, ea, eb, a.F0, a.tw, sync, io);
-  } else {
-#pragma unroll
-    for (int i = 0; i < R; ++i) io[i] = s[sp<float>(t + i * G)];
-  }
-#pragma unroll
-  for (int i = 0; i < R; ++i) {
-    const int n = t + i * G;
-    if (va) ga[n] = io[i].x;
-    if (vb) gbp[n] = io[i].y;
   }
   sync();
 }

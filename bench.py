@@ -129,11 +129,12 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
-# DRAM bytes of one sweep row pass per cell (dram__bytes_read.sum +
-# dram__bytes_write.sum summed over the pass's three nv-class launches),
-# measured by ncu on the 800-run sweep (36.0 M cells): 145.04 MB read,
-# 34.40 MB written.  The full 4096-run pass is scaled from it per cell.
-ROW_PASS_DRAM_BYTES_PER_CELL = (145037312 + 34400768) / 36036608
+# DRAM bytes of the sweep row pass per cell (dram__bytes_read.sum +
+# dram__bytes_write.sum), measured by ncu on the nv = 1024 launch of the
+# 800-run sweep (2592 CTAs x 4 row pairs x 2048 cells = 21.23 M cells):
+# 85.22 MB read, 27.92 MB written.  The full 4096-run pass is scaled from
+# it per cell.
+ROW_PASS_DRAM_BYTES_PER_CELL = (85217792 + 27923712) / 21233664
 
 
 def peaks():
@@ -787,7 +788,7 @@ def main_sweep(args, w, rank, world):
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": ROW_PASS_DRAM_BYTES_PER_CELL * cells if dom_name == "sweep_row_pass" else None,
-                     "traffic_source": "ncu dram bytes of one row pass of the 800-run sweep, scaled per cell; "
+                     "traffic_source": "ncu dram bytes of the nv=1024 row launch of the 800-run sweep, scaled per cell; "
                                        "below the algorithmic 8 B/cell because written rows stay in L2 past the "
                                        "launch",
                      "kernel": dom_name, "peak_source": peak_kind, "kernel_ms": avg_ms,

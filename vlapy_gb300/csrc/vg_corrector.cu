@@ -1031,7 +1031,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 
 // the four layers' BF16 weights in the fused kernel's shared-memory image
 __global__ void k_pack_tc(const float* __restrict__ w, __nv_bfloat16* __restrict__ img) {
-  // layer l: (offset in params, cout real, cin, N padded, byte offset in the image)
+  // layers 2 and 3: (offset in params, cout, cin, N, byte offset in the image);
+  // layers 1 and 4 have their own folded layouts below
   const int n_total = HID * TC_K1 + 2 * 5 * HID * HID + 16 * HID;
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n_total; q += gridDim.x * blockDim.x) {
     int r = q, off, cout, cin, np, base;

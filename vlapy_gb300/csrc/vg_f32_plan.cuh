@@ -66,7 +66,8 @@ struct F32Plan {
   int n_sm;
 };
 
-// launch shapes (shared by kernels' __launch_bounds__ and the launchers)
+// launch shapes of the single-run kernels (shared by their __launch_bounds__
+// and the launchers; the batched sweep chooses its own)
 // column tiles: radix 8 up to nx = 1024, radix 16 above; S column pairs per
 // CTA, at least 4 (32-byte row segments) but at most 512 threads, so that a
 // thread keeps up to 128 registers

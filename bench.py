@@ -581,9 +581,11 @@ def _oracle_sweep_sample(args):
     return nx * nv * steps, time.perf_counter() - t0
 
 
-def cpu_baseline_sweep(w, n_sample=36, steps=10, cores=None):
+def cpu_baseline_sweep(w, n_sample=36, steps=10, cores=None, reps=1, warmup=0):
     """Reference step (CPU oracle) on a stratified sample of sweep runs, one
-    process per host core; aggregate cell-updates/s and extrapolated runs/s."""
+    process per host core; aggregate cell-updates/s and extrapolated runs/s.
+    One sample advances every sampled run by `steps` oracle steps; `warmup`
+    untimed samples run first, then `reps` timed ones."""
     import multiprocessing as mp
     from vlapy_gb300.sweep import sweep_config
     runs = sweep_config(w["n_runs"], w["seed"])
@@ -595,19 +597,25 @@ def cpu_baseline_sweep(w, n_sample=36, steps=10, cores=None):
     for key in sorted(classes):
         sample += classes[key][:per_class]
     cores = cores or os.cpu_count() or 1
+    walls, results = [], []
     with mp.get_context("spawn").Pool(min(cores, len(sample))) as pool:
         # warm the workers (imports, first FFT plans) before timing
         pool.map(_oracle_sweep_sample, [(r, 1, w["vmax"], w["dt"]) for r in sample])
-        t0 = time.perf_counter()
-        res = pool.map(_oracle_sweep_sample, [(r, steps, w["vmax"], w["dt"]) for r in sample])
-        wall = time.perf_counter() - t0
-    cells = sum(c for c, _ in res)
+        for _ in range(warmup):
+            pool.map(_oracle_sweep_sample, [(r, steps, w["vmax"], w["dt"]) for r in sample])
+        for _ in range(max(1, reps)):
+            t0 = time.perf_counter()
+            results.append(pool.map(_oracle_sweep_sample, [(r, steps, w["vmax"], w["dt"]) for r in sample]))
+            walls.append(time.perf_counter() - t0)
+    cells = sum(c for res in results for c, _ in res)
     # seconds per step per class (single core), then the whole sweep on `cores` cores
     sec_class = {}
-    for r, (c, sec) in zip(sample, res):
-        sec_class.setdefault((r["nx"], r["nv"]), []).append(sec / steps)
+    for res in results:
+        for r, (c, sec) in zip(sample, res):
+            sec_class.setdefault((r["nx"], r["nv"]), []).append(sec / steps)
     core_sec = sum(np.mean(sec_class[key]) * len(classes[key]) for key in classes) * SWEEP_STEPS
     runs_per_s = len(runs) / (core_sec / min(cores, len(sample)))
+    wall = sum(walls)
     value = cells / wall
     return value, runs_per_s, min(cores, len(sample)), len(sample), steps, wall
 
@@ -734,15 +742,20 @@ def main_sweep(args, w, rank, world):
     if args.impl == "reference":
         if rank != 0:
             return
-        val, rps, cores, n, steps, wall = cpu_baseline_sweep(w, n_sample=max(36, args.steps), steps=360)
+        # each bench step: the 36 stratified runs advanced 36 oracle steps (~1 s
+        # on 16 cores), W untimed then K timed
+        val, rps, cores, n, osteps, wall = cpu_baseline_sweep(w, n_sample=36, steps=36, reps=args.steps,
+                                                              warmup=args.warmup)
         line = {"metric": "cell-updates/s", "value": val, "unit": "cell-updates/s", "n_gpus": args.gpus,
-                "steps": steps, "warmup": 0, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * wall / max(1, args.steps),
+                "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg, "impl": "reference",
                 "runs_per_s": rps,
                 "cpu_baseline": {"value": val, "unit": "cell-updates/s", "cores": cores, "kind": "port",
-                                 "sample": "%d sweep runs (stratified over the 9 shapes) x %d full oracle steps, "
-                                           "one process per core, %.1f s wall; runs/s extrapolated to 4096 "
-                                           "runs x 2000 steps" % (n, steps, wall)},
+                                 "sample": "each step: %d sweep runs (stratified over the 9 shapes) x %d full "
+                                           "oracle steps, one process per core; %d timed steps, %.1f s wall; "
+                                           "runs/s extrapolated to 4096 runs x 2000 steps"
+                                           % (n, osteps, args.steps, wall)},
                 "e2e": {"value": val, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
         return

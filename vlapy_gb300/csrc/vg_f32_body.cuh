@@ -184,14 +184,6 @@ __device__ __forceinline__ void kick_io(cx<float>* s, int t, float hk, float ea,
   block_fft_io<float, N, true, R, IO & 2>(s, t, tw, sync, io);
 }
 
-template <int N, int R, typename Sync = CtaSync>
-__device__ __forceinline__ void kick(cx<float>* s, int t, float hk, float ea, float eb,
-                                     const cx<float>* __restrict__ F0, const cx<float>* __restrict__ tw,
-                                     const Sync& sync = Sync()) {
-  cx<float> none[R];
-  kick_io<N, R, 0>(s, t, hk, ea, eb, F0, tw, sync, none);
-}
-
 // Per-row collision scalars from the row's raw moment sums (sum w g v^p,
 // p = 0, 1, 2), in double-float; each FP32 coefficient is rounded once:
 // out = {-vth/dv^2, 1 + 2 nudt vth/dv^2, vbar, nudt vth, nudt vbar}.

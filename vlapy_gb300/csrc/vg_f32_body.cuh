@@ -166,8 +166,9 @@ __device__ __forceinline__ void kick_rotate(cx<float>* s, int t, int G, Ang ha, 
   }
 }
 
-// the kick with the row pair in registers at one end (IO = 1: io holds the
-// pair's elements t + i G on entry and s need not; IO = 2: they end in io)
+// the kick with the row pair in registers at either end (IO bit 0: io holds
+// the pair's elements t + i G on entry and s need not; bit 1: they end in io;
+// the row pass uses IO = 3, both)
 template <int N, int R, int IO, typename Sync>
 __device__ __forceinline__ void kick_io(cx<float>* s, int t, float hk, float ea, float eb,
                                         const cx<float>* __restrict__ F0, const cx<float>* __restrict__ tw,

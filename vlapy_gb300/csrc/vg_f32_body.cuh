@@ -292,8 +292,9 @@ __device__ __forceinline__ void collide_pair(cx<float>* s, int t, const RowConst
 // memory (row32_group_bytes); macc: the CTA's mode accumulators [n_modes][N].
 // NPOW: how many power moments sum w g v^p (p < NPOW) the storage needs (6:
 // n, j, T, q, fv4, vN; the batched sweep's series need only p < 3); the
-// slots of the others are left unwritten.
-template <int N, int R, typename Sync = CtaSync, int NPOW = 6>
+// slots of the others are left unwritten.  KICK_ONLY: the leading half kick
+// of a step sequence alone (registers in from global memory, out to it).
+template <int N, int R, typename Sync = CtaSync, int NPOW = 6, bool KICK_ONLY = false>
 __device__ __forceinline__ void row_pair(const RowArgs& a, int pair, unsigned char* grp_base, cx<float>* macc,
                                          int P, int grp, int t, const Sync& sync = Sync()) {
   constexpr int G = N / R;
@@ -312,6 +313,23 @@ __device__ __forceinline__ void row_pair(const RowArgs& a, int pair, unsigned ch
   float* gbp = a.g + (size_t)rb * N;
   const bool kicks = a.hk1 != 0.f || a.hk2 != 0.f;
   const float ea = (kicks && va) ? a.e32[ra] : 0.f, eb = (kicks && vb) ? a.e32[rb] : 0.f;
+  if constexpr (KICK_ONLY) {
+    cx<float> io[R];
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+      const int n = t + i * G;
+      io[i] = {va ? ga[n] : 0.f, vb ? gbp[n] : 0.f};
+    }
+    if (a.hk1 != 0.f) kick_io<N, R, 3>(s, t, a.hk1, ea, eb, a.F0, a.tw, sync, io);
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+      const int n = t + i * G;
+      if (va) ga[n] = io[i].x;
+      if (vb) gbp[n] = io[i].y;
+    }
+    sync();
+    return;
+  }
   // both kicks run the same code (registers in, registers out), once each in
   // a loop the compiler keeps rolled, so the kernel holds one copy of the
   // kick's FFTs instead of four differently specialised ones (instruction-

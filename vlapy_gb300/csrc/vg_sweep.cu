@@ -288,9 +288,14 @@ struct SweepRowArgs {
   const cx<float>* tw;
 };
 
-// one (run, row-pair group) item per CTA; one kernel per nv class
-template <int N>
-__global__ void __launch_bounds__(sweep_row_block(N), sweep_row_min_blocks(N)) k_sweep_row(const SweepRunDev* __restrict__ runs,
+// CTAs per SM of the kick-only row kernel (the leading half kick of a call)
+#ifndef VG_KICK_MIN_BLOCKS
+#define VG_KICK_MIN_BLOCKS 4
+#endif
+// one (run, row-pair group) item per CTA; one kernel per nv class (KICK:
+// the leading half kick alone, a lighter instantiation)
+template <int N, bool KICK = false>
+__global__ void __launch_bounds__(sweep_row_block(N), KICK ? VG_KICK_MIN_BLOCKS : sweep_row_min_blocks(N)) k_sweep_row(const SweepRunDev* __restrict__ runs,
                                                               const int2* __restrict__ items, SweepRowArgs sa,
                                                               const SweepConsts* __restrict__ scp) {
   constexpr int R = sweep_row_radix(N);
@@ -323,8 +328,8 @@ __global__ void __launch_bounds__(sweep_row_block(N), sweep_row_min_blocks(N)) k
   a.rc = &scp->rc[r.cls];
   // the row-pair groups of a CTA are independent: each synchronises alone
   // the sweep's series use the power moments p = 0, 1, 2 only
-  row_pair<N, R, GroupSync, 3>(a, it.y * P + grp, smem_raw + (size_t)grp * row32_group_bytes(N, R), nullptr, P,
-                               grp, t, GroupSync::of(grp, G));
+  row_pair<N, R, GroupSync, 3, KICK>(a, it.y * P + grp, smem_raw + (size_t)grp * row32_group_bytes(N, R), nullptr,
+                                     P, grp, t, GroupSync::of(grp, G));
 }
 
 // e history row and the seven series of every run (one CTA per run, one
@@ -679,13 +684,14 @@ cudaError_t sweep_col_launch(vg_sweep* s, int c, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-template <int N>
+template <int N, bool KICK = false>
 cudaError_t sweep_row_launch(vg_sweep* s, int c, const SweepRowArgs& a, cudaStream_t st) {
   constexpr int R = sweep_row_radix(N);
   const size_t smem = (size_t)(sweep_row_block(N) / (N / R)) * row32_group_bytes(N, R);
-  cudaError_t err = ensure_smem((const void*)k_sweep_row<N>, smem);
+  cudaError_t err = ensure_smem((const void*)k_sweep_row<N, KICK>, smem);
   if (err != cudaSuccess) return err;
-  k_sweep_row<N><<<s->row_count[c], sweep_row_block(N), smem, st>>>(s->runs, s->row_items + s->row_first[c], a, s->consts);
+  k_sweep_row<N, KICK><<<s->row_count[c], sweep_row_block(N), smem, st>>>(s->runs, s->row_items + s->row_first[c],
+                                                                         a, s->consts);
   return cudaGetLastError();
 }
 
@@ -713,14 +719,22 @@ int sweep_sequence(vg_sweep* s, int nsteps, double* e_hist, double* s_hist, int 
                            const double dkv = s->consts_h.rc[cls].dkv;
                            ac.hk1 = (float)(-0.5 * dkv * dt1);
                            ac.hk2 = (float)(-0.5 * dkv * dt2);
+                           const bool kick = kind == SK_KICK;
+#define VG_ROW_CASE(NV)                                                                       \
+  case NV:                                                                                    \
+    err = kick ? sweep_row_launch<NV, true>(s, (int)c, ac, st) : sweep_row_launch<NV>(s, (int)c, ac, st); \
+    break;
                            switch (s->row_nv[c]) {
-                             case 64: err = sweep_row_launch<64>(s, (int)c, ac, st); break;
-                             case 128: err = sweep_row_launch<128>(s, (int)c, ac, st); break;
-                             case 256: err = sweep_row_launch<256>(s, (int)c, ac, st); break;
-                             case 512: err = sweep_row_launch<512>(s, (int)c, ac, st); break;
-                             case 1024: err = sweep_row_launch<1024>(s, (int)c, ac, st); break;
-                             default: err = sweep_row_launch<2048>(s, (int)c, ac, st); break;
+                             VG_ROW_CASE(64)
+                             VG_ROW_CASE(128)
+                             VG_ROW_CASE(256)
+                             VG_ROW_CASE(512)
+                             VG_ROW_CASE(1024)
+                             default: err = kick ? sweep_row_launch<2048, true>(s, (int)c, ac, st)
+                                                 : sweep_row_launch<2048>(s, (int)c, ac, st);
+                                      break;
                            }
+#undef VG_ROW_CASE
                            if (err != cudaSuccess) return err;
                          }
                          return cudaSuccess;

@@ -112,8 +112,10 @@ __global__ void __launch_bounds__(fft_threads<float>(NX)) k_field_f32(
 // row pass: kick / collide / measure / kick
 // ---------------------------------------------------------------------------
 
-template <int N, int R>
-__global__ void __launch_bounds__(row32_block(N, R)) k_row_f32(RowArgs a) {
+// KICK: a launch that only kicks (no collision, no moments, no trailing
+// kick), a lighter instantiation at two CTAs per SM
+template <int N, int R, bool KICK = false>
+__global__ void __launch_bounds__(row32_block(N, R), KICK ? 2 : 1) k_row_f32(RowArgs a) {
   constexpr int G = N / R;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int P = blockDim.x / G;
@@ -125,7 +127,7 @@ __global__ void __launch_bounds__(row32_block(N, R)) k_row_f32(RowArgs a) {
   const int npairs = (a.nx + 1) / 2;
   const int ngroups = (npairs + P - 1) / P;
   for (int pg = blockIdx.x; pg < ngroups; pg += gridDim.x)
-    row_pair<N, R>(a, pg * P + grp, smem_raw + (size_t)grp * grp_bytes, macc, P, grp, t);
+    row_pair<N, R, CtaSync, 6, KICK>(a, pg * P + grp, smem_raw + (size_t)grp * grp_bytes, macc, P, grp, t);
   if (nm > 0) {
     __syncthreads();
     for (int q = threadIdx.x; q < nm * N; q += blockDim.x)
@@ -252,8 +254,8 @@ cudaError_t field_n(const vg_plan& p, const double* driver, const FieldTime& ft,
   return cudaGetLastError();
 }
 
-template <int N>
-cudaError_t row_n(const vg_plan& p, RowArgs a, cudaStream_t s) {
+template <int N, bool KICK>
+cudaError_t row_nk(const vg_plan& p, RowArgs a, cudaStream_t s) {
   constexpr int R = row32_radix(N);
   constexpr int G = N / R;
   const int block = row32_block(N, R);
@@ -261,16 +263,22 @@ cudaError_t row_n(const vg_plan& p, RowArgs a, cudaStream_t s) {
   const int npairs = (p.nx + 1) / 2;
   const int ngroups = (npairs + P - 1) / P;
   const size_t smem = (size_t)P * row32_group_bytes(N, R) + (size_t)a.n_modes * N * sizeof(cx<float>);
-  cudaError_t err = ensure_smem((const void*)k_row_f32<N, R>, smem);
+  cudaError_t err = ensure_smem((const void*)k_row_f32<N, R, KICK>, smem);
   if (err != cudaSuccess) return err;
   int occ = 1;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_row_f32<N, R>, block, smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_row_f32<N, R, KICK>, block, smem);
   int grid = (occ > 0 ? occ : 1) * p.f32->n_sm;
   if (grid > p.f32->row_grid_max) grid = p.f32->row_grid_max;
   if (grid > ngroups) grid = ngroups;
-  k_row_f32<N, R><<<grid, block, smem, s>>>(a);
+  k_row_f32<N, R, KICK><<<grid, block, smem, s>>>(a);
   p.f32->mgrid = grid;
   return cudaGetLastError();
+}
+
+template <int N>
+cudaError_t row_n(const vg_plan& p, RowArgs a, cudaStream_t s) {
+  const bool kick_only = !a.fp && !a.want_mom && a.hk2 == 0.f;
+  return kick_only ? row_nk<N, true>(p, a, s) : row_nk<N, false>(p, a, s);
 }
 
 }  // namespace

@@ -23,26 +23,29 @@ __device__ __forceinline__ cx<T> cmul(cx<T> a, cx<T> b) {
 template <typename T>
 __device__ __forceinline__ cx<T> cscale(cx<T> a, T s) { return {a.x * s, a.y * s}; }
 
-// cos(2*pi*j/16), exact to double precision; folded at compile time when j is.
-__host__ __device__ constexpr double cos16(int j) {
-  return (j & 15) == 0 ? 1.0
-       : (j & 15) == 1 ? 0.92387953251128675613
-       : (j & 15) == 2 ? 0.70710678118654752440
-       : (j & 15) == 3 ? 0.38268343236508977173
-       : (j & 15) == 4 ? 0.0
-       : (j & 15) == 5 ? -0.38268343236508977173
-       : (j & 15) == 6 ? -0.70710678118654752440
-       : (j & 15) == 7 ? -0.92387953251128675613
-       : (j & 15) == 8 ? -1.0
-       : (j & 15) == 9 ? -0.92387953251128675613
-       : (j & 15) == 10 ? -0.70710678118654752440
-       : (j & 15) == 11 ? -0.38268343236508977173
-       : (j & 15) == 12 ? 0.0
-       : (j & 15) == 13 ? 0.38268343236508977173
-       : (j & 15) == 14 ? 0.70710678118654752440
-       : 0.92387953251128675613;
+// cos(2*pi*j/32), exact to double precision; folded at compile time when j is.
+// The first quadrant holds cos(pi q/16), q = 0..8; the others follow by symmetry.
+__host__ __device__ constexpr double cos32_q(int q) {
+  return q == 0 ? 1.0
+       : q == 1 ? 0.98078528040323044913
+       : q == 2 ? 0.92387953251128675613
+       : q == 3 ? 0.83146961230254523708
+       : q == 4 ? 0.70710678118654752440
+       : q == 5 ? 0.55557023301960222474
+       : q == 6 ? 0.38268343236508977173
+       : q == 7 ? 0.19509032201612826785
+       : 0.0;
 }
-__host__ __device__ constexpr double sin16(int j) { return cos16(j + 12); }
+__host__ __device__ constexpr double cos32(int j) {
+  return (j & 31) <= 8 ? cos32_q(j & 31)
+       : (j & 31) <= 16 ? -cos32_q(16 - (j & 31))
+       : (j & 31) <= 24 ? -cos32_q((j & 31) - 16)
+       : cos32_q(32 - (j & 31));
+}
+__host__ __device__ constexpr double sin32(int j) { return cos32(j + 24); }
+// the 16-point values are the even entries (identical doubles)
+__host__ __device__ constexpr double cos16(int j) { return cos32(2 * j); }
+__host__ __device__ constexpr double sin16(int j) { return sin32(2 * j); }
 
 // Exactly-rounded FP64 products and sums that nvcc may not contract into FMAs.
 // Used where the FP64 mode must reproduce NumPy's rounding bit for bit.

@@ -105,10 +105,11 @@ __device__ __forceinline__ int sp_step(int spbase, int base, int m) {
 // multiply by exp(-+2 pi i k / R), forward sign '-' unless INV
 template <typename T, int R, bool INV>
 __device__ __forceinline__ cx<T> rot_const(int k, cx<T> a) {
+  static_assert(R >= 1 && 32 % R == 0, "the rotation table covers radices dividing 32");
   if (k == 0) return a;
   if (4 * k == R) return INV ? cx<T>{-a.y, a.x} : cx<T>{a.y, -a.x};
-  const int j = (16 / R) * k;
-  const T c = (T)cos16(j), s = (T)sin16(j);
+  const int j = (32 / R) * k;
+  const T c = (T)cos32(j), s = (T)sin32(j);
   if (INV) return {a.x * c - a.y * s, a.x * s + a.y * c};
   return {a.x * c + a.y * s, a.y * c - a.x * s};
 }

@@ -76,8 +76,19 @@ __host__ __device__ constexpr int sweep_col_radix(int nx) {
   return (nx >= 32 && nx <= 256 && ((VG_SWEEP_COL_R16_MASK >> ilog2(nx)) & 1)) ? 16 : col32_radix(nx);
 }
 __host__ __device__ constexpr int sweep_col_w(int nx) { return 2 * (SWEEP_BLOCK / (nx / sweep_col_radix(nx))); }
+// nv classes (bit log2 nv) on radix-32 passes (32 elements a thread, a row
+// pair per warp; build-time knob).  nv = 1024 (two passes instead of 16 x
+// 16 x 4): row pass 1.333 ms against 1.365 ms on radix 16
+#ifndef VG_SWEEP_R32_MASK
+#define VG_SWEEP_R32_MASK 0x400
+#endif
+#ifndef VG_ROW_MIN_BLOCKS_R32
+#define VG_ROW_MIN_BLOCKS_R32 2
+#endif
 __host__ __device__ constexpr int sweep_row_radix(int nv) {
-  return (nv >= 64 && nv <= 4096 && ((VG_SWEEP_R16_MASK >> ilog2(nv)) & 1)) ? 16 : row32_radix(nv);
+  return (nv >= 256 && nv <= 4096 && ((VG_SWEEP_R32_MASK >> ilog2(nv)) & 1))   ? 32
+         : (nv >= 64 && nv <= 4096 && ((VG_SWEEP_R16_MASK >> ilog2(nv)) & 1)) ? 16
+                                                                               : row32_radix(nv);
 }
 // threads per CTA of the nv-class row kernel: SWEEP_ROW_BLOCK, or one group
 // where a group (nv / radix threads) is larger
@@ -91,7 +102,9 @@ __host__ __device__ constexpr int sweep_row_block(int nv) {
 #define VG_ROW_MIN_BLOCKS_R16 3
 #endif
 __host__ __device__ constexpr int sweep_row_min_blocks(int nv) {
-  return sweep_row_radix(nv) == 16 ? VG_ROW_MIN_BLOCKS_R16 : VG_ROW_MIN_BLOCKS;
+  return sweep_row_radix(nv) == 32   ? VG_ROW_MIN_BLOCKS_R32
+         : sweep_row_radix(nv) == 16 ? VG_ROW_MIN_BLOCKS_R16
+                                     : VG_ROW_MIN_BLOCKS;
 }
 
 struct SweepConsts {
@@ -288,14 +301,16 @@ struct SweepRowArgs {
   const cx<float>* tw;
 };
 
-// CTAs per SM of the kick-only row kernel (the leading half kick of a call)
+// CTAs per SM of the kick-only row kernel (the leading half kick of a call;
+// 2 for the radix-32 classes, whose 32 elements a thread need the registers)
 #ifndef VG_KICK_MIN_BLOCKS
 #define VG_KICK_MIN_BLOCKS 4
 #endif
 // one (run, row-pair group) item per CTA; one kernel per nv class (KICK:
 // the leading half kick alone, a lighter instantiation)
 template <int N, bool KICK = false>
-__global__ void __launch_bounds__(sweep_row_block(N), KICK ? VG_KICK_MIN_BLOCKS : sweep_row_min_blocks(N)) k_sweep_row(const SweepRunDev* __restrict__ runs,
+__global__ void __launch_bounds__(sweep_row_block(N), KICK ? (sweep_row_radix(N) == 32 ? 2 : VG_KICK_MIN_BLOCKS)
+                                                           : sweep_row_min_blocks(N)) k_sweep_row(const SweepRunDev* __restrict__ runs,
                                                               const int2* __restrict__ items, SweepRowArgs sa,
                                                               const SweepConsts* __restrict__ scp) {
   constexpr int R = sweep_row_radix(N);

@@ -113,6 +113,27 @@ int vg_edfdv(vg_plan* plan, void* f, const double* e, double dt, vg_stream strea
 /* x-advection f <- Re IFFT_x(exp(-i kx v dt) FFT_x f), in place.
  * Replaces step_vdfdx_exponential, vlapy/core/vlasov.py:83-110. */
 int vg_vdfdx(vg_plan* plan, void* f, double dt, vg_stream stream);
+/* The alternative v df/dx and e df/dv steppers, FP64 plans only, OUT OF
+ * PLACE (f_out must not overlap f_in), as the reference's closures return a
+ * new array.  The semi-Lagrangian steps evaluate the not-a-knot cubic spline
+ * of each line, extended by one periodic cell at each end, at the departure
+ * points (clamped to the extended range), which is what the reference's
+ * s = 0 bicubic spline gives there; they agree with it to rounding.  The
+ * first semi-Lagrangian call on a plan allocates the plan's spline scratch
+ * (cudaMalloc), so make it outside stream capture.
+ * vg_vdfdx_sl: f_out(x, v) = spline_x(f(., v))(x - v dt); nx >= 3, nv >= 4.
+ *   Replaces update_spatial_adv_sl, vlapy/core/vlasov.py:42-80. */
+int vg_vdfdx_sl(vg_plan* plan, const double* f_in, double* f_out, double dt, vg_stream stream);
+/* vg_edfdv_sl: f_out(x, v) = spline_v(f(x, .))(v - e(x) dt); nx >= 4, nv >= 3.
+ *   Replaces update_velocity_adv_sl, vlapy/core/vlasov.py:168-210. */
+int vg_edfdv_sl(vg_plan* plan, const double* f_in, const double* e, double* f_out, double dt,
+                vg_stream stream);
+/* vg_edfdv_cd2: f_out = f - (e * df/dv) * dt with numpy.gradient's
+ * second-order stencils (centred inside, one-sided at the ends), rounded as
+ * NumPy rounds them; nv >= 3.
+ *   Replaces step_edfdv_center_difference, vlapy/core/vlasov.py:143-165. */
+int vg_edfdv_cd2(vg_plan* plan, const double* f_in, const double* e, double* f_out, double dt,
+                 vg_stream stream);
 /* n(x) = trapz_v f.  Replaces compute_charges, vlapy/core/field.py:27-36. */
 int vg_charge_density(vg_plan* plan, const void* f, double* n, vg_stream stream);
 /* e = Re IFFT(i/kx FFT(rho)) for a net charge rho[nx] (nx any size).

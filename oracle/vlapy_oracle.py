@@ -20,7 +20,9 @@ Third-party arithmetic used by the reference and therefore here:
   * scipy.fft.fft / ifft (pocketfft, as shipped in SciPy; unpinned by the
     reference's setup.py:25-35),
   * numpy.trapezoid (numpy >= 2 name of numpy.trapz),
-  * scipy.special.wofz + scipy.optimize.newton (dispersion root).
+  * scipy.special.wofz + scipy.optimize.newton (dispersion root),
+  * scipy.interpolate.RectBivariateSpline and interp1d (the semi-Lagrangian
+    steppers; FITPACK inside SciPy).
 """
 
 from __future__ import annotations
@@ -29,7 +31,7 @@ import math
 
 import numpy as np
 from scipy import fft as sfft
-from scipy import optimize, special
+from scipy import interpolate, optimize, special
 
 
 def trapz(y, dx, axis=-1):
@@ -103,6 +105,46 @@ def edfdv_exponential(f, e, kv, dt):
 def edfdv_center_differenced(f, e, dv, dt):
     """Second-order centred E df/dv update (vlapy/core/vlasov.py:143-165)."""
     return f - e[:, None] * np.gradient(f, dv, axis=1, edge_order=2) * dt
+
+
+def padded_axis(ax):
+    """The axis with one node of spacing ax[2] - ax[1] added at each end
+    (vlapy/core/vlasov.py:27-39)."""
+    out = np.zeros(ax.size + 2)
+    out[1:-1] = ax
+    out[0] = ax[0] - (ax[2] - ax[1])
+    out[-1] = ax[-1] + (ax[2] - ax[1])
+    return out
+
+
+def vdfdx_sl(f, x, v, dt):
+    """Backward semi-Lagrangian x step (vlapy/core/vlasov.py:42-80): the s = 0
+    bicubic spline (scipy RectBivariateSpline, FITPACK) of f over the x axis
+    extended by one periodic row at each end, evaluated at (x - v dt, v)."""
+    xm, vm = np.meshgrid(x, v, indexing="ij")
+    f_pad = np.zeros((x.size + 2, v.size))
+    f_pad[1:-1, :] = f
+    f_pad[0, :] = f[-1, :]
+    f_pad[-1, :] = f[0, :]
+    spline = interpolate.RectBivariateSpline(padded_axis(x), v, f_pad)
+    return spline(xm.flatten() - vm.flatten() * dt, vm.flatten(), grid=False).reshape((x.size, v.size))
+
+
+def edfdv_sl(f, e, x, v, dt):
+    """Backward semi-Lagrangian v step (vlapy/core/vlasov.py:168-210): the
+    bicubic spline over the v axis extended by one periodic column at each
+    end, evaluated at (x, v - e(x) dt), with e taken through a cubic
+    interp1d at the grid nodes as the reference does."""
+    xm, vm = np.meshgrid(x, v, indexing="ij")
+    xm = xm.flatten()
+    vm = vm.flatten()
+    f_pad = np.zeros((x.size, v.size + 2))
+    f_pad[:, 1:-1] = f
+    f_pad[:, 0] = f[:, -1]
+    f_pad[:, -1] = f[:, 0]
+    em = interpolate.interp1d(x, e, kind="cubic")(xm)
+    spline = interpolate.RectBivariateSpline(x, padded_axis(v), f_pad)
+    return spline(xm, vm - em * dt, grid=False).reshape((x.size, v.size))
 
 
 # --------------------------------------------------------------------------
@@ -235,14 +277,24 @@ class Operators:
     """Bundle of the sub-operator closures a VP integrator composes
     (vlapy/core/step.py:29-67)."""
 
-    def __init__(self, x, v, kx, kv, inv_kx, dv, driver=None):
+    def __init__(self, x, v, kx, kv, inv_kx, dv, driver=None, vdfdx="exponential", edfdv="exponential"):
         self.x, self.v, self.kx, self.kv, self.inv_kx, self.dv = x, v, kx, kv, inv_kx, dv
         self.driver = driver if driver is not None else (lambda t: np.zeros(x.size))
+        # the stepper names of vlapy/core/vlasov.py:213-260
+        if vdfdx not in ("exponential", "sl") or edfdv not in ("exponential", "cd2", "sl"):
+            raise NotImplementedError((vdfdx, edfdv))
+        self.vdfdx_name, self.edfdv_name = vdfdx, edfdv
 
     def vdfdx(self, f, dt):
+        if self.vdfdx_name == "sl":
+            return vdfdx_sl(f, self.x, self.v, dt)
         return vdfdx_exponential(f, self.kx, self.v, dt)
 
     def edfdv(self, f, e, dt):
+        if self.edfdv_name == "sl":
+            return edfdv_sl(f, e, self.x, self.v, dt)
+        if self.edfdv_name == "cd2":
+            return edfdv_center_differenced(f, e, self.dv, dt)
         return edfdv_exponential(f, e, self.kv, dt)
 
     def field(self, t, f):
@@ -396,11 +448,12 @@ class OracleRun:
     order of vlapy/core/step.py:286-328, driven like vlapy/outer_loop.py:248-281."""
 
     def __init__(self, nx, nv, xmax, vmax, dt, nu=0.0, operator="dg",
-                 integrator="leapfrog", driver=None, xmin=0.0, n_modes=None):
+                 integrator="leapfrog", driver=None, xmin=0.0, n_modes=None, vdfdx="exponential",
+                 edfdv="exponential"):
         self.dx, self.x, self.kx, self.inv_kx = spatial_axis(xmin, xmax, nx)
         self.dv, self.v, self.kv = velocity_axis(vmax, nv)
         self.dt, self.nu, self.operator = dt, nu, operator
-        self.ops = Operators(self.x, self.v, self.kx, self.kv, self.inv_kx, self.dv, driver)
+        self.ops = Operators(self.x, self.v, self.kx, self.kv, self.inv_kx, self.dv, driver, vdfdx, edfdv)
         self.vp = INTEGRATORS[integrator]
         self.n_modes = n_modes
 

@@ -52,12 +52,12 @@ def _stuff(ref, nx, nv, xmax, vmax, dt, nu, driver_function, n_modes):
     }
 
 
-def _params(time="leapfrog", fp_type="dg", nu=0.0):
+def _params(time="leapfrog", fp_type="dg", nu=0.0, vdfdx="exponential", edfdv="exponential"):
     return {
         "nu": nu,
         "fokker-planck": {"type": fp_type, "solver": "batched_tridiagonal"},
-        "vlasov-poisson": {"time": time, "vdfdx": "exponential",
-                           "edfdv": "exponential", "poisson": "spectral"},
+        "vlasov-poisson": {"time": time, "vdfdx": vdfdx,
+                           "edfdv": edfdv, "poisson": "spectral"},
         "backend": {"core": "numpy"},
     }
 
@@ -81,7 +81,8 @@ def _sim_config(stuff, f, nt, n_modes):
 
 
 def run_steps(ref, name, nx, nv, xmax, vmax, dt, nu, f0, nsteps, time="leapfrog",
-              fp_type="dg", pulses=None, n_modes=2, snapshots=(1,)):
+              fp_type="dg", pulses=None, n_modes=2, snapshots=(1,), vdfdx="exponential",
+              edfdv="exponential"):
     """Run get_timestep (vlapy/core/step.py:286-328) from f0, e=0 and save the
     storage arrays plus f/e after the listed step counts."""
     dx, x, kx, inv_kx = ref.initializers.initialize_spatial_quantities(0.0, xmax, nx)
@@ -90,7 +91,7 @@ def run_steps(ref, name, nx, nv, xmax, vmax, dt, nu, f0, nsteps, time="leapfrog"
     else:
         drv = ref.field_driver.get_driver_function(x=x, pulse_dictionary=pulses, np=np)
     stuff = _stuff(ref, nx, nv, xmax, vmax, dt, nu, drv, n_modes)
-    ts = ref.step.get_timestep(_params(time, fp_type, nu), stuff)
+    ts = ref.step.get_timestep(_params(time, fp_type, nu, vdfdx, edfdv), stuff)
     t = dt * np.arange(nsteps)
     driver_array = np.array([drv(tt) for tt in t])
     sc = _sim_config(stuff, f0, nsteps, n_modes)
@@ -108,7 +109,8 @@ def run_steps(ref, name, nx, nv, xmax, vmax, dt, nu, f0, nsteps, time="leapfrog"
         out["series_" + k] = val
     out["stored_f"] = sc["stored_f"]
     meta = dict(nx=nx, nv=nv, xmax=xmax, vmax=vmax, dt=dt, nu=nu, nsteps=nsteps,
-                time=time, fp_type=fp_type, n_modes=-1 if n_modes is None else n_modes)
+                time=time, fp_type=fp_type, n_modes=-1 if n_modes is None else n_modes,
+                vdfdx=vdfdx, edfdv=edfdv)
     for k, val in meta.items():
         out["meta_" + k] = np.array(val)
     if pulses is not None:
@@ -117,6 +119,37 @@ def run_steps(ref, name, nx, nv, xmax, vmax, dt, nu, f0, nsteps, time="leapfrog"
             out["pulse_" + k] = np.array(p[k])
     np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
     print("wrote", name, sorted(out.keys())[:6], "...")
+
+
+def advect_alt(ref):
+    """The alternative steppers of vlapy/core/vlasov.py: semi-Lagrangian in x
+    and v (:42-80, :168-210) and the centred difference in v (:143-165), each
+    called directly, plus short runs of the full timestep that use them."""
+    I = ref.initializers
+    k, nx, nv, vmax = 0.3, 16, 64, 6.4
+    dx, x, kx, inv_kx = I.initialize_spatial_quantities(0.0, 2 * np.pi / k, nx)
+    dv, v, kv = I.initialize_velocity_quantities(vmax, nv)
+    rng = np.random.default_rng(11)
+    f = I.initialize_distribution(nx, nv, vmax) * (1.0 + 0.05 * np.cos(k * x))[:, None]
+    f = f + 1e-3 * rng.standard_normal((nx, nv))
+    e = 0.2 * np.sin(k * x) + 0.05
+    out = {"x": x, "v": v, "dv": np.array(dv), "f": f, "e": e}
+    vd_sl = ref.vlasov.get_vdfdx_sl(x=x, v=v)
+    ed_sl = ref.vlasov.get_edfdv_sl(x=x, v=v)
+    ed_cd2 = ref.vlasov.get_edfdv_center_differenced(dv=dv)
+    # dt = 2.5 moves the outer departure points past the padded grid (clamped)
+    for tag, dt in (("0p1", 0.1), ("2p5", 2.5)):
+        out["vdfdx_sl_" + tag] = vd_sl(f, dt)
+        out["edfdv_sl_" + tag] = ed_sl(f, e, dt)
+        out["edfdv_cd2_" + tag] = ed_cd2(f, e, dt)
+    np.savez_compressed(os.path.join(HERE, "advect_alt_16x64.npz"), **out)
+    print("wrote advect_alt_16x64")
+
+    f0 = I.initialize_distribution(nx, nv, vmax) * (1.0 + 1e-2 * np.cos(k * x))[:, None]
+    run_steps(ref, "step_sl_dg_16x64", nx, nv, 2 * np.pi / k, vmax, 0.1, 1e-3, f0, 3,
+              fp_type="dg", snapshots=(1, 3), vdfdx="sl", edfdv="sl")
+    run_steps(ref, "step_cd2_16x64", nx, nv, 2 * np.pi / k, vmax, 0.1, 0.0, f0, 3,
+              snapshots=(1, 3), edfdv="cd2")
 
 
 def main(root):
@@ -201,6 +234,14 @@ def main(root):
                         w_imag_table=np.array(ref.canosa.w_imag), root=roots)
     print("wrote dispersion")
 
+    advect_alt(ref)
+
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    # `make_golden.py ROOT` writes every fixture; `make_golden.py ROOT advect_alt`
+    # writes only those of the alternative steppers
+    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) > 2 and sys.argv[2] == "advect_alt":
+        advect_alt(_import_reference(root))
+    else:
+        main(root)

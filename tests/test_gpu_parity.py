@@ -195,14 +195,15 @@ def _golden_run(name):
              "dt": dt, "nu": nu, "driver_function": drv, "rules_to_store_f": rules,
              "f": d["f0"], "e": np.zeros(nx)}
     params = {"nu": nu, "fokker-planck": {"type": str(m["fp_type"]), "solver": "batched_tridiagonal"},
-              "vlasov-poisson": {"time": str(m["time"]), "vdfdx": "exponential", "edfdv": "exponential",
-                                 "poisson": "spectral"},
+              "vlasov-poisson": {"time": str(m["time"]), "vdfdx": str(m.get("vdfdx", "exponential")),
+                                 "edfdv": str(m.get("edfdv", "exponential")), "poisson": "spectral"},
               "backend": {"core": "gb300", "precision": "fp64"}}
     return d, m, stuff, params, rules, step, get_arrays_for_inner_loop
 
 
 @pytest.mark.parametrize("name", ["landau_32x512", "driven_dg_16x256", "driven_lb_16x256",
-                                  "integrator_pefrl_16x128", "integrator_h-sixth_16x128"])
+                                  "integrator_pefrl_16x128", "integrator_h-sixth_16x128",
+                                  "step_sl_dg_16x64", "step_cd2_16x64"])
 def test_timestep_matches_golden(name):
     d, m, stuff, params, rules, step, arrays = _golden_run(name)
     nsteps = int(m["nsteps"])
@@ -241,7 +242,12 @@ def _check_storage(sc, d, nsteps):
             np.testing.assert_allclose(got, ref, rtol=1e-11, atol=1e-12 * scale, err_msg=k)
     for k in vo.SERIES_KEYS:
         got = sc["series"][k].cpu().numpy()
-        np.testing.assert_allclose(got, d["series_" + k], rtol=1e-11, atol=1e-14, err_msg=k)
+        atol = 1e-14
+        if k == "mean_j":
+            # the mean current of a near-symmetric f is ~0: bound its error by the
+            # scale of the integrand, as for the odd moments above
+            atol = max(atol, 1e-12 * vo.trapz(np.abs(f0) * np.abs(v), dv, 1).mean())
+        np.testing.assert_allclose(got, d["series_" + k], rtol=1e-11, atol=atol, err_msg=k)
     sf = sc["stored_f"].cpu().numpy()
     ref = d["stored_f"]
     if sf.dtype == np.complex64:

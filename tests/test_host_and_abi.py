@@ -110,6 +110,19 @@ def test_unknown_names_raise_not_implemented():
     with pytest.raises(NotImplementedError):
         collisions.check_names({"type": "dg", "solver": "lu"})
     assert collisions.check_names({"type": "dg", "solver": "naive"}) == ("dg", "naive")
+    # stepper names are checked before any device plan is built: "cd2" exists
+    # only for e df/dv, and the alternatives run in the fp64 mode only
+    from vlapy_gb300.core import vlasov
+    stuff = {"nx": 8, "nv": 16, "dv": 0.8, "dt": 0.1}
+    with pytest.raises(NotImplementedError):
+        vlasov.get_vdfdx(stuff, "cd2")
+    with pytest.raises(NotImplementedError):
+        vlasov.get_edfdv(stuff, "upwind")
+    for name in ("sl", "cd2"):
+        with pytest.raises(NotImplementedError):
+            vlasov.get_edfdv(stuff, name, {"backend": {"precision": "fp32-deltaf"}})
+    with pytest.raises(NotImplementedError):
+        vlasov.get_vdfdx(stuff, "sl", {"backend": {"precision": "fp32-deltaf"}})
 
 
 def test_host_driver_matches_oracle():

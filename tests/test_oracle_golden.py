@@ -25,7 +25,8 @@ def _run_fixture(d, driver=None):
     n_modes = None if int(m["n_modes"]) < 0 else int(m["n_modes"])
     run = vo.OracleRun(nx, nv, float(m["xmax"]), float(m["vmax"]), float(m["dt"]),
                        nu=float(m["nu"]), operator=str(m["fp_type"]),
-                       integrator=str(m["time"]), driver=driver, n_modes=n_modes)
+                       integrator=str(m["time"]), driver=driver, n_modes=n_modes,
+                       vdfdx=str(m.get("vdfdx", "exponential")), edfdv=str(m.get("edfdv", "exponential")))
     st = vo.new_storage(d["f0"], np.zeros(nx), int(m["nsteps"]), n_modes)
     st["time_batch"] = d["time"]
     st["driver_array_batch"] = d["driver_array"]
@@ -42,7 +43,8 @@ def _pulse_driver(d, x):
 
 
 @pytest.mark.parametrize("name", ["landau_32x512", "driven_dg_16x256", "driven_lb_16x256",
-                                  "integrator_pefrl_16x128", "integrator_h-sixth_16x128"])
+                                  "integrator_pefrl_16x128", "integrator_h-sixth_16x128",
+                                  "step_sl_dg_16x64", "step_cd2_16x64"])
 def test_oracle_timestep_matches_reference(name):
     d = _load(name)
     driver = None
@@ -60,6 +62,22 @@ def test_oracle_timestep_matches_reference(name):
     for k in vo.SERIES_KEYS:
         np.testing.assert_array_equal(st["series"][k], d["series_" + k], err_msg=k)
     np.testing.assert_array_equal(st["stored_f"], d["stored_f"])
+
+
+@pytest.mark.parametrize("tag", ["0p1", "2p5"])
+def test_oracle_alternative_steppers_match_reference(tag):
+    """Semi-Lagrangian x and v steps and the centred-difference v step against
+    the reference's own closures (vlapy/core/vlasov.py:42-80, 143-210)."""
+    d = _load("advect_alt_16x64")
+    dx, x, kx, inv = vo.spatial_axis(0.0, 2 * np.pi / 0.3, 16)
+    dv, v, kv = vo.velocity_axis(6.4, 64)
+    np.testing.assert_array_equal(x, d["x"])
+    np.testing.assert_array_equal(v, d["v"])
+    dt = {"0p1": 0.1, "2p5": 2.5}[tag]
+    f, e = d["f"], d["e"]
+    np.testing.assert_array_equal(vo.vdfdx_sl(f, x, v, dt), d["vdfdx_sl_" + tag])
+    np.testing.assert_array_equal(vo.edfdv_sl(f, e, x, v, dt), d["edfdv_sl_" + tag])
+    np.testing.assert_array_equal(vo.edfdv_center_differenced(f, e, dv, dt), d["edfdv_cd2_" + tag])
 
 
 @pytest.mark.parametrize("op", ["lb", "dg"])

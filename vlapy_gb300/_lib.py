@@ -79,6 +79,9 @@ EXPORTS = {
     "vg_plan_destroy": (C.c_int, [C.c_void_p]),
     "vg_edfdv": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_void_p]),
     "vg_vdfdx": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_void_p]),
+    "vg_vdfdx_sl": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_void_p]),
+    "vg_edfdv_sl": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_void_p]),
+    "vg_edfdv_cd2": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_void_p]),
     "vg_charge_density": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "vg_poisson": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "vg_field_solve": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),

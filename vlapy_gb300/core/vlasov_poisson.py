@@ -93,8 +93,15 @@ def get_6th_order_integrator(vdfdx, edfdv, field_solve, dt, driver_function):
 
 def get_time_integrator(time_integrator_name, vdfdx, edfdv, field_solver, stuff_for_time_loop):
     """vlapy/core/vlasov_poisson.py:235-280."""
+    drv = stuff_for_time_loop.get("driver_function")
+    if drv is None:
+        # no driver: a zero field, as the fused step treats a missing driver
+        nx = int(stuff_for_time_loop["nx"])
+
+        def drv(t):
+            return torch.zeros(nx, dtype=torch.float64, device="cuda")
     args = dict(vdfdx=vdfdx, edfdv=edfdv, field_solve=field_solver, dt=stuff_for_time_loop["dt"],
-                driver_function=stuff_for_time_loop["driver_function"])
+                driver_function=drv)
     if time_integrator_name == "leapfrog":
         return get_full_leapfrog_step(**args)
     if time_integrator_name == "pefrl":

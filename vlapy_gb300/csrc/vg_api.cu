@@ -162,7 +162,7 @@ int dev_copy(T** dst, const T* src, size_t n, const char* what) {
 void free_plan(vg_plan* p) {
   if (!p) return;
   void* ptrs[] = {p->x, p->v, p->kx, p->kv, p->inv_kx, p->v_pow, p->f_bg, p->pulses, p->tw64, p->tw32,
-                  p->pw_v, p->pw_x, p->dens, p->mom, p->bb, p->rho, p->etmp};
+                  p->pw_v, p->pw_x, p->dens, p->mom, p->bb, p->rho, p->etmp, p->sl_m, p->sl_w};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   if (p->graph_cache) {
@@ -665,6 +665,62 @@ int vg_vdfdx(vg_plan* p, void* f, double dt, vg_stream stream) {
   if (p->f32) return cuda_status(launch_col_f32(*p, static_cast<float*>(f), dt, (cudaStream_t)stream), "vdfdx");
   VG_CHECK(require_fft_x(p));
   return cuda_status(launch_vdfdx_f64(*p, static_cast<double*>(f), dt, (cudaStream_t)stream), "vdfdx");
+}
+
+namespace {
+
+// checks shared by the out-of-place FP64 alternatives: an FP64 plan, distinct
+// non-null buffers, and the grid sizes the reference's own routine accepts
+int require_alt(const vg_plan* p, const void* fin, const void* fout, int min_nx, int min_nv, const char* what) {
+  VG_CHECK(require_plan(p));
+  if (p->f32) {
+    set_error(std::string(what) + " is implemented in the FP64 mode only");
+    return VG_ERR_UNSUPPORTED;
+  }
+  if (!fin || !fout) {
+    set_error(std::string(what) + ": null f_in or f_out");
+    return VG_ERR_ARG;
+  }
+  if (fin == fout) {
+    set_error(std::string(what) + " is out of place: f_out must not be f_in");
+    return VG_ERR_ARG;
+  }
+  if (p->nx < min_nx || p->nv < min_nv) {
+    set_error(std::string(what) + " needs nx >= " + std::to_string(min_nx) + " and nv >= " +
+              std::to_string(min_nv) + ", got " + std::to_string(p->nx) + " x " + std::to_string(p->nv));
+    return VG_ERR_ARG;
+  }
+  return VG_OK;
+}
+
+}  // namespace
+
+int vg_vdfdx_sl(vg_plan* p, const double* f_in, double* f_out, double dt, vg_stream stream) {
+  // x_pad needs x[2] (nx >= 3); the cubic spline along v needs nv >= 4
+  VG_CHECK(require_alt(p, f_in, f_out, 3, 4, "vdfdx sl"));
+  VG_CHECK(cuda_status(ensure_sl_scratch(*p), "sl scratch"));
+  return cuda_status(launch_vdfdx_sl_f64(*p, f_in, f_out, dt, (cudaStream_t)stream), "vdfdx sl");
+}
+
+int vg_edfdv_sl(vg_plan* p, const double* f_in, const double* e, double* f_out, double dt, vg_stream stream) {
+  // the cubic spline along x (and the cubic fit of e) needs nx >= 4; v_pad needs v[2]
+  VG_CHECK(require_alt(p, f_in, f_out, 4, 3, "edfdv sl"));
+  if (!e) {
+    set_error("edfdv sl: null e");
+    return VG_ERR_ARG;
+  }
+  VG_CHECK(cuda_status(ensure_sl_scratch(*p), "sl scratch"));
+  return cuda_status(launch_edfdv_sl_f64(*p, f_in, e, f_out, dt, (cudaStream_t)stream), "edfdv sl");
+}
+
+int vg_edfdv_cd2(vg_plan* p, const double* f_in, const double* e, double* f_out, double dt, vg_stream stream) {
+  // numpy.gradient with edge_order=2 needs three points along v
+  VG_CHECK(require_alt(p, f_in, f_out, 1, 3, "edfdv cd2"));
+  if (!e) {
+    set_error("edfdv cd2: null e");
+    return VG_ERR_ARG;
+  }
+  return cuda_status(launch_edfdv_cd2_f64(*p, f_in, e, f_out, dt, (cudaStream_t)stream), "edfdv cd2");
 }
 
 int vg_charge_density(vg_plan* p, const void* f, double* n, vg_stream stream) {

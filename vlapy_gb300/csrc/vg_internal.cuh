@@ -34,6 +34,10 @@ struct vg_plan {
   double* bb;     // [nx][nv] Thomas elimination scratch (FP64 mode)
   double* rho;    // [nx]
   double* etmp;   // [nx]
+  // semi-Lagrangian steps (allocated by their first call): spline second
+  // derivatives [(nx + 2) * (nv + 2)] and the Thomas pivot table [max(nx, nv)]
+  double* sl_m;
+  double* sl_w;
   // graph cache and per-kernel profiling state
   void* graph_cache;
   void* prof;
@@ -104,6 +108,13 @@ cudaError_t ensure_smem(const void* kernel, size_t bytes);
 // launchers (return cudaError_t of the launch)
 cudaError_t launch_edfdv_f64(const vg_plan& p, double* f, const double* e, double dt, cudaStream_t s);
 cudaError_t launch_vdfdx_f64(const vg_plan& p, double* f, double dt, cudaStream_t s);
+// alternative FP64 operators (vg_advect_alt_f64.cu); out of place
+cudaError_t ensure_sl_scratch(vg_plan& p);
+cudaError_t launch_vdfdx_sl_f64(const vg_plan& p, const double* fin, double* fout, double dt, cudaStream_t s);
+cudaError_t launch_edfdv_sl_f64(const vg_plan& p, const double* fin, const double* e, double* fout, double dt,
+                                cudaStream_t s);
+cudaError_t launch_edfdv_cd2_f64(const vg_plan& p, const double* fin, const double* e, double* fout, double dt,
+                                 cudaStream_t s);
 cudaError_t launch_row_moments_f64(const vg_plan& p, const double* f, const MomSpec& spec,
                                    double* out, int out_stride, cudaStream_t s);
 // e = [driver or pulses(t)] + Re IFFT(i/kx FFT(rho)), rho = 1 - dens (dens_is_density) or dens

@@ -119,6 +119,23 @@ class Plan:
         check(self._lib.vg_vdfdx(self._h, ptr(f), float(dt), stream_handle(stream)), "vdfdx")
         return f
 
+    def vdfdx_sl(self, f, out, dt, stream=None):
+        """Semi-Lagrangian x step of f into out (FP64 plans; out must not be f)."""
+        check(self._lib.vg_vdfdx_sl(self._h, ptr(f), ptr(out), float(dt), stream_handle(stream)), "vdfdx sl")
+        return out
+
+    def edfdv_sl(self, f, e, out, dt, stream=None):
+        """Semi-Lagrangian v step of f into out (FP64 plans; out must not be f)."""
+        check(self._lib.vg_edfdv_sl(self._h, ptr(f), ptr(e), ptr(out), float(dt), stream_handle(stream)),
+              "edfdv sl")
+        return out
+
+    def edfdv_cd2(self, f, e, out, dt, stream=None):
+        """Centred-difference v step of f into out (FP64 plans; out must not be f)."""
+        check(self._lib.vg_edfdv_cd2(self._h, ptr(f), ptr(e), ptr(out), float(dt), stream_handle(stream)),
+              "edfdv cd2")
+        return out
+
     def charge_density(self, f, out, stream=None):
         check(self._lib.vg_charge_density(self._h, ptr(f), ptr(out), stream_handle(stream)), "density")
         return out

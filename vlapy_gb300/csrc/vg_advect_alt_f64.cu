@@ -21,8 +21,10 @@
 //      elimination with a pivot table shared by all lines;
 //   2. evaluated on the cubic piece that holds each departure point, clamped
 //      to the padded range as FITPACK's evaluator (fpbisp) clamps it.
-// Step 1 runs one thread per line (a serial recurrence), step 2 one thread per
-// cell, coalesced along v.  FITPACK solves for B-spline coefficients by Givens
+// Step 1 runs one thread per v column for the x step (a serial recurrence over
+// nx; the columns are many) and one warp per x row for the v step (the rows are
+// few and long: a warp-parallel scan of the recurrence).  Step 2 runs one thread
+// per cell, coalesced along v.  FITPACK solves for B-spline coefficients by Givens
 // rotations instead, so the two agree to rounding, not bit for bit.
 //
 // Centred difference.  f - (e * df/dv) * dt with numpy.gradient's uniform
@@ -52,6 +54,9 @@ __device__ void sl_solve_line(const double* __restrict__ f, size_t lb, size_t es
   // forward elimination; a sliding window of three line values
   double ym = y(1), y0 = y(2);
   double d = 0.0;
+  // unrolled so that the loads of several iterations (independent of the
+  // recurrence) are in flight together
+#pragma unroll 8
   for (int q = 0; q < m; ++q) {
     const int k = q + 2;
     const double yp = y(k + 1);
@@ -64,8 +69,22 @@ __device__ void sl_solve_line(const double* __restrict__ f, size_t lb, size_t es
     y0 = yp;
   }
   // back substitution: M_{N-1} = d'_{m-1}, M_k = d'_k - w_k M_{k+1}
+  // The loads of M come in batches of eight ahead of the recurrence: a load
+  // after a store to the same array at a run-time stride is not reordered by
+  // the compiler, and each would otherwise wait on L2.
   double next = d;
-  for (int k = N - 2; k >= 2; --k) {
+  int k = N - 2;
+  for (; k >= 2 + 7; k -= 8) {
+    double dd[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) dd[u] = M[mb + (size_t)(k - u) * ms];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      next = dd[u] - w[k - u - 2] * next;
+      M[mb + (size_t)(k - u) * ms] = next;
+    }
+  }
+  for (; k >= 2; --k) {
     const size_t at = mb + (size_t)k * ms;
     next = M[at] - w[k - 2] * next;
     M[at] = next;
@@ -84,12 +103,87 @@ __global__ void k_sl_solve_x(const double* __restrict__ f, double* __restrict__ 
   sl_solve_line(f, (size_t)j, (size_t)nv, M, (size_t)j, (size_t)nv, nx, x[2] - x[1], w);
 }
 
-// v step: one thread per x row; M[nx][nv + 2]
+// v step: one WARP per x row; M[nx][nv + 2].  The rows are few (nx) and long
+// (nv), so the serial recurrences are split: lane l owns the unknowns
+// q in [l L, (l + 1) L), L = ceil(m / 32).  Each Thomas sweep is a chain of
+// affine maps (forward d_q = -w_q d_{q-1} + w_q r_q; backward
+// x_q = -w_q x_{q+1} + d_q), so a lane composes its chunk's map, a 5-step
+// shuffle scan composes the maps of the lanes before it (after it, for the
+// backward sweep), and the lane replays its chunk from the value that gives.
+// The maps contract (|w_q| < 0.27), so the reassociation changes only rounding.
 __global__ void k_sl_solve_v(const double* __restrict__ f, double* __restrict__ M, int nx, int nv,
                              const double* __restrict__ v, const double* __restrict__ w) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nx) return;
-  sl_solve_line(f, (size_t)i * nv, 1, M, (size_t)i * (nv + 2), 1, nv, v[2] - v[1], w);
+  constexpr unsigned FULL = 0xffffffffu;
+  const int row = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (row >= nx) return;  // uniform per warp
+  const int N = nv, m = N - 2;
+  const double* y = f + (size_t)row * nv;   // y(k) = y[pad_src(k, N)]
+  double* Mr = M + (size_t)row * (nv + 2);
+  const double h = v[2] - v[1];
+  const double inv_h2 = 1.0 / (h * h);
+  const double c6 = 6.0 * inv_h2;
+  const double m1 = ((y[N - 1] + y[1]) - 2.0 * y[0]) * inv_h2;            // M_1
+  const double mn = ((y[N - 2] + y[0]) - 2.0 * y[N - 1]) * inv_h2;        // M_{n-2}
+  const int L = (m + 31) >> 5;
+  const int q0 = min(lane * L, m), q1 = min(q0 + L, m);
+  // right-hand side of unknown q (padded node k = q + 2, line values k - 2 .. k)
+  auto rhs = [&](int q) {
+    double r = ((y[q] + y[q + 2]) - 2.0 * y[q + 1]) * c6;
+    if (q == 0) r -= m1;
+    if (q == m - 1) r -= mn;
+    return r;
+  };
+  // forward sweep
+  double A = 1.0, B = 0.0;
+  for (int q = q0; q < q1; ++q) {
+    const double wq = w[q];
+    A = -wq * A;
+    B = (rhs(q) - B) * wq;
+  }
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const double Ap = __shfl_up_sync(FULL, A, off), Bp = __shfl_up_sync(FULL, B, off);
+    if (lane >= off) {
+      B = A * Bp + B;
+      A = A * Ap;
+    }
+  }
+  double d = __shfl_up_sync(FULL, B, 1);
+  if (lane == 0) d = 0.0;
+  for (int q = q0; q < q1; ++q) {
+    d = (rhs(q) - d) * w[q];
+    Mr[q + 2] = d;
+  }
+  // backward sweep, from x_m = 0; each lane reads back only its own chunk
+  A = 1.0;
+  B = 0.0;
+  for (int q = q1 - 1; q >= q0; --q) {
+    const double wq = w[q];
+    A = -wq * A;
+    B = Mr[q + 2] - wq * B;
+  }
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const double Ap = __shfl_down_sync(FULL, A, off), Bp = __shfl_down_sync(FULL, B, off);
+    if (lane + off < 32) {
+      B = A * Bp + B;
+      A = A * Ap;
+    }
+  }
+  double x = __shfl_down_sync(FULL, B, 1);
+  if (lane == 31) x = 0.0;
+  for (int q = q1 - 1; q >= q0; --q) {
+    x = Mr[q + 2] - w[q] * x;
+    Mr[q + 2] = x;
+  }
+  __syncwarp();  // M_2 and M_{N-1} come from other lanes' chunks
+  if (lane == 0) {
+    Mr[1] = m1;
+    Mr[N] = mn;
+    Mr[0] = 2.0 * m1 - Mr[2];
+    Mr[N + 1] = 2.0 * mn - Mr[N - 1];
+  }
 }
 
 // Evaluation at the departure points: x_i - v_j dt (ALONG_X) or v_j - e_i dt.
@@ -194,7 +288,7 @@ cudaError_t launch_vdfdx_sl_f64(const vg_plan& p, const double* fin, double* fou
 
 cudaError_t launch_edfdv_sl_f64(const vg_plan& p, const double* fin, const double* e, double* fout, double dt,
                                 cudaStream_t s) {
-  k_sl_solve_v<<<div_up(p.nx, 64), 64, 0, s>>>(fin, p.sl_m, p.nx, p.nv, p.v, p.sl_w);
+  k_sl_solve_v<<<div_up(p.nx, 4), 128, 0, s>>>(fin, p.sl_m, p.nx, p.nv, p.v, p.sl_w);  // a warp per row
   cudaError_t err = cudaGetLastError();
   if (err != cudaSuccess) return err;
   k_sl_eval<false><<<cell_blocks((size_t)p.nx * p.nv), 256, 0, s>>>(fin, fout, p.sl_m, p.nx, p.nv, p.x, p.v,

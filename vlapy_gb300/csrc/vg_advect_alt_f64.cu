@@ -278,7 +278,8 @@ cudaError_t ensure_sl_scratch(vg_plan& p) {
 }
 
 cudaError_t launch_vdfdx_sl_f64(const vg_plan& p, const double* fin, double* fout, double dt, cudaStream_t s) {
-  k_sl_solve_x<<<div_up(p.nv, 128), 128, 0, s>>>(fin, p.sl_m, p.nx, p.nv, p.x, p.sl_w);
+  // one-warp CTAs (each column's chain is bound by its warp's FP64 issue, not by the CTA shape)
+  k_sl_solve_x<<<div_up(p.nv, 32), 32, 0, s>>>(fin, p.sl_m, p.nx, p.nv, p.x, p.sl_w);
   cudaError_t err = cudaGetLastError();
   if (err != cudaSuccess) return err;
   k_sl_eval<true><<<cell_blocks((size_t)p.nx * p.nv), 256, 0, s>>>(fin, fout, p.sl_m, p.nx, p.nv, p.x, p.v,

@@ -103,6 +103,23 @@ def test_mode_count_follows_reference_rule_dict():
         n_modes_of({"space": ["x"]})
 
 
+def test_stepper_arguments_checked_on_host():
+    """The out-of-place steppers refuse a wrong dtype or shape before any pointer
+    reaches a kernel."""
+    import torch
+    from vlapy_gb300.plan import check_f64
+    t = torch.zeros((4, 8), dtype=torch.float64)
+    assert check_f64(t, (4, 8), "f") is t
+    with pytest.raises(ValueError):
+        check_f64(t.float(), (4, 8), "f")
+    with pytest.raises(ValueError):
+        check_f64(t, (4, 9), "f")
+    with pytest.raises(ValueError):
+        check_f64(torch.zeros(5, dtype=torch.float64), (4,), "e")
+    with pytest.raises(TypeError):
+        check_f64(np.zeros((4, 8)), (4, 8), "f")
+
+
 def test_unknown_names_raise_not_implemented():
     from vlapy_gb300.core import collisions
     with pytest.raises(NotImplementedError):

@@ -41,6 +41,17 @@ def ptr(t) -> int:
     return int(t.data_ptr())
 
 
+def check_f64(t, shape, name):
+    """Refuse a tensor that is not float64 of the given shape before its pointer
+    reaches a kernel (the out-of-place steppers index nx * nv cells of it)."""
+    if not isinstance(t, torch.Tensor):
+        raise TypeError("%s: expected a tensor, got %r" % (name, type(t)))
+    if t.dtype != torch.float64 or tuple(t.shape) != tuple(shape):
+        raise ValueError("%s: expected float64 of shape %s, got %s of shape %s"
+                         % (name, tuple(shape), t.dtype, tuple(t.shape)))
+    return t
+
+
 def require_cuda():
     if not torch.cuda.is_available():
         raise RuntimeError("vlapy_gb300 needs a CUDA device (GB300); none is available")
@@ -119,19 +130,31 @@ class Plan:
         check(self._lib.vg_vdfdx(self._h, ptr(f), float(dt), stream_handle(stream)), "vdfdx")
         return f
 
+    def _alt_args(self, name, f, out, e=None):
+        if self.precision != "fp64":
+            raise NotImplementedError(name + " is implemented in the fp64 precision mode only")
+        grid = (self.nx, self.nv)
+        check_f64(f, grid, name + " f")
+        check_f64(out, grid, name + " out")
+        if e is not None:
+            check_f64(e, (self.nx,), name + " e")
+
     def vdfdx_sl(self, f, out, dt, stream=None):
         """Semi-Lagrangian x step of f into out (FP64 plans; out must not be f)."""
+        self._alt_args("vdfdx sl", f, out)
         check(self._lib.vg_vdfdx_sl(self._h, ptr(f), ptr(out), float(dt), stream_handle(stream)), "vdfdx sl")
         return out
 
     def edfdv_sl(self, f, e, out, dt, stream=None):
         """Semi-Lagrangian v step of f into out (FP64 plans; out must not be f)."""
+        self._alt_args("edfdv sl", f, out, e)
         check(self._lib.vg_edfdv_sl(self._h, ptr(f), ptr(e), ptr(out), float(dt), stream_handle(stream)),
               "edfdv sl")
         return out
 
     def edfdv_cd2(self, f, e, out, dt, stream=None):
         """Centred-difference v step of f into out (FP64 plans; out must not be f)."""
+        self._alt_args("edfdv cd2", f, out, e)
         check(self._lib.vg_edfdv_cd2(self._h, ptr(f), ptr(e), ptr(out), float(dt), stream_handle(stream)),
               "edfdv cd2")
         return out

@@ -120,6 +120,37 @@ def test_stepper_arguments_checked_on_host():
         check_f64(np.zeros((4, 8)), (4, 8), "f")
 
 
+@pytest.mark.parametrize("name", ["leapfrog", "pefrl", "h-sixth"])
+def test_composed_integrators_follow_the_oracle(name, monkeypatch):
+    """The composed integrators of vlapy_gb300.core.vlasov_poisson (used with the
+    semi-Lagrangian and centred-difference steppers, and with a Python driver
+    closure) call the sub-operators in the reference's order with the
+    reference's sub-step sizes and driver times.  Fed the oracle's NumPy
+    closures they reproduce the oracle's integrators bit for bit."""
+    from oracle import vlapy_oracle as vo
+    from vlapy_gb300.core import vlasov_poisson as vp
+    monkeypatch.setattr(vp, "as_device", np.asarray)  # host arrays stand in for device buffers
+    k, nx, nv, dt, t = 0.3, 16, 64, 0.1, 1.7
+    dx, x, kx, inv = vo.spatial_axis(0.0, 2 * np.pi / k, nx)
+    dv, v, kv = vo.velocity_axis(6.4, nv)
+    pulses = {"p": {"k0": k, "w0": 1.16, "a0": 1e-2, "t_L": 0.5, "t_R": 5.0, "t_wL": 0.5, "t_wR": 0.5}}
+
+    def drv(tt):
+        return vo.driver_tanh(x, pulses, tt)
+
+    ops = vo.Operators(x, v, kx, kv, inv, dv, drv, vdfdx="sl", edfdv="cd2")
+    step = vp.get_time_integrator(
+        name, lambda f, dt: ops.vdfdx(f, dt), lambda f, e, dt: ops.edfdv(f, e, dt),
+        lambda driver_field, f: vo.total_field(driver_field, f, dv, inv),
+        {"dt": dt, "driver_function": drv, "nx": nx})
+    f0 = vo.maxwellian(nx, nv, 6.4) * (1.0 + 1e-2 * np.cos(k * x))[:, None]
+    e0 = 1e-3 * np.sin(k * x)
+    e1, f1 = step(e=e0, f=f0, t=t)
+    e2, f2 = vo.INTEGRATORS[name](ops, e0, f0, t, dt)
+    np.testing.assert_array_equal(f1, f2)
+    np.testing.assert_array_equal(e1, e2)
+
+
 def test_unknown_names_raise_not_implemented():
     from vlapy_gb300.core import collisions
     with pytest.raises(NotImplementedError):

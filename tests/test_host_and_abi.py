@@ -44,6 +44,40 @@ def test_library_exports_every_header_symbol(lib_path):
     assert lib.vg_version() >= 1
 
 
+C_CONSUMER = r"""
+#include <stdio.h>
+#include "vlagpu.h"
+int main(void) {
+  vg_plan* p = 0;
+  int v = vg_version();
+  int st = vg_plan_create(NULL, &p);
+  printf("%d %d %s\n", v, st, vg_last_error());
+  return (v >= 1 && st == VG_ERR_ARG && p == NULL) ? 0 : 1;
+}
+"""
+
+
+@pytest.mark.parametrize("compiler,std", [("gcc", "-std=c99"), ("g++", "-std=c++17")])
+def test_header_serves_a_c_consumer(lib_path, tmp_path, compiler, std):
+    """What a cgo / JNI / plain C binding does first: compile against the header
+    with warnings as errors, link libvlagpu.so, and make the calls that need no
+    GPU (the version, and a plan refused for a null descriptor)."""
+    import subprocess
+    if shutil.which(compiler) is None:
+        pytest.skip(compiler + " not installed")
+    src = tmp_path / ("consumer.c" if compiler == "gcc" else "consumer.cpp")
+    src.write_text(C_CONSUMER)
+    exe = str(tmp_path / "consumer")
+    libdir = os.path.dirname(lib_path)
+    cmd = [compiler, std, "-Wall", "-Wextra", "-Werror", "-pedantic", str(src), "-I",
+           os.path.join(ROOT, "include"), "-L", libdir, "-lvlagpu", "-Wl,-rpath," + libdir, "-o", exe]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([exe], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "null descriptor" in r.stdout
+
+
 def test_binding_covers_header(lib_path):
     from vlapy_gb300 import _lib
     assert set(header_functions()) <= set(_lib.EXPORTS)

@@ -107,3 +107,49 @@ def test_relative_l2():
     assert AT.relative_l2([1.0, 2.0], [1.0, 2.0]) == 0.0
     assert AT.relative_l2([0.0], [0.0]) == 0.0
     assert AT.relative_l2([1.0, 0.0], [0.0, 1.0]) == pytest.approx(2 ** 0.5)
+
+
+def test_measurer_orchestration(tmp_path, monkeypatch):
+    """Measurer with the build stubbed and a stand-in interpreter for the probe
+    process: the first configuration becomes the reference, a candidate whose
+    fields differ, whose probe fails or whose build fails is dropped, and a
+    matching one returns its time."""
+    import stat
+    import sys
+
+    import numpy as np
+
+    builds = []
+
+    def fake_build(tuning=None, lib_path=None, build_dir=None, **kw):
+        if tuning.get("VG_SWEEP_ROW_BLOCK") == 64:
+            raise RuntimeError("nvcc failed")
+        os.makedirs(os.path.dirname(lib_path), exist_ok=True)
+        open(lib_path, "w").write(json.dumps(tuning))     # the probe reads the tuning back
+        builds.append(dict(tuning))
+        return lib_path
+
+    monkeypatch.setattr(AT.B, "build", fake_build)
+    probe = tmp_path / "fake_python"
+    probe.write_text(
+        "#!%s\n"
+        "import json, sys, numpy as np\n"
+        "a = sys.argv[1:]\n"
+        "tuning = json.load(open(a[a.index('--lib') + 1]))\n"
+        "if tuning.get('VG_COL_MIN_BLOCKS_R16') == 2: sys.exit(3)\n"
+        "e = np.ones((4, 8)) * (1.5 if tuning.get('VG_SWEEP_R32_MASK') == 0 else 1.0)\n"
+        "np.savez(a[a.index('--out') + 1], ms=np.float64(2.0 - tuning.get('VG_ROW_MIN_BLOCKS_R16', 3) / 10), e=e)\n"
+        % sys.executable)
+    probe.chmod(probe.stat().st_mode | stat.S_IEXEC)
+    meas = AT.Measurer(16, 1, 4, 3, str(tmp_path), python=str(probe))
+    base = {"VG_SWEEP_R32_MASK": 0x400, "VG_ROW_MIN_BLOCKS_R16": 3, "VG_COL_MIN_BLOCKS_R16": 3,
+            "VG_SWEEP_ROW_BLOCK": 256}
+    assert meas(base) == pytest.approx(1.7)
+    assert meas(dict(base, VG_ROW_MIN_BLOCKS_R16=4)) == pytest.approx(1.6)
+    with pytest.raises(AT.CandidateError, match="differ"):
+        meas(dict(base, VG_SWEEP_R32_MASK=0))
+    with pytest.raises(AT.CandidateError, match="probe failed"):
+        meas(dict(base, VG_COL_MIN_BLOCKS_R16=2))
+    with pytest.raises(AT.CandidateError, match="build failed"):
+        meas(dict(base, VG_SWEEP_ROW_BLOCK=64))
+    assert len(builds) == 4

@@ -2,7 +2,7 @@
 
 Run in a container where the reference source tree is available:
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py REFERENCE_ROOT [advect_alt|driven_sin2]
 
 The reference is pure Python; it is imported unmodified with two shims:
 ``np.trapz = np.trapezoid`` (NumPy 2 removed trapz) and a stub ``mlflow``
@@ -13,6 +13,7 @@ never read the reference tree; they read these fixtures.
 
 from __future__ import annotations
 
+import math
 import os
 import sys
 import types
@@ -82,11 +83,16 @@ def _sim_config(stuff, f, nt, n_modes):
 
 def run_steps(ref, name, nx, nv, xmax, vmax, dt, nu, f0, nsteps, time="leapfrog",
               fp_type="dg", pulses=None, n_modes=2, snapshots=(1,), vdfdx="exponential",
-              edfdv="exponential"):
+              edfdv="exponential", driver=None, keep_every=1):
     """Run get_timestep (vlapy/core/step.py:286-328) from f0, e=0 and save the
-    storage arrays plus f/e after the listed step counts."""
+    storage arrays plus f/e after the listed step counts.  driver: a closure
+    of x returning the driver function, in place of the reference's tanh
+    pulses; keep_every > 1 keeps only every keep_every-th row of the stored
+    fields (except e) and of stored_f, to keep a long run's fixture small."""
     dx, x, kx, inv_kx = ref.initializers.initialize_spatial_quantities(0.0, xmax, nx)
-    if pulses is None:
+    if driver is not None:
+        drv = driver(x)
+    elif pulses is None:
         drv = lambda t: np.zeros(nx)  # noqa: E731
     else:
         drv = ref.field_driver.get_driver_function(x=x, pulse_dictionary=pulses, np=np)
@@ -104,19 +110,20 @@ def run_steps(ref, name, nx, nv, xmax, vmax, dt, nu, f0, nsteps, time="leapfrog"
             out["f_%d" % (i + 1)] = np.array(sc["f"])
             out["e_%d" % (i + 1)] = np.array(sc["e"])
     for k, val in sc["fields"].items():
-        out["fields_" + k] = val
+        out["fields_" + k] = val if k == "e" else val[::keep_every]
     for k, val in sc["series"].items():
         out["series_" + k] = val
-    out["stored_f"] = sc["stored_f"]
+    out["stored_f"] = sc["stored_f"][::keep_every]
     meta = dict(nx=nx, nv=nv, xmax=xmax, vmax=vmax, dt=dt, nu=nu, nsteps=nsteps,
                 time=time, fp_type=fp_type, n_modes=-1 if n_modes is None else n_modes,
-                vdfdx=vdfdx, edfdv=edfdv)
+                vdfdx=vdfdx, edfdv=edfdv, keep_every=keep_every)
     for k, val in meta.items():
         out["meta_" + k] = np.array(val)
     if pulses is not None:
         p = list(pulses.values())[0]
         for k in ("k0", "w0", "a0", "t_L", "t_R", "t_wL", "t_wR"):
             out["pulse_" + k] = np.array(p[k])
+        out["pulse_envelope"] = np.array(p.get("envelope", "tanh"))
     np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
     print("wrote", name, sorted(out.keys())[:6], "...")
 
@@ -150,6 +157,34 @@ def advect_alt(ref):
               fp_type="dg", snapshots=(1, 3), vdfdx="sl", edfdv="sl")
     run_steps(ref, "step_cd2_16x64", nx, nv, 2 * np.pi / k, vmax, 0.1, 0.0, f0, 3,
               snapshots=(1, 3), edfdv="cd2")
+
+
+def driven_sin2(ref):
+    """The driven electron-plasma-wave workload on its own grid: 64 x 1024,
+    k = 0.3, vmax = 6.4, Maxwellian start, Dougherty collisions nu = 1e-3,
+    dt = 0.1, and the external field a0 sin(k x - w t) sin^2(pi t / 100) on
+    [0, 100] (zero after), a0 = 1e-2, w the real part of the reference's
+    dispersion root.  The reference has no such envelope; its step calls any
+    driver closure (vlapy/core/vlasov_poisson.py:55), so the closure is
+    written here.  150 steps (t up to 15, the envelope rising); f at the
+    last step, e at every step, the other fields and stored_f every 10th."""
+    I = ref.initializers
+    k, nx, nv, vmax, a0, t_end = 0.3, 64, 1024, 6.4, 1e-2, 100.0
+    w = float(np.real(ref.z_function.get_roots_to_electrostatic_dispersion(1.0, 1.0, k)))
+
+    def closure(x):
+        def drv(t):
+            if t < 0.0 or t > t_end:
+                return np.zeros(x.size)
+            s = math.sin(math.pi * t / t_end)
+            return (a0 * (s * s)) * np.sin(k * x - w * t)
+        return drv
+
+    pulses = {"p": {"k0": k, "w0": w, "a0": a0, "t_L": 0.0, "t_R": t_end, "t_wL": 1.0, "t_wR": 1.0,
+                    "envelope": "sin2"}}
+    f0 = I.initialize_distribution(nx, nv, vmax)
+    run_steps(ref, "driven_sin2_dg_64x1024", nx, nv, 2 * np.pi / k, vmax, 0.1, 1e-3, f0, 150,
+              fp_type="dg", pulses=pulses, snapshots=(150,), driver=closure, keep_every=10)
 
 
 def main(root):
@@ -235,13 +270,19 @@ def main(root):
     print("wrote dispersion")
 
     advect_alt(ref)
+    driven_sin2(ref)
 
 
 if __name__ == "__main__":
     # `make_golden.py ROOT` writes every fixture; `make_golden.py ROOT advect_alt`
-    # writes only those of the alternative steppers
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    # (or `driven_sin2`) writes only those of the alternative steppers (or of
+    # the sin^2-driven wave)
+    if len(sys.argv) < 2:
+        sys.exit("usage: make_golden.py REFERENCE_ROOT [advect_alt|driven_sin2]")
+    root = sys.argv[1]
     if len(sys.argv) > 2 and sys.argv[2] == "advect_alt":
         advect_alt(_import_reference(root))
+    elif len(sys.argv) > 2 and sys.argv[2] == "driven_sin2":
+        driven_sin2(_import_reference(root))
     else:
         main(root)

@@ -230,7 +230,25 @@ def test_initializers_match_oracle():
     for a, b in zip(I.initialize_spatial_quantities(0.0, 20.0, 32), vo.spatial_axis(0.0, 20.0, 32)):
         np.testing.assert_array_equal(a, b)
     p = I.specify_epw_params_to_dict(0.3, I.make_default_params_dictionary())
-    np.testing.assert_allclose(p["w_epw"] + 1j * p["nu_ld"], vo.epw_root(0.3), rtol=1e-14)
+    np.testing.assert_allclose(p["w_epw"] + 1j * p["nu_ld"], vo.epw_root(0.3), rtol=1e-12)
+
+
+def test_dispersion_root_matches_reference_roots():
+    """The Newton root of the set-up module against the roots the reference's
+    own solver wrote (vlapy/diagnostics/z_function.py:26-50, fixture
+    dispersion.npz) and the Canosa table of tests/test_zsolver.py."""
+    import os
+    from oracle import vlapy_oracle as vo
+    from vlapy_gb300 import dispersion
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "dispersion.npz"))
+    for k0, wr, wi, r in zip(d["k0"], d["w_real_table"], d["w_imag_table"], d["root"]):
+        got = dispersion.get_roots_to_electrostatic_dispersion(1.0, 1.0, float(k0))
+        # the reference's secant iteration stops at a 1.5e-8 tolerance
+        np.testing.assert_allclose(got, r, rtol=1e-8)
+        np.testing.assert_almost_equal(got, wr + 1j * wi, decimal=4)
+    # another starting frequency converges to the same root
+    g = dispersion.get_roots_to_electrostatic_dispersion(1.0, 1.0, 0.3, initial_root_guess=1.1)
+    np.testing.assert_allclose(g, vo.epw_root(0.3), rtol=1e-8)
 
 
 def test_corrector_layout_and_restriction():
@@ -299,3 +317,47 @@ def test_damping_fit_matches_oracle_fit():
     e = np.random.default_rng(0).standard_normal((50, 16))
     np.testing.assert_array_equal(mode_amplitude(e), vo.mode_amplitude(e))
     assert np.isnan(damping_fit(t[:20], amp[:20])[0])
+
+
+@pytest.mark.parametrize("rules", [{"time": "first-last", "space": ["k0", "k1"]},
+                                   {"time": "all", "space": "all"}])
+def test_storage_batch_layout_matches_reference(rules):
+    """The sim_config layout of this backend goes through the conversion of
+    StorageManager.batch_update (vlapy/storage.py:177-315): host arrays with
+    the reference's keys, shapes and dtypes (the oracle's restatement of
+    vlapy/outer_loop.py:149-215), each fitting the coordinates batch_update
+    attaches.  Built in host memory here; the GPU tests run the same check on
+    a sim_config that the inner loop has filled."""
+    import torch
+    from oracle import vlapy_oracle as vo
+    from vlapy_gb300 import initializers as I, outer_loop, storage
+    nx, nv, nt = 16, 64, 5
+    dx, x, kx, inv = I.initialize_spatial_quantities(0.0, 2 * np.pi / 0.3, nx)
+    dv, v, kv = I.initialize_velocity_quantities(6.4, nv)
+    f = I.initialize_distribution(nx, nv, 6.4)
+    stuff = {"f": f, "e": np.zeros(nx)}
+    sc = outer_loop.get_arrays_for_inner_loop(stuff, nt, rules, device="cpu")
+    sc["time_batch"] = torch.as_tensor(0.1 * np.arange(nt))
+    sc["series"]["mean_de2"] += 1e-3
+    sc = outer_loop.post_inner_loop_update(sc)
+    ref = vo.new_storage(f, np.zeros(nx), nt, None if rules["space"] == "all" else len(rules["space"]))
+    fields, stored_f, t, series, cur = storage.check_batch(sc, x, v, rules)
+    assert set(fields) == set(ref["fields"]) and set(series) >= set(ref["series"])
+    for k in ref["fields"]:
+        assert fields[k].shape == ref["fields"][k].shape and fields[k].dtype == ref["fields"][k].dtype
+    for k in ref["series"]:
+        assert series[k].shape == ref["series"][k].shape and series[k].dtype == ref["series"][k].dtype
+    assert stored_f.shape == ref["stored_f"].shape and stored_f.dtype == ref["stored_f"].dtype
+    np.testing.assert_allclose(stored_f[0], ref["stored_f"][0], rtol=1e-6, atol=1e-7)
+    np.testing.assert_array_equal(cur, f)
+    np.testing.assert_array_equal(t, 0.1 * np.arange(nt))
+    # the post-batch series of vlapy/outer_loop.py:218-245
+    np.testing.assert_allclose(series["mean_cum_de2"], 1e-3 * np.arange(1, nt + 1))
+    assert sc["mean_cum_de2_previous"] == pytest.approx(1e-3 * nt)
+    coords = storage.batch_coords(t, x, v, rules)
+    second = coords["distribution_function"][1]
+    assert second[0] == ("space" if rules["space"] == "all" else "fourier_mode")
+    # a mismatched array is refused with the coordinate it misses
+    sc["fields"]["e"] = sc["fields"]["e"][:, :-1]
+    with pytest.raises(ValueError, match="space"):
+        storage.check_batch(sc, x, v, rules)

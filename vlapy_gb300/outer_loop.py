@@ -57,16 +57,20 @@ def get_everything_ready_for_outer_loop(diagnostics, all_params, pulse_dictionar
     }
 
 
-def get_arrays_for_inner_loop(stuff_for_time_loop, nt_in_loop, store_f_rules, this_np=None):
-    """sim_config dict of CUDA tensors (vlapy/outer_loop.py:149-215)."""
-    require_cuda()
+def get_arrays_for_inner_loop(stuff_for_time_loop, nt_in_loop, store_f_rules, this_np=None, device=None):
+    """sim_config dict of CUDA tensors (vlapy/outer_loop.py:149-215).  device
+    defaults to the current CUDA device; "cpu" builds the same layout in host
+    memory (for inspecting the layout without a GPU; the steps need CUDA)."""
+    dev = torch.device(device) if device is not None else torch.device("cuda")
+    if dev.type == "cuda":
+        require_cuda()
     f0 = np.asarray(stuff_for_time_loop["f"], dtype=np.float64)
     e0 = np.asarray(stuff_for_time_loop["e"], dtype=np.float64)
     nx, nv = f0.shape
-    dev = torch.device("cuda")
+    put = (lambda a: torch.as_tensor(a, dtype=torch.float64, device=dev)) if dev.type != "cuda" else as_device
     if store_f_rules["space"] == "all":
         store_f = torch.zeros((nt_in_loop, nx, nv), dtype=torch.float64, device=dev)
-        store_f[0] = as_device(f0)
+        store_f[0] = put(f0)
     elif isinstance(store_f_rules["space"], list) and store_f_rules["space"][0] == "k0":
         m = len(store_f_rules["space"])
         first = np.fft.fft(f0, axis=0)[:m].astype(np.complex64)
@@ -77,8 +81,8 @@ def get_arrays_for_inner_loop(stuff_for_time_loop, nt_in_loop, store_f_rules, th
     z = lambda *s: torch.zeros(s, dtype=torch.float64, device=dev)  # noqa: E731
     return {
         "time_batch": z(nt_in_loop),
-        "e": as_device(e0).clone(),
-        "f": as_device(f0).clone(),
+        "e": put(e0).clone(),
+        "f": put(f0).clone(),
         "stored_f": store_f,
         "mean_cum_de2_previous": 0.0,
         "series": {k: z(nt_in_loop) for k in

@@ -312,41 +312,48 @@ def run_sweep_gpu(args, w, rank, world, global_rank=0):
     return ms, prof, clk, (e2e_sec, 0, d2h), sw
 
 
-def fp64_plain_sweep(w, steps=3):
-    """Plain FP64 GPU step (the parity mode, one run at a time) timed on one
-    sampled run of each shape class and extrapolated to the sweep."""
+def fp64_plain_sweep(w, steps=2):
+    """Plain FP64 GPU method on the whole sweep: every run of the workload in
+    one batched FP64 step (vg_batch: the reference's FP64 step per run, the
+    parity mode's device code, every launch covering all runs of a shape),
+    timed with CUDA events over `steps` steps after one warm-up step and
+    extrapolated to the workload's steps per run; then one profiled step."""
     import torch
-    from vlapy_gb300 import initializers as I
-    from vlapy_gb300.plan import Plan
+    from vlapy_gb300.batch import Batch64
     from vlapy_gb300.sweep import sweep_config
     runs = sweep_config(w["n_runs"], w["seed"])
-    classes = {}
-    for r in runs:
-        classes.setdefault((r["nx"], r["nv"]), []).append(r)
-    total_ms = 0.0
-    per = {}
-    for (nx, nv), rs in sorted(classes.items()):
-        r = next((q for q in rs if q["nu"] > 0), rs[0])
-        dx, x, kx, inv = I.initialize_spatial_quantities(0.0, 2 * np.pi / r["k"], nx)
-        dv, v, kv = I.initialize_velocity_quantities(w["vmax"], nv)
-        p = Plan(nx, nv, x, v, kx, kv, inv, dx, dv, dt=w["dt"], nu=r["nu"], collision="dg" if r["nu"] > 0 else "none")
-        f = torch.as_tensor(I.initialize_distribution(nx, nv, w["vmax"]) * (1 + r["amplitude"] * np.cos(r["k"] * x))[:, None],
-                            device="cuda")
-        e = torch.zeros(nx, dtype=torch.float64, device="cuda")
-        tb = torch.as_tensor(w["dt"] * np.arange(steps + 2), device="cuda")
-        p.run_steps(f, e, None, tb, None, 0, 2, use_graph=False)
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        p.run_steps(f, e, None, tb, None, 0, steps, use_graph=False)
-        e1.record()
-        torch.cuda.synchronize()
-        ms = e0.elapsed_time(e1) / steps
-        per["%dx%d" % (nx, nv)] = ms
-        total_ms += ms * len(rs)
-        p.close()
-    runs_per_s = len(runs) / (total_ms / 1e3 * SWEEP_STEPS)
-    return runs_per_s, per
+    b = Batch64(runs, vmax=w["vmax"], dt=w["dt"])
+    f, e = b.initial_state()
+    eh, sh = b.history(steps)
+    stream = torch.cuda.Stream()
+    stream.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(stream):
+        b.run_steps(f, e, 1, eh, sh, stream=stream)
+        b.run_steps(f, e, steps, eh, sh, use_graph=True, stream=stream)  # capture + first replay
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    with torch.cuda.stream(stream):
+        b.run_steps(f, e, steps, eh, sh, use_graph=True, stream=stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    if not torch.isfinite(eh).all():
+        raise RuntimeError("non-finite field in the FP64 batch history")
+    b.profile(True)
+    with torch.cuda.stream(stream):
+        b.run_steps(f, e, 1, eh, sh, stream=stream)
+    prof = b.profile_read()
+    b.profile(False)
+    out = {"runs_per_s": len(runs) / (ms / 1e3 * SWEEP_STEPS), "ms_per_step": ms,
+           "cells_per_s": b.cells / (ms / 1e3),
+           "kernels_ms_per_step": {k: d["total_ms"] for k, d in prof.items()},
+           "how": "all %d runs in one batched FP64 step (vg_batch), %d graph-replayed steps timed with CUDA "
+                  "events, extrapolated to %d steps per run" % (len(runs), steps, SWEEP_STEPS)}
+    b.close()
+    del f, e, eh, sh
+    torch.cuda.empty_cache()
+    return out
 
 
 def _damping_errors(t, sw_ref, e_ref, sw, e_hist, t_max=60.0):
@@ -779,10 +786,7 @@ def main_sweep(args, w, rank, world):
         return
     fp64 = None
     if not args.no_fp64_compare:
-        fp64_rps, fp64_per = fp64_plain_sweep(w)
-        fp64 = {"runs_per_s": fp64_rps, "ms_per_step_by_shape": fp64_per,
-                "how": "FP64 parity step, one run at a time, timed on one run per shape and "
-                       "weighted by the shape counts"}
+        fp64 = fp64_plain_sweep(w)
     learned = None if args.no_learned else learned_path(args, w)
     cpu = None
     if not args.no_cpu_baseline:

@@ -177,12 +177,49 @@ int vg_run_steps(vg_plan* plan, void* f, double* e, const vg_history* hist,
  * one static device array of about 580 KB that every GPU loading the library
  * keeps until exit.  Limits: 2 <= nx <= 8192, 2 <= nv <= 16384; larger sizes
  * return VG_ERR_ARG.  one_over_kx[nx], driver[nx] (may be NULL) and e[nx] are
- * DEVICE arrays.  The first call on a device resolves the array's address
- * and fills its twiddle table; make that call before any stream capture.
- * Calls share the array: calls that overlap on the GPU race and must be
- * ordered by the caller.  No counterpart in the reference. */
+ * DEVICE arrays.  The first call on a device (and the first after its context
+ * is recreated, e.g. by cudaDeviceReset) fills the array's twiddle table on
+ * the caller's stream and waits for that stream: make it during set-up,
+ * before any stream capture.  Later calls only launch kernels on the caller's
+ * stream (the summation table for nv is written on the device) and copy
+ * nothing from the host.  Calls share the array: calls that overlap on the
+ * GPU race and must be ordered by the caller.  No counterpart in the
+ * reference. */
 int vg_field_solve_noalloc(const double* f, int32_t nx, int32_t nv, double dv, const double* one_over_kx,
                            const double* driver, double* e, vg_stream stream);
+
+/* ---- batched FP64 step ------------------------------------------------- */
+/* n_runs independent runs of the FP64 time step advanced together: each
+ * step is the reference's leapfrog step with exponential advection, the
+ * spectral Poisson solve, the implicit collision step of the runs' operator
+ * and the per-step moments (vlapy/core/step.py:286-328 applied per run),
+ * with every kernel launch covering all runs of one nv (the row operators)
+ * or one nx (the x-drift and the Poisson solve).  Each run is described as
+ * for vg_plan_create and goes through the same device code as a plan, so it
+ * follows the reference's NumPy step as a plan does.  Requirements: FP64,
+ * leapfrog, no pulses, one dt for all runs, one collision operator for all
+ * runs with nu > 0 (runs with nu = 0 or VG_COLL_NONE skip the collision
+ * step, as the reference does), power-of-two nx in [2, 1024], and the runs
+ * of one nv contiguous and on the same velocity grid.  No reference
+ * counterpart: the reference runs one simulation per process
+ * (vlapy/manager.py:35-177). */
+typedef struct vg_batch vg_batch;
+int vg_batch_create(const vg_run_desc* runs, int32_t n_runs, vg_batch** out);
+int vg_batch_destroy(vg_batch* batch);
+/* total cells and x points (the e-history row length) */
+int vg_batch_sizes(const vg_batch* batch, int64_t* cells, int64_t* x_points);
+/* nsteps steps of every run, in place.  f: DEVICE float64, the runs' f[nx][nv]
+ * back to back in the order of the descriptors; e: DEVICE float64, the runs'
+ * e[nx] back to back.  If e_hist/series_hist are non-NULL, step i of this call
+ * is stored at row (hist_row0 + i) of e_hist [rows][x_points] and
+ * series_hist [rows][n_runs][7] (mean n, j, T, e^2, driver^2 (0), f^2,
+ * f log f), for rows < hist_rows.  use_graph != 0 replays one captured CUDA
+ * graph per (buffers, nsteps, rows, stream) on a non-default stream. */
+int vg_batch_run_steps(vg_batch* batch, double* f, double* e, int32_t nsteps, double* e_hist, double* series_hist,
+                       int32_t hist_rows, int32_t hist_row0, int32_t use_graph, vg_stream stream);
+/* per-kernel timing of vg_batch_run_steps (same contract as vg_profile_*) */
+int vg_batch_profile_enable(vg_batch* batch, int32_t enable);
+int vg_batch_profile_read(vg_batch* batch, vg_prof_entry* out, int32_t max, int32_t* n_out);
 
 /* ---- batched sweep ----------------------------------------------------- */
 /* Thousands of independent runs of uneven shape advanced together in the

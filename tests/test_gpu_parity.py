@@ -59,7 +59,7 @@ def cuda(a):
 
 
 SHAPES = [(32, 512), (16, 128), (7, 64), (64, 1024), (2, 8192), (4, 2), (256, 32), (8192, 4),
-          (4096, 8)]
+          (4096, 8), (12, 96), (5, 1000), (96, 30), (3, 4095)]
 
 
 @pytest.mark.parametrize("nx,nv", SHAPES)
@@ -76,8 +76,6 @@ def test_edfdv_matches_oracle(nx, nv):
 
 @pytest.mark.parametrize("nx,nv", SHAPES)
 def test_vdfdx_matches_oracle(nx, nv):
-    if nx & (nx - 1):
-        pytest.skip("x-advection supports power-of-two nx (others raise NotImplementedError)")
     p, (x, v, kx, kv, inv, dx, dv) = make_plan(nx, nv)
     f = perturbed(nx, nv)
     for dt in (0.1, 0.05, 1.3):
@@ -188,6 +186,8 @@ def _golden_run(name):
     drv = None
     if "pulse_k0" in d.files:
         pulses = {"p": {k: float(d["pulse_" + k]) for k in ("k0", "w0", "a0", "t_L", "t_R", "t_wL", "t_wR")}}
+        if "pulse_envelope" in d.files:
+            pulses["p"]["envelope"] = str(d["pulse_envelope"])
         drv = field_driver.get_driver_function(x, pulses)
     rules = ({"time": "first-last", "space": "all"} if n_modes < 0
              else {"time": "first-last", "space": ["k%d" % i for i in range(n_modes)]})
@@ -203,8 +203,11 @@ def _golden_run(name):
 
 @pytest.mark.parametrize("name", ["landau_32x512", "driven_dg_16x256", "driven_lb_16x256",
                                   "integrator_pefrl_16x128", "integrator_h-sixth_16x128",
-                                  "step_sl_dg_16x64", "step_cd2_16x64"])
+                                  "step_sl_dg_16x64", "step_cd2_16x64", "driven_sin2_dg_64x1024"])
 def test_timestep_matches_golden(name):
+    """The reference's own time steps, including the driven-wave workload's
+    grid (64 x 1024, Dougherty nu = 1e-3) under the sin^2-envelope driver,
+    whose pulses the device evaluates at every sub-step time."""
     d, m, stuff, params, rules, step, arrays = _golden_run(name)
     nsteps = int(m["nsteps"])
     ts = step.get_timestep(params, stuff)
@@ -228,18 +231,23 @@ def _check_storage(sc, d, nsteps):
     nx, nv = f0.shape
     vmax = float(d["meta_vmax"])
     dv, v, kv = vo.velocity_axis(vmax, nv)
+    # long fixtures keep every ke-th row of the fields other than e, and of stored_f
+    ke = int(d["meta_keep_every"]) if "meta_keep_every" in d.files else 1
+    # f carries up to TOL relative error per step (the FFT rounding differs from
+    # pocketfft's): the bounds on its moments grow with the steps like f's own
+    grow = max(1.0, nsteps / 10.0)
     for k in vo.FIELD_KEYS:
-        got = sc["fields"][k].cpu().numpy()
+        got = sc["fields"][k].cpu().numpy()[::1 if k == "e" else ke]
         ref = d["fields_" + k]
         if k == "driver":
             np.testing.assert_array_equal(got, ref)
         elif k == "e":
-            assert rel(got, ref) <= 1e-11, k
+            assert rel(got, ref) <= 1e-11 * grow, k
         else:
             # odd moments of a near-symmetric f are ~0: bound the error by the
             # scale of the integrand, trapz(|f| |v|^p)
             scale = vo.trapz(np.abs(f0) * np.abs(v) ** FIELD_POW[k], dv, 1).max()
-            np.testing.assert_allclose(got, ref, rtol=1e-11, atol=1e-12 * scale, err_msg=k)
+            np.testing.assert_allclose(got, ref, rtol=1e-11 * grow, atol=1e-12 * scale * grow, err_msg=k)
     for k in vo.SERIES_KEYS:
         got = sc["series"][k].cpu().numpy()
         atol = 1e-14
@@ -247,8 +255,8 @@ def _check_storage(sc, d, nsteps):
             # the mean current of a near-symmetric f is ~0: bound its error by the
             # scale of the integrand, as for the odd moments above
             atol = max(atol, 1e-12 * vo.trapz(np.abs(f0) * np.abs(v), dv, 1).mean())
-        np.testing.assert_allclose(got, d["series_" + k], rtol=1e-11, atol=atol, err_msg=k)
-    sf = sc["stored_f"].cpu().numpy()
+        np.testing.assert_allclose(got, d["series_" + k], rtol=1e-11 * grow, atol=atol * grow, err_msg=k)
+    sf = sc["stored_f"].cpu().numpy()[::ke]
     ref = d["stored_f"]
     if sf.dtype == np.complex64:
         np.testing.assert_allclose(sf, ref, rtol=2e-6, atol=1e-6 * np.abs(ref).max())
@@ -256,7 +264,7 @@ def _check_storage(sc, d, nsteps):
         assert rel(sf, ref) <= 1e-11
 
 
-@pytest.mark.parametrize("name", ["landau_32x512", "driven_dg_16x256"])
+@pytest.mark.parametrize("name", ["landau_32x512", "driven_dg_16x256", "driven_sin2_dg_64x1024"])
 def test_inner_loop_graph_matches_golden(name):
     """The graph-captured inner loop over the whole batch."""
     from vlapy_gb300 import outer_loop
@@ -273,6 +281,11 @@ def test_inner_loop_graph_matches_golden(name):
         assert rel(sc["f"].cpu().numpy(), d["f_%d" % nsteps]) <= TOL * nsteps
         assert rel(sc["e"].cpu().numpy(), d["e_%d" % nsteps]) <= TOL * nsteps
         _check_storage(sc, d, nsteps)
+        # what StorageManager.batch_update (vlapy/storage.py:177-315) receives
+        from vlapy_gb300 import storage
+        fields, stored_f, t, series, cur = storage.check_batch(sc, stuff["x"], stuff["v"], rules)
+        np.testing.assert_array_equal(t, d["time"])
+        assert "mean_cum_de2" in series and stored_f.shape[0] == nsteps
 
 
 def test_leapfrog_parity_many_steps():
@@ -291,11 +304,31 @@ def test_leapfrog_parity_many_steps():
     assert rel(eg.cpu().numpy(), e) <= 1e-10
 
 
+def test_non_power_of_two_steps_match_oracle():
+    """Full steps (leapfrog, Dougherty collisions, storage) on grids that are
+    not powers of two, where both advections take the direct-DFT path, against
+    the oracle (the reference transforms any length)."""
+    nx, nv, k, nu, nsteps = 12, 96, 0.3, 1e-3, 5
+    p, (x, v, kx, kv, inv, dx, dv) = make_plan(nx, nv, nu=nu, collision="dg")
+    f0 = perturbed(nx, nv, amp=1e-2)
+    run = vo.OracleRun(nx, nv, 2 * np.pi / k, 6.4, 0.1, nu=nu, operator="dg")
+    e, f = np.zeros(nx), f0
+    g, eg = cuda(f0), torch.zeros(nx, dtype=torch.float64, device="cuda")
+    tb = cuda(0.1 * np.arange(nsteps))
+    p.run_steps(g, eg, None, tb, None, 0, nsteps, use_graph=False)
+    for i in range(nsteps):
+        e, f = run.step(e, f, 0.1 * i)  # VP step, then the collision step
+    assert rel(g.cpu().numpy(), f) <= TOL * nsteps
+    assert rel(eg.cpu().numpy(), e) <= TOL * nsteps
+
+
 def test_unsupported_sizes_raise():
-    p, _ = make_plan(12, 64)
-    g = cuda(np.ones((12, 64)))
+    """Lengths that are not powers of two go through direct DFTs up to 4096;
+    longer ones are refused."""
+    p, _ = make_plan(4100, 4)
+    g = cuda(np.ones((4100, 4)))
     with pytest.raises(NotImplementedError):
         p.vdfdx(g, 0.1)
-    p2, _ = make_plan(8, 96)
+    p2, _ = make_plan(2, 4100)
     with pytest.raises(NotImplementedError):
-        p2.edfdv(cuda(np.ones((8, 96))), cuda(np.zeros(8)), 0.1)
+        p2.edfdv(cuda(np.ones((2, 4100))), cuda(np.zeros(2)), 0.1)

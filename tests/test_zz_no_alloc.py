@@ -64,3 +64,30 @@ def test_noalloc_rejects_sizes_beyond_its_scratch(lib):
     st = lib.vg_field_solve_noalloc(ptr(f), 16384, 2, C.c_double(0.1), ptr(inv), None, ptr(e), stream_handle())
     assert st == VG_ERR_ARG
     assert b"nx <= 8192" in lib.vg_last_error()
+    # one velocity point past the limit (the sizes are checked before any launch)
+    f2 = torch.zeros((2, 16385), dtype=torch.float64, device="cuda")
+    st = lib.vg_field_solve_noalloc(ptr(f2), 2, 16385, C.c_double(0.1), ptr(inv), None, ptr(e), stream_handle())
+    assert st == VG_ERR_ARG
+    assert b"nv <= 16384" in lib.vg_last_error() or b"nv=16385" in lib.vg_last_error()
+
+
+def test_noalloc_on_a_second_stream(lib):
+    """After the set-up call, a call on another stream (ordered after the
+    first by the caller, as the shared scratch requires) gives the same field."""
+    from vlapy_gb300._lib import check
+    from vlapy_gb300.plan import Plan, ptr, stream_handle
+    nx, nv = 64, 1024
+    f, drv, (x, v, kx, kv, inv, dx, dv) = _case(nx, nv, 7)
+    plan = Plan(nx, nv, x, v, kx, kv, inv, dx, dv)
+    ft, dt_, inv_t = (torch.as_tensor(a, device="cuda") for a in (f, drv, inv))
+    ref = torch.empty(nx, dtype=torch.float64, device="cuda")
+    plan.field_solve(ft, dt_, ref)
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    out = torch.full((nx,), float("nan"), dtype=torch.float64, device="cuda")
+    with torch.cuda.stream(s):
+        check(lib.vg_field_solve_noalloc(ptr(ft), nx, nv, C.c_double(dv), ptr(inv_t), ptr(dt_), ptr(out),
+                                         stream_handle(s)), "field solve noalloc")
+    torch.cuda.synchronize()
+    a, b = out.cpu().numpy(), ref.cpu().numpy()
+    assert np.linalg.norm(a - b) <= TOL * np.linalg.norm(b)

@@ -94,6 +94,13 @@ EXPORTS = {
                                C.c_void_p]),
     "vg_field_solve_noalloc": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_double, C.c_void_p,
                                          C.c_void_p, C.c_void_p, C.c_void_p]),
+    "vg_batch_create": (C.c_int, [C.POINTER(VgRunDesc), C.c_int32, C.POINTER(C.c_void_p)]),
+    "vg_batch_destroy": (C.c_int, [C.c_void_p]),
+    "vg_batch_sizes": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    "vg_batch_run_steps": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p,
+                                     C.c_int32, C.c_int32, C.c_int32, C.c_void_p]),
+    "vg_batch_profile_enable": (C.c_int, [C.c_void_p, C.c_int32]),
+    "vg_batch_profile_read": (C.c_int, [C.c_void_p, C.POINTER(VgProfEntry), C.c_int32, C.POINTER(C.c_int32)]),
     "vg_sweep_create": (C.c_int, [C.POINTER(VgSweepDesc), C.POINTER(C.c_void_p)]),
     "vg_sweep_destroy": (C.c_int, [C.c_void_p]),
     "vg_sweep_sizes": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),

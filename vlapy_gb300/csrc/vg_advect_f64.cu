@@ -13,6 +13,7 @@
 // rotated by exp(i (-kx dt) v_col).  Loads/stores are row segments of W
 // contiguous doubles (coalesced), transposed through shared memory.
 #include "vg_internal.cuh"
+#include "vg_f64_body.cuh"
 
 namespace vg {
 
@@ -58,52 +59,86 @@ __global__ void __launch_bounds__(row_block<double>(N)) k_edfdv_f64(double* __re
   }
 }
 
-// pad one element per sequence so column-pair sequences start in different banks
-constexpr int COL_PAD = 1;
-
 template <int NX>
 __global__ void __launch_bounds__(col_seqs<double>(NX) * fft_threads<double>(NX)) k_vdfdx_f64(double* __restrict__ f, int nv, int W,
                                                     const double* __restrict__ kx,
                                                     const double* __restrict__ v, double dt,
                                                     const cx<double>* __restrict__ tw) {
-  constexpr int R = fft_radix<double>(NX);
-  constexpr int G = NX / R;
-  constexpr int LD = sp_len<double>(NX) + COL_PAD;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  cx<double>* s = reinterpret_cast<cx<double>*>(smem_raw);
-  double* sd = reinterpret_cast<double*>(smem_raw);
-  const int c0 = blockIdx.x * W;
-  const int total = NX * W;
-  for (int q = threadIdx.x; q < total; q += blockDim.x) {
-    const int x = q / W, c = q - x * W;
-    const int col = c0 + c;
-    const double val = col < nv ? f[(size_t)x * nv + col] : 0.0;
-    sd[2 * ((c >> 1) * LD + sp<double>(x)) + (c & 1)] = val;
+  vdfdx_tile_body<NX>(f, nv, blockIdx.x * W, W, kx, v, dt, tw, smem_raw);
+}
+
+// Exponential advection of lines whose length N is not a power of two, by
+// direct DFTs (the reference's scipy.fft transforms any length; O(N^2) work
+// per line here).  Line l is the row l of f for the v step (elements
+// contiguous) or the column l for the x step (elements nv apart):
+//   F_k = sum_n f_n w^(n k),  w = exp(-2 pi i / N),
+//   G_k = exp(i theta_k) F_k,  theta_k = ((-kw[k]) * dt) * c_l,
+//   f_n <- Re (1/N) sum_k G_k w^(-n k),
+// with kw = kv, c_l = e[l] (v step) or kw = kx, c_l = v[l] (x step), the
+// phase the reference evaluates (vlapy/core/vlasov.py:106-108, 136-138).  One
+// CTA per line; shared memory holds the line, G and the N twiddles w^q,
+// q = (n k) mod N, each from sincospi(2 q / N).
+__global__ void k_dft_advect_f64(double* __restrict__ f, int N, int n_lines, long long elem_stride,
+                                 long long line_stride, const double* __restrict__ kw,
+                                 const double* __restrict__ c, double dt) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double* line = reinterpret_cast<double*>(smem_raw);
+  cx<double>* G = reinterpret_cast<cx<double>*>(line + N + (N & 1));
+  cx<double>* W = G + N;
+  const int l = blockIdx.x;
+  if (l >= n_lines) return;
+  double* fl = f + (long long)l * line_stride;
+  for (int q = threadIdx.x; q < N; q += blockDim.x) {
+    double sn, cs;
+    sincospi(2.0 * (double)q / (double)N, &sn, &cs);
+    W[q] = {cs, -sn};
+    line[q] = fl[(long long)q * elem_stride];
   }
   __syncthreads();
-  const int g = threadIdx.x / G, t = threadIdx.x - g * G;
-  cx<double>* sg = s + (size_t)g * LD;
-  block_fft<double, NX, false>(sg, t, tw);
-  const int ca_col = c0 + 2 * g, cb_col = ca_col + 1;
-  const double vva = ca_col < nv ? v[ca_col] : 0.0;
-  const double vvb = cb_col < nv ? v[cb_col] : 0.0;
-  // theta = ((-kx) * dt) * v, the imaginary part of (-1j * kx * dt * v)
-  two_real_rotate<double>(sg, NX, t, G, [&](int m, double& ca, double& sa, double& cb, double& sb) {
-    const double ph = -kx[m] * dt;
-    sincos(ph * vva, &sa, &ca);
-    sincos(ph * vvb, &sb, &cb);
-  });
+  const double cl = c[l];
+  for (int k = threadIdx.x; k < N; k += blockDim.x) {
+    double zr = 0.0, zi = 0.0;
+    int q = 0;
+    for (int n = 0; n < N; ++n) {
+      const cx<double> w = W[q];
+      zr += line[n] * w.x;
+      zi += line[n] * w.y;
+      q += k;
+      if (q >= N) q -= N;
+    }
+    double sa, ca;
+    sincos(((-kw[k]) * dt) * cl, &sa, &ca);
+    G[k] = {ca * zr - sa * zi, ca * zi + sa * zr};
+  }
   __syncthreads();
-  block_fft<double, NX, true>(sg, t, tw);
-  const double sc = 1.0 / NX;
-  for (int q = threadIdx.x; q < total; q += blockDim.x) {
-    const int x = q / W, c = q - x * W;
-    const int col = c0 + c;
-    if (col < nv) f[(size_t)x * nv + col] = sd[2 * ((c >> 1) * LD + sp<double>(x)) + (c & 1)] * sc;
+  const double sc = 1.0 / N;
+  for (int n = threadIdx.x; n < N; n += blockDim.x) {
+    double acc = 0.0;
+    int q = 0;
+    for (int k = 0; k < N; ++k) {
+      // Re(G_k conj(w^(n k)))
+      const cx<double> w = W[q];
+      acc += G[k].x * w.x + G[k].y * w.y;
+      q += n;
+      if (q >= N) q -= N;
+    }
+    fl[(long long)n * elem_stride] = acc * sc;
   }
 }
 
+static size_t dft_advect_smem(int n) { return ((size_t)n + (n & 1) + 4 * (size_t)n) * sizeof(double); }
+
 namespace {
+
+cudaError_t dft_advect(double* f, int N, int n_lines, long long elem_stride, long long line_stride,
+                       const double* kw, const double* c, double dt, cudaStream_t s) {
+  const size_t smem = dft_advect_smem(N);
+  cudaError_t err = ensure_smem((const void*)k_dft_advect_f64, smem);
+  if (err != cudaSuccess) return err;
+  k_dft_advect_f64<<<n_lines, 256, smem, s>>>(f, N, n_lines, elem_stride, line_stride, kw, c, dt);
+  return cudaGetLastError();
+}
 
 template <int N>
 cudaError_t edfdv_n(const vg_plan& p, double* f, const double* e, double dt, cudaStream_t s) {
@@ -139,6 +174,7 @@ cudaError_t vdfdx_n(const vg_plan& p, double* f, double dt, cudaStream_t s) {
   M(11, __VA_ARGS__) M(12, __VA_ARGS__) M(13, __VA_ARGS__)
 
 cudaError_t launch_edfdv_f64(const vg_plan& p, double* f, const double* e, double dt, cudaStream_t s) {
+  if (!p.nv_pow2) return dft_advect(f, p.nv, p.nx, 1, p.nv, p.kv, e, dt, s);
   switch (ilog2(p.nv)) {
 #define CASE(L, ...) case L: return edfdv_n<(1 << L)>(p, f, e, dt, s);
     VG_POW2_CASES(CASE, 0)
@@ -148,6 +184,7 @@ cudaError_t launch_edfdv_f64(const vg_plan& p, double* f, const double* e, doubl
 }
 
 cudaError_t launch_vdfdx_f64(const vg_plan& p, double* f, double dt, cudaStream_t s) {
+  if (!p.nx_pow2) return dft_advect(f, p.nx, p.nv, p.nv, 1, p.kx, p.v, dt, s);
   switch (ilog2(p.nx)) {
 #define CASE(L, ...) case L: return vdfdx_n<(1 << L)>(p, f, dt, s);
     VG_POW2_CASES(CASE, 0)

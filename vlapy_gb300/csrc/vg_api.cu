@@ -82,7 +82,7 @@ static void pairwise_tree(int start, int len, std::vector<int>& leaves, std::vec
   prog.push_back(-1);
 }
 
-static std::vector<int> pairwise_table(int n) {
+std::vector<int> pairwise_table(int n) {
   std::vector<int> leaves, prog;
   pairwise_tree(0, n, leaves, prog);
   std::vector<int> out;
@@ -195,17 +195,21 @@ int require_plan(const vg_plan* p) {
   return VG_OK;
 }
 
+// exponential advection sizes: powers of two by shared-memory FFTs, other
+// lengths by direct DFTs (shared memory holds 5 N doubles of a line)
 int require_fft_v(const vg_plan* p) {
-  if (!p->nv_pow2 || p->nv > 8192) {
-    set_error("v-advection needs nv a power of two <= 8192, got " + std::to_string(p->nv));
+  if (p->nv_pow2 ? p->nv > 8192 : p->nv > DFT_ADVECT_NMAX) {
+    set_error("v-advection needs nv a power of two <= 8192 or any nv <= " + std::to_string(DFT_ADVECT_NMAX) +
+              ", got " + std::to_string(p->nv));
     return VG_ERR_UNSUPPORTED;
   }
   return VG_OK;
 }
 
 int require_fft_x(const vg_plan* p) {
-  if (!p->nx_pow2 || p->nx > 8192) {
-    set_error("x-advection needs nx a power of two <= 8192, got " + std::to_string(p->nx));
+  if (p->nx_pow2 ? p->nx > 8192 : p->nx > DFT_ADVECT_NMAX) {
+    set_error("x-advection needs nx a power of two <= 8192 or any nx <= " + std::to_string(DFT_ADVECT_NMAX) +
+              ", got " + std::to_string(p->nx));
     return VG_ERR_UNSUPPORTED;
   }
   return VG_OK;
@@ -623,7 +627,7 @@ int vg_plan_create(const vg_run_desc* d, vg_plan** out) {
   TRY(dev_copy<double>(&p->rho, nullptr, nx, "scratch"));
   TRY(dev_copy<double>(&p->etmp, nullptr, 4 * nx + 4, "scratch"));
   if (d->precision == VG_F64 && d->collision != VG_COLL_NONE)
-    TRY(dev_copy<double>(&p->bb, nullptr, nx * nv, "thomas scratch"));
+    TRY(dev_copy<double>(&p->bb, nullptr, 2 * nx * nv, "thomas scratch"));
   if (d->precision == VG_F32_DELTA_F) TRY(setup_f32(p, d));
   TRY(cuda_status(launch_twiddles(*p, 0), "twiddles"));
   TRY(cuda_status(cudaDeviceSynchronize(), "plan setup"));

@@ -31,7 +31,7 @@ struct vg_plan {
   // scratch
   double* dens;   // [nx]
   double* mom;    // [nx][MOM_STRIDE]
-  double* bb;     // [nx][nv] Thomas elimination scratch (FP64 mode)
+  double* bb;     // [nx][2][nv] Thomas elimination scratch (pivots, upper diagonal; FP64 mode)
   double* rho;    // [nx]
   double* etmp;   // [nx]
   // semi-Lagrangian steps (allocated by their first call): spline second
@@ -100,10 +100,17 @@ int prof_collect(ProfState* ps, int n_kinds, const char* const* names, const dou
                  vg_prof_entry* out, int max, int* n_out);
 
 void set_error(const std::string& msg);
+// NumPy's pairwise summation tree over n terms as [n_leaves, n_prog,
+// (start, len) per leaf, post-order program] (leaf index, -1 = combine)
+std::vector<int> pairwise_table(int n);
 int cuda_status(cudaError_t err, const char* what);
 // raise a kernel's dynamic shared-memory limit once (not a stream operation,
 // so it is legal while a stream is being captured)
 cudaError_t ensure_smem(const void* kernel, size_t bytes);
+
+// longest line the direct-DFT advection takes (lengths that are not powers of
+// two; its shared memory holds 5 N doubles)
+constexpr int DFT_ADVECT_NMAX = 4096;
 
 // launchers (return cudaError_t of the launch)
 cudaError_t launch_edfdv_f64(const vg_plan& p, double* f, const double* e, double dt, cudaStream_t s);

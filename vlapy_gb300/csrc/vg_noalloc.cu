@@ -11,17 +11,21 @@
 // work area of the direct DFT -- lives in one file-scope __device__ array of
 // fixed size, which each GPU that loads this library holds until exit.
 //
-// The first call on a device resolves the array's device address with
-// cudaGetSymbolAddress (with that device current) and fills the twiddle
-// table; make that first call before any stream capture.  Every call shares
-// the array and keeps the last call's contents; nothing in it has to start
-// at zero (each call overwrites the density, the table and the DFT work area
-// before reading them).  Calls whose executions overlap on the GPU (on
-// different streams, or from different threads) race on the array and must
-// be ordered by the caller.
+// Host code cannot use the array's name as a device address, so each call
+// asks cudaGetSymbolAddress for it (with the calling device current).  The
+// first call on a device, and the first after the address changes (a new
+// context after cudaDeviceReset), fills the twiddle table with a kernel on
+// the caller's stream and waits for that stream; make that first call during
+// set-up, before any stream capture.  Later calls only launch kernels on the
+// caller's stream: the summation table for the call's nv is written on the
+// device by a one-thread kernel, so no call copies from host memory.  Every
+// call shares the array and keeps the last call's contents; nothing in it has
+// to start at zero (each call overwrites the density, the table and the DFT
+// work area before reading them).  Calls whose executions overlap on the GPU
+// (on different streams, or from different threads) race on the array and
+// must be ordered by the caller.
 #include <cstring>
 #include <mutex>
-#include <vector>
 
 #include "vg_internal.cuh"
 
@@ -51,6 +55,51 @@ __global__ void k_noalloc_twiddles(cx<double>* __restrict__ t64) {
   t64[q] = {cs, -sn};
 }
 
+// NumPy's pairwise summation tree over n terms (a node of more than 128 terms
+// splits at half = n/2 rounded down to a multiple of 8; smaller ones are
+// leaves), laid out as [n_leaves, n_prog, (start, len) per leaf, prog...]
+// with prog the post-order walk: a leaf's index when it is reached, -1 after
+// both children of a node.  One thread, an explicit stack (the tree is at
+// most 8 levels deep for n < 16384).
+__global__ void k_noalloc_tree(int n, int n_leaves, int* __restrict__ table) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  int st_start[48], st_len[48], st_open[48];
+  int sp = 0, nl = 0, np = 0;
+  int* leaves = table + 2;
+  int* prog = table + 2 + 2 * n_leaves;
+  st_start[0] = 0;
+  st_len[0] = n;
+  st_open[0] = 0;
+  sp = 1;
+  while (sp > 0) {
+    --sp;
+    const int start = st_start[sp], len = st_len[sp];
+    if (len <= 128) {
+      leaves[2 * nl] = start;
+      leaves[2 * nl + 1] = len;
+      prog[np++] = nl++;
+    } else if (st_open[sp]) {
+      prog[np++] = -1;
+    } else {
+      int half = len / 2;
+      half -= half % 8;
+      // the node again (closed after its children), then right, then left on top
+      st_open[sp] = 1;
+      ++sp;
+      st_start[sp] = start + half;
+      st_len[sp] = len - half;
+      st_open[sp] = 0;
+      ++sp;
+      st_start[sp] = start;
+      st_len[sp] = half;
+      st_open[sp] = 0;
+      ++sp;
+    }
+  }
+  table[0] = nl;
+  table[1] = np;
+}
+
 namespace {
 
 struct DeviceScratch {
@@ -60,33 +109,30 @@ struct DeviceScratch {
 std::mutex g_na_mu;
 DeviceScratch g_na_dev[64];
 
-// NumPy's pairwise tree over n terms, packed as [n_leaves, n_prog, (start, len)..., prog...]
-void na_tree(int start, int len, std::vector<int>& leaves, std::vector<int>& prog) {
-  if (len <= 128) {
-    prog.push_back((int)(leaves.size() / 2));
-    leaves.push_back(start);
-    leaves.push_back(len);
-    return;
-  }
+// leaves of NumPy's pairwise tree over n terms (the shape k_noalloc_tree walks)
+int na_leaves(int len) {
+  if (len <= 128) return 1;
   int half = len / 2;
   half -= half % 8;
-  na_tree(start, half, leaves, prog);
-  na_tree(start + half, len - half, leaves, prog);
-  prog.push_back(-1);
+  return na_leaves(half) + na_leaves(len - half);
 }
 
-int na_setup(int dev, unsigned char** out) {
+// the scratch array's device address on the current device; fills the
+// twiddles (on stream s, then waits for s) when the device has not been set up
+// or the address has changed since
+int na_setup(int dev, cudaStream_t s, unsigned char** out) {
+  void* p = nullptr;
+  int st = cuda_status(cudaGetSymbolAddress(&p, g_noalloc_scratch), "no-alloc scratch address");
+  if (st != VG_OK) return st;
   std::lock_guard<std::mutex> lk(g_na_mu);
   DeviceScratch& d = g_na_dev[dev];
-  if (!d.ready) {
-    void* p = nullptr;
-    int st = cuda_status(cudaGetSymbolAddress(&p, g_noalloc_scratch), "no-alloc scratch address");
-    if (st != VG_OK) return st;
+  if (!d.ready || d.ptr != p) {
+    d.ready = false;
     d.ptr = static_cast<unsigned char*>(p);
-    k_noalloc_twiddles<<<div_up(FFT_NMAX, 256), 256>>>(reinterpret_cast<cx<double>*>(d.ptr + NA_TW_OFF));
+    k_noalloc_twiddles<<<div_up(FFT_NMAX, 256), 256, 0, s>>>(reinterpret_cast<cx<double>*>(d.ptr + NA_TW_OFF));
     st = cuda_status(cudaGetLastError(), "no-alloc twiddles");
     if (st != VG_OK) return st;
-    st = cuda_status(cudaDeviceSynchronize(), "no-alloc set-up");
+    st = cuda_status(cudaStreamSynchronize(s), "no-alloc set-up");
     if (st != VG_OK) return st;
     d.ready = true;
   }
@@ -117,25 +163,19 @@ extern "C" int vg_field_solve_noalloc(const double* f, int32_t nx, int32_t nv, d
     set_error("device index out of range for the no-alloc scratch table");
     return VG_ERR_ARG;
   }
-  unsigned char* base = nullptr;
-  st = na_setup(dev, &base);
-  if (st != VG_OK) return st;
   cudaStream_t s = (cudaStream_t)stream;
-  // summation-tree table of the nv - 1 trapz terms, copied into the scratch
-  std::vector<int> leaves, prog;
-  na_tree(0, nv - 1, leaves, prog);
-  std::vector<int> table;
-  table.push_back((int)(leaves.size() / 2));
-  table.push_back((int)prog.size());
-  table.insert(table.end(), leaves.begin(), leaves.end());
-  table.insert(table.end(), prog.begin(), prog.end());
-  if (table.size() > NA_PW_WORDS) {
+  unsigned char* base = nullptr;
+  st = na_setup(dev, s, &base);
+  if (st != VG_OK) return st;
+  // summation-tree table of the nv - 1 trapz terms, written on the device
+  const int leaves = na_leaves(nv - 1);
+  if ((size_t)(2 + 2 * leaves + (2 * leaves - 1)) > NA_PW_WORDS) {
     set_error("summation table exceeds the no-alloc scratch");
     return VG_ERR_ARG;
   }
   int* d_table = reinterpret_cast<int*>(base + NA_PW_OFF);
-  st = cuda_status(cudaMemcpyAsync(d_table, table.data(), table.size() * sizeof(int), cudaMemcpyHostToDevice, s),
-                   "no-alloc table upload");
+  k_noalloc_tree<<<1, 32, 0, s>>>(nv - 1, leaves, d_table);
+  st = cuda_status(cudaGetLastError(), "no-alloc summation table");
   if (st != VG_OK) return st;
   // a plan-shaped view over the caller's arrays and the static scratch (nothing allocated)
   vg_plan view;
@@ -149,7 +189,7 @@ extern "C" int vg_field_solve_noalloc(const double* f, int32_t nx, int32_t nv, d
   view.inv_kx = const_cast<double*>(one_over_kx);
   view.tw64 = reinterpret_cast<cx<double>*>(base + NA_TW_OFF);
   view.pw_v = d_table;
-  view.pw_v_leaves = table[0];
+  view.pw_v_leaves = leaves;
   view.dens = reinterpret_cast<double*>(base + NA_DENS_OFF);
   view.etmp = reinterpret_cast<double*>(base + NA_ETMP_OFF);
   MomSpec spec;

@@ -8,79 +8,10 @@
 // f equal, densities and moments are then bit-identical to the reference's
 // np.trapz (vlapy/core/field.py:36, vlapy/core/step.py:164-223).
 #include "vg_internal.cuh"
+#include "vg_f64_body.cuh"
 
 namespace vg {
 
-// ---------------------------------------------------------------------------
-// pairwise-sum helpers
-// ---------------------------------------------------------------------------
-
-// Sum of leaf (start, len) of terms term(j), NumPy order.
-template <typename TermFn>
-__device__ __forceinline__ double leaf_sum(int start, int len, TermFn term) {
-  if (len < 8) {
-    double r = 0.0;
-    for (int i = 0; i < len; ++i) r = add_rn(r, term(start + i));
-    return r;
-  }
-  double a0 = term(start), a1 = term(start + 1), a2 = term(start + 2), a3 = term(start + 3);
-  double a4 = term(start + 4), a5 = term(start + 5), a6 = term(start + 6), a7 = term(start + 7);
-  int i = 8;
-  const int stop = len - (len % 8);
-  for (; i < stop; i += 8) {
-    a0 = add_rn(a0, term(start + i));
-    a1 = add_rn(a1, term(start + i + 1));
-    a2 = add_rn(a2, term(start + i + 2));
-    a3 = add_rn(a3, term(start + i + 3));
-    a4 = add_rn(a4, term(start + i + 4));
-    a5 = add_rn(a5, term(start + i + 5));
-    a6 = add_rn(a6, term(start + i + 6));
-    a7 = add_rn(a7, term(start + i + 7));
-  }
-  double res = add_rn(add_rn(add_rn(a0, a1), add_rn(a2, a3)), add_rn(add_rn(a4, a5), add_rn(a6, a7)));
-  for (; i < len; ++i) res = add_rn(res, term(start + i));
-  return res;
-}
-
-// Replay the combine program over leaf sums leaf[0..n_leaves).
-__device__ __forceinline__ double combine_leaves(const int* __restrict__ table, const double* leaf) {
-  const int nl = table[0], np = table[1];
-  const int* prog = table + 2 + 2 * nl;
-  double stk[24];
-  int sp = 0;
-  for (int i = 0; i < np; ++i) {
-    const int op = prog[i];
-    if (op >= 0) {
-      stk[sp++] = leaf[op];
-    } else {
-      const double r = stk[--sp];
-      const double l = stk[--sp];
-      stk[sp++] = add_rn(l, r);
-    }
-  }
-  return sp ? stk[0] : 0.0;
-}
-
-// ---------------------------------------------------------------------------
-// row moments: out[row][q] = trapz_v p_q(f[row]) with NumPy's rounding
-// ---------------------------------------------------------------------------
-
-__device__ __forceinline__ double mom_product(int kind, int arg, double fj, int j,
-                                              const double* __restrict__ v,
-                                              const double* __restrict__ v_pow, int nv,
-                                              double vbar) {
-  switch (kind) {
-    case MOM_ONE: return fj;
-    case MOM_V: return mul_rn(fj, v[j]);
-    case MOM_W: return mul_rn(fj, v_pow[(size_t)arg * nv + j]);
-    case MOM_SQ: return mul_rn(fj, fj);
-    case MOM_FLOGF: return mul_rn(fj, log(fj));
-    default: {  // MOM_DG2: f * (v - vbar) ** 2.0
-      const double d = sub_rn(v[j], vbar);
-      return mul_rn(fj, mul_rn(d, d));
-    }
-  }
-}
 
 __global__ void k_row_moments_f64(const double* __restrict__ f, int nv, const double* __restrict__ v,
                                   const double* __restrict__ v_pow, MomSpec spec,
@@ -129,44 +60,6 @@ cudaError_t launch_row_moments_f64(const vg_plan& p, const double* f, const MomS
   return cudaGetLastError();
 }
 
-// ---------------------------------------------------------------------------
-// driver pulses, vlapy/field_driver.py:24-50 (+ the sin^2 envelope)
-// ---------------------------------------------------------------------------
-
-__device__ __forceinline__ double pulse_sum(const vg_pulse* __restrict__ P, int np, double t, double x) {
-  double total = 0.0;
-  for (int i = 0; i < np; ++i) {
-    const vg_pulse q = P[i];
-    const double arg = sub_rn(mul_rn(q.k0, x), mul_rn(q.w0, t));
-    double term;
-    if (q.envelope == VG_ENV_SIN2) {
-      if (t < 0.0 || t > q.t_R) {
-        term = 0.0;
-      } else {
-        const double sn = sin(__ddiv_rn(mul_rn(3.141592653589793, t), q.t_R));
-        term = mul_rn(mul_rn(q.a0, mul_rn(sn, sn)), sin(arg));
-      }
-    } else {
-      const double env = 0.5 * sub_rn(tanh((t - q.t_L) / q.t_wL), tanh((t - q.t_R) / q.t_wR));
-      term = mul_rn(mul_rn(mul_rn(env, q.k0), q.a0), sin(arg));
-    }
-    total = add_rn(total, term);
-  }
-  return total;
-}
-
-struct FieldTimeDev {
-  const double* t_ptr;
-  double t_host;
-  int nadd;
-  double add[6];
-};
-
-__device__ __forceinline__ double field_time(const FieldTimeDev& ft) {
-  double t = ft.t_ptr ? *ft.t_ptr : ft.t_host;
-  for (int i = 0; i < ft.nadd; ++i) t = add_rn(t, ft.add[i]);
-  return t;
-}
 
 __global__ void k_driver(const vg_pulse* __restrict__ P, int np, const double* __restrict__ x, int nx,
                          FieldTimeDev ft, double* __restrict__ out) {
@@ -193,13 +86,6 @@ cudaError_t launch_driver(const vg_plan& p, const FieldTime& ft, double* out, cu
 // spectral Poisson, vlapy/core/field.py:39-88
 // ---------------------------------------------------------------------------
 
-__device__ __forceinline__ double driver_value(const double* __restrict__ driver, int use_pulses,
-                                               const vg_pulse* __restrict__ P, int np, double t,
-                                               const double* __restrict__ x, int n) {
-  if (driver) return driver[n];
-  if (use_pulses) return pulse_sum(P, np, t, x[n]);
-  return 0.0;
-}
 
 template <int NX>
 __global__ void __launch_bounds__(fft_threads<double>(NX)) k_poisson_fft_f64(
@@ -207,28 +93,9 @@ __global__ void __launch_bounds__(fft_threads<double>(NX)) k_poisson_fft_f64(
     const double* __restrict__ driver, int use_pulses, const vg_pulse* __restrict__ P, int np,
     const double* __restrict__ x, FieldTimeDev ft, const cx<double>* __restrict__ tw,
     double* __restrict__ e) {
-  constexpr int R = fft_radix<double>(NX);
-  constexpr int G = NX / R;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  cx<double>* s = reinterpret_cast<cx<double>*>(smem_raw);
-  const int t = threadIdx.x;
-  for (int n = t; n < NX; n += G) s[sp<double>(n)] = {is_density ? sub_rn(1.0, dens[n]) : dens[n], 0.0};
-  __syncthreads();
-  block_fft<double, NX, false>(s, t, tw);
-  // (1j * inv_kx) * Z = (0 + i k)(zr + i zi) = (0*zr - k*zi) + i (0*zi + k*zr)
-  for (int k = t; k < NX; k += G) {
-    const cx<double> z = s[sp<double>(k)];
-    const double ik = inv_kx[k];
-    s[sp<double>(k)] = {sub_rn(mul_rn(0.0, z.x), mul_rn(ik, z.y)), add_rn(mul_rn(0.0, z.y), mul_rn(ik, z.x))};
-  }
-  __syncthreads();
-  block_fft<double, NX, true>(s, t, tw);
-  const double tt = field_time(ft);
-  const double sc = 1.0 / NX;
-  for (int n = t; n < NX; n += G) {
-    const double self = s[sp<double>(n)].x * sc;
-    e[n] = add_rn(driver_value(driver, use_pulses, P, np, tt, x, n), self);
-  }
+  poisson_fft_body<NX>(dens, is_density, inv_kx, driver, use_pulses, P, np, x, ft, tw, e,
+                       reinterpret_cast<cx<double>*>(smem_raw), threadIdx.x);
 }
 
 // Direct DFT for lengths that are not powers of two (O(nx^2), one CTA).
@@ -320,33 +187,7 @@ __global__ void k_thomas_f64(double* __restrict__ f, int nrows, int nv, const do
   if (row >= nrows) return;
   const double vbar = dougherty ? mom[(size_t)row * mstride + vbar_col] : 0.0;
   const double vth = mom[(size_t)row * mstride + vth_col];
-  const double A = __ddiv_rn(-vth, dv_sq);
-  const double b = add_rn(1.0, mul_rn(nudt, __ddiv_rn(mul_rn(2.0, vth), dv_sq)));
-  auto drift = [&](int j) {
-    const double num = dougherty ? sub_rn(v[j], vbar) : v[j];
-    return __ddiv_rn(num * 0.5, dv);
-  };
-  auto sub_diag = [&](int j) { return mul_rn(nudt, add_rn(A, drift(j))); };      // a[j], j < nv-1
-  auto sup_diag = [&](int j) { return mul_rn(nudt, sub_rn(A, drift(j + 1))); };  // c[j], j < nv-1
-  double* fr = f + (size_t)row * nv;
-  double* br = bb + (size_t)row * nv;
-  double bprev = b, dprev = fr[0];
-  br[0] = b;
-  for (int j = 1; j < nv; ++j) {
-    const double m = __ddiv_rn(sub_diag(j - 1), bprev);
-    const double bj = sub_rn(b, mul_rn(m, sup_diag(j - 1)));
-    const double dj = sub_rn(fr[j], mul_rn(m, dprev));
-    br[j] = bj;
-    fr[j] = dj;
-    bprev = bj;
-    dprev = dj;
-  }
-  double xj = __ddiv_rn(dprev, bprev);
-  fr[nv - 1] = xj;
-  for (int j = nv - 2; j >= 0; --j) {
-    xj = __ddiv_rn(sub_rn(fr[j], mul_rn(sup_diag(j), xj)), br[j]);
-    fr[j] = xj;
-  }
+  thomas_row_f64(f + (size_t)row * nv, bb + (size_t)row * 2 * nv, nv, v, vbar, vth, dougherty, nudt, dv, dv_sq);
 }
 
 cudaError_t launch_thomas_f64(const vg_plan& p, double* f, const double* mom, int vbar_col, int vth_col,

@@ -284,6 +284,13 @@ int vg_sweep_state_ptr(vg_sweep* sweep, float** g, double** e);
  * estimator that is unbiased for undriven runs; rows <= 16384). */
 int vg_sweep_damping(vg_sweep* sweep, const double* e_hist, int32_t rows, double t0, double t_min, double t_max,
                      double* rate_out, double* freq_out, vg_stream stream);
+/* Synchronises the device; *uses_tma (may be NULL) says whether the x-drift
+ * loads its tiles through the tensor-memory accelerator (cp.async.bulk.tensor;
+ * every run must start on a whole row of nv floats, and the environment
+ * variable VG_SWEEP_NO_TMA, read at vg_sweep_create, must be unset or "0"), and
+ * *flags the bounded-wait events of that kernel since creation; VG_ERR_TIMEOUT
+ * if there were any (the affected steps are not valid). */
+int vg_sweep_status(vg_sweep* sweep, int32_t* flags, int32_t* uses_tma);
 /* per-kernel timing of vg_sweep_run_steps (same contract as vg_profile_*) */
 int vg_sweep_profile_enable(vg_sweep* sweep, int32_t enable);
 int vg_sweep_profile_read(vg_sweep* sweep, vg_prof_entry* out, int32_t max, int32_t* n_out);

@@ -92,6 +92,39 @@ def test_sweep_graph_equals_direct():
         np.testing.assert_array_equal(a.read_run(i)[0].cpu().numpy(), b.read_run(i)[0].cpu().numpy())
 
 
+def test_sweep_tma_x_drift_equals_plain_loads():
+    """The x-drift fed by the tensor-memory accelerator (the default for runs
+    that start on whole rows) gives the plain-load kernel's result to FP32
+    rounding: only the way the tiles reach the transform differs (the two
+    kernels may contract their products into FMAs differently).  More runs
+    than SMs exercise the persistent CTAs' double-buffered stages."""
+    import os
+    from vlapy_gb300.sweep import Sweep, sweep_config
+    runs = mixed_runs() + sweep_config(600, seed=3)
+    a = Sweep(runs)
+    os.environ["VG_SWEEP_NO_TMA"] = "1"
+    try:
+        b = Sweep(runs)
+    finally:
+        del os.environ["VG_SWEEP_NO_TMA"]
+    assert a.status() == (0, True)
+    assert b.status() == (0, False)
+    for sw in (a, b):
+        sw.reset()
+    ea, sa = a.history(6)
+    eb, sb = b.history(6)
+    a.run_steps(6, ea, sa)
+    b.run_steps(6, eb, sb)
+    torch.cuda.synchronize()
+    assert a.status()[0] == 0
+    ea, eb = ea.cpu().numpy(), eb.cpu().numpy()
+    assert np.isfinite(ea).all()
+    assert np.linalg.norm(ea - eb) <= 1e-6 * np.linalg.norm(eb)
+    ga, _ = a.get_state()
+    gb, _ = b.get_state()
+    assert float(torch.linalg.norm((ga - gb).double())) <= 1e-6 * float(torch.linalg.norm(gb.double()))
+
+
 def test_sweep_config_distribution():
     from vlapy_gb300.sweep import sweep_config
     runs = sweep_config(4096)

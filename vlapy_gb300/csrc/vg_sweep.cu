@@ -11,10 +11,13 @@
 // preceded once per call by the first half kick.  Kernels dispatch on the
 // item's shape to the same device bodies as the single-run path.
 #include <algorithm>
+#include <cstdlib>
 #include <cmath>
 #include <cstring>
 #include <map>
 #include <vector>
+
+#include <cuda.h>
 
 #include "vg_f32_body.cuh"
 #include "vg_internal.cuh"
@@ -139,11 +142,22 @@ __host__ __device__ constexpr int sweep_col_lanes(int nx) {
 __host__ __device__ constexpr int sweep_col_ld(int nx) {
   return nx == 256 ? sp_len<float>(nx) + 2 : (sp_len<float>(nx) | 1);
 }
+// shared memory of one x-drift item: the groups' padded sequences, then the
+// density-partial scratch (floats)
 template <int NX>
-__global__ void __launch_bounds__(SWEEP_BLOCK, sweep_col_radix(NX) == 16 ? VG_COL_MIN_BLOCKS_R16 : VG_COL_MIN_BLOCKS) k_sweep_col(const SweepRunDev* __restrict__ runs,
-                                                              const int2* __restrict__ items, float* g,
-                                                              const SweepConsts* __restrict__ scp,
-                                                              const cx<float>* __restrict__ tw, float2* dpart) {
+__host__ __device__ constexpr size_t sweep_col_work_bytes() {
+  return (size_t)(SWEEP_BLOCK / (NX / sweep_col_radix(NX))) * sweep_col_ld(NX) * sizeof(cx<float>) +
+         (size_t)(SWEEP_BLOCK / ((NX / sweep_col_radix(NX)) * sweep_col_lanes(NX))) * NX * sizeof(float);
+}
+
+// One (run, tile) item of the x-drift.  load(io, x0, stride, c) fills this
+// thread's R elements: io[i] = the column pair (c, c + 1) of the tile at
+// x = x0 + i stride.
+template <int NX, typename LoadFn>
+__device__ __forceinline__ void sweep_col_item(const SweepRunDev& r, int tile, float* g,
+                                               const SweepConsts* __restrict__ scp,
+                                               const cx<float>* __restrict__ tw, float2* dpart,
+                                               unsigned char* smem, LoadFn load) {
   constexpr int R = sweep_col_radix(NX);
   constexpr int G = NX / R;
   constexpr int W = sweep_col_w(NX);
@@ -152,26 +166,18 @@ __global__ void __launch_bounds__(SWEEP_BLOCK, sweep_col_radix(NX) == 16 ? VG_CO
   constexpr int NSET = SWEEP_BLOCK / SET;
   constexpr int LDG = sweep_col_ld(NX);
   static_assert(W == 2 * (SWEEP_BLOCK / G) && SET % 32 == 0 && NSET <= 15, "tile shape");
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int2 it = items[blockIdx.x];
-  const SweepRunDev r = runs[it.x];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int vr = warp * (32 / L) + lane / L;  // this lane's row slot
   const int t = vr & (G - 1), set = vr / G;
   const int grp = (lane & (L - 1)) + L * set;
-  cx<float>* sg = reinterpret_cast<cx<float>*>(smem_raw) + (size_t)grp * LDG;
-  float* red = reinterpret_cast<float*>(smem_raw + (size_t)(SWEEP_BLOCK / G) * LDG * sizeof(cx<float>));
+  cx<float>* sg = reinterpret_cast<cx<float>*>(smem) + (size_t)grp * LDG;
+  float* red = reinterpret_cast<float*>(smem + (size_t)(SWEEP_BLOCK / G) * LDG * sizeof(cx<float>));
   const GroupSync sync = {1u + (unsigned)set, (unsigned)SET, 0xffffffffu};
   const int nv = r.nv;
-  const int c = it.y * W + 2 * grp;  // this group's column pair (c, c + 1)
+  const int c = tile * W + 2 * grp;  // this group's column pair (c, c + 1)
   float* gc = g + r.g_off + c;
   cx<float> io[R];
-#pragma unroll
-  for (int i = 0; i < R; ++i) {
-    const float2 q = *reinterpret_cast<const float2*>(gc + (size_t)(t + i * G) * nv);
-    io[i].x = q.x;
-    io[i].y = q.y;
-  }
+  load(io, t, G, 2 * grp);
   block_fft_io<float, NX, false, R, 1>(sg, t, tw, sync, io);
   // theta(m) = m * (-dkx dt) v_col (kx = m dkx on the bins m <= NX/2); the angle
   // per unit m is the double-float product of kdt = -dkx dt and v (both split)
@@ -220,12 +226,152 @@ __global__ void __launch_bounds__(SWEEP_BLOCK, sweep_col_radix(NX) == 16 ? VG_CO
 #pragma unroll
     for (int q = 0; q < CNT; ++q) red[set * NX + t + (idx + q) * G] = d[q];
   __syncthreads();
-  float2* out = dpart + r.dp_off + (size_t)it.y * NX;
+  float2* out = dpart + r.dp_off + (size_t)tile * NX;
   for (int x = threadIdx.x; x < NX; x += SWEEP_BLOCK) {
     df32 acc = {0.f, 0.f};
 #pragma unroll
     for (int q = 0; q < NSET; ++q) acc = df_add(acc, {red[q * NX + x], 0.f});
     out[x] = make_float2(acc.hi, acc.lo);
+  }
+}
+
+template <int NX>
+__global__ void __launch_bounds__(SWEEP_BLOCK, sweep_col_radix(NX) == 16 ? VG_COL_MIN_BLOCKS_R16 : VG_COL_MIN_BLOCKS) k_sweep_col(const SweepRunDev* __restrict__ runs,
+                                                              const int2* __restrict__ items, float* g,
+                                                              const SweepConsts* __restrict__ scp,
+                                                              const cx<float>* __restrict__ tw, float2* dpart) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int2 it = items[blockIdx.x];
+  const SweepRunDev r = runs[it.x];
+  constexpr int W = sweep_col_w(NX);
+  // the first FFT pass reads its elements straight from global memory
+  const float* gt = g + r.g_off + (size_t)it.y * W;
+  const int nv = r.nv;
+  sweep_col_item<NX>(r, it.y, g, scp, tw, dpart, smem_raw, [&](auto& io, int x0, int stride, int col) {
+#pragma unroll
+    for (int i = 0; i < (int)(sizeof(io) / sizeof(io[0])); ++i) {
+      const float2 q = *reinterpret_cast<const float2*>(gt + (size_t)(x0 + i * stride) * nv + col);
+      io[i].x = q.x;
+      io[i].y = q.y;
+    }
+  });
+}
+
+// ---- the x-drift fed by the tensor-memory accelerator ----------------------
+// For each x class, one tensor map per nv class views the whole state as
+// rows of nv floats (every run starts on a row: its cell offset is a multiple
+// of its nv), with a box of NX rows x W columns: one (run, tile) item.
+// Persistent CTAs walk their items with two tile stages in shared memory: the
+// load of item i + 2 strides is issued (one thread, cp.async.bulk.tensor,
+// completion counted on the stage's mbarrier) as soon as every thread has
+// taken item i's elements into registers, so it overlaps the transforms of
+// items i and i + 1.  Every wait is bounded: after TMA_WAIT_NS of the global
+// timer without the stage's bytes the CTA records the event in *err, waits
+// (again bounded) for its copies in flight and stops.
+struct SweepTmaps {
+  CUtensorMap m[SWEEP_MAX_CLASSES];
+};
+constexpr unsigned long long TMA_WAIT_NS = 2000000000ull;  // 2 s of the global timer
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+// bounded wait for phase `parity` of an mbarrier; false when it ran out
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity, unsigned long long limit_ns) {
+  const unsigned long long t0 = global_ns();
+  while (true) {
+    uint32_t done;
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if (global_ns() - t0 > limit_ns) return false;
+  }
+}
+
+template <int NX>
+__host__ __device__ constexpr size_t sweep_col_tile_bytes() {
+  return (size_t)NX * sweep_col_w(NX) * sizeof(float);
+}
+// dynamic shared memory of the TMA kernel: two tile stages (128-byte
+// aligned), the item work area, two mbarriers
+template <int NX>
+__host__ __device__ constexpr size_t sweep_col_tma_smem() {
+  return 128 + 2 * sweep_col_tile_bytes<NX>() + sweep_col_work_bytes<NX>() + 16;
+}
+
+template <int NX>
+__global__ void __launch_bounds__(SWEEP_BLOCK, sweep_col_radix(NX) == 16 ? 2 : VG_COL_MIN_BLOCKS) k_sweep_col_tma(
+    const SweepRunDev* __restrict__ runs, const int2* __restrict__ items, int n_items, float* g,
+    const SweepConsts* __restrict__ scp, const cx<float>* __restrict__ tw, float2* dpart,
+    const __grid_constant__ SweepTmaps maps, int* err) {
+  constexpr int W = sweep_col_w(NX);
+  constexpr uint32_t TILE = (uint32_t)sweep_col_tile_bytes<NX>();
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  unsigned char* base = smem_raw + ((128 - (reinterpret_cast<uintptr_t>(smem_raw) & 127)) & 127);
+  float* tiles = reinterpret_cast<float*>(base);
+  unsigned char* work = base + 2 * TILE;
+  const uint32_t bar0 = (uint32_t)__cvta_generic_to_shared(work + sweep_col_work_bytes<NX>());
+  const uint32_t tile0 = (uint32_t)__cvta_generic_to_shared(tiles);
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar0) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar0 + 8) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  __syncthreads();
+  // one thread: expect the stage's bytes, then load item idx's box into it
+  auto issue = [&](int idx, int stage) {
+    const int2 it = items[idx];
+    const SweepRunDev r = runs[it.x];
+    const uint32_t bar = bar0 + 8 * stage;
+    const int cx0 = it.y * W, row0 = (int)(r.g_off / r.nv);
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"(TILE) : "memory");
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];\n" ::"r"(
+            tile0 + stage * TILE),
+        "l"(reinterpret_cast<uint64_t>(&maps.m[r.cls])), "r"(cx0), "r"(row0), "r"(bar)
+        : "memory");
+  };
+  const int stride = gridDim.x;
+  if (threadIdx.x == 0) {
+    if ((int)blockIdx.x < n_items) issue(blockIdx.x, 0);
+    if ((int)blockIdx.x + stride < n_items) issue(blockIdx.x + stride, 1);
+  }
+  int iter = 0;
+  for (int idx = blockIdx.x; idx < n_items; idx += stride, ++iter) {
+    const int stage = iter & 1;
+    const uint32_t parity = (uint32_t)((iter >> 1) & 1);
+    const bool ok = mbar_wait_bounded(bar0 + 8 * stage, parity, TMA_WAIT_NS);
+    if (__syncthreads_or(!ok)) {
+      // the stage never filled: record it, let the copies in flight land, stop
+      if (threadIdx.x == 0) {
+        atomicOr(err, 1);
+        int q = iter;
+        for (int j = idx; j < n_items && q < iter + 2; j += stride, ++q)
+          mbar_wait_bounded(bar0 + 8 * (q & 1), (uint32_t)((q >> 1) & 1), TMA_WAIT_NS);
+      }
+      __syncthreads();
+      return;
+    }
+    const int2 it = items[idx];
+    const SweepRunDev r = runs[it.x];
+    const float* tb = tiles + (size_t)stage * (TILE / sizeof(float));
+    sweep_col_item<NX>(r, it.y, g, scp, tw, dpart, work, [&](auto& io, int x0, int xs, int col) {
+#pragma unroll
+      for (int i = 0; i < (int)(sizeof(io) / sizeof(io[0])); ++i) {
+        const float2 q = *reinterpret_cast<const float2*>(tb + (size_t)(x0 + i * xs) * W + col);
+        io[i].x = q.x;
+        io[i].y = q.y;
+      }
+      // every thread has its elements: the stage is free for item idx + 2 strides
+      __syncthreads();
+      if (threadIdx.x == 0 && idx + 2 * stride < n_items) issue(idx + 2 * stride, stage);
+    });
   }
 }
 
@@ -546,6 +692,12 @@ struct vg_sweep {
   size_t field_smem;
   std::map<std::tuple<int, const void*, const void*, int, int, cudaStream_t>, cudaGraphExec_t> graphs;
   ProfState prof;
+  // x-drift through the tensor-memory accelerator, per x class
+  bool use_tma = false;           // some x class loads its tiles through the TMA
+  std::vector<char> tma_x;        // per x class (col_nx order): this class does
+  std::vector<SweepTmaps> tmaps;  // per x class, one map per nv class
+  int* err = nullptr;             // bounded-wait events of the TMA x-drift
+  int n_sm = 0;
 };
 
 namespace {
@@ -688,10 +840,19 @@ const char* const kSweepNames[SK_COUNT] = {"sweep_kick", "sweep_x_drift", "sweep
 
 template <int NX>
 cudaError_t sweep_col_launch(vg_sweep* s, int c, cudaStream_t st) {
-  constexpr int G = NX / sweep_col_radix(NX);
-  constexpr int SET = G * sweep_col_lanes(NX);
-  const size_t smem = (size_t)(SWEEP_BLOCK / G) * sweep_col_ld(NX) * sizeof(cx<float>) +
-                      (size_t)(SWEEP_BLOCK / SET) * NX * sizeof(float);
+  if (s->use_tma && s->tma_x[c]) {
+    const size_t smem = sweep_col_tma_smem<NX>();
+    cudaError_t err = ensure_smem((const void*)k_sweep_col_tma<NX>, smem);
+    if (err != cudaSuccess) return err;
+    int per_sm = 0;
+    err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep_col_tma<NX>, SWEEP_BLOCK, smem);
+    if (err != cudaSuccess) return err;
+    const int grid = std::max(1, std::min(s->col_count[c], std::max(1, per_sm) * s->n_sm));
+    k_sweep_col_tma<NX><<<grid, SWEEP_BLOCK, smem, st>>>(s->runs, s->col_items + s->col_first[c], s->col_count[c],
+                                                         s->g, s->consts, s->tw32, s->dpart, s->tmaps[c], s->err);
+    return cudaGetLastError();
+  }
+  const size_t smem = sweep_col_work_bytes<NX>();
   cudaError_t err = ensure_smem((const void*)k_sweep_col<NX>, smem);
   if (err != cudaSuccess) return err;
   k_sweep_col<NX><<<s->col_count[c], SWEEP_BLOCK, smem, st>>>(s->runs, s->col_items + s->col_first[c], s->g,
@@ -792,6 +953,61 @@ int sweep_sequence(vg_sweep* s, int nsteps, double* e_hist, double* s_hist, int 
                            }),
                            "sweep store"));
     }
+  }
+  return VG_OK;
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+// Tensor maps of the TMA x-drift: per x class and nv class, the state as rows
+// of nv floats, boxes of nx rows x W columns.  The TMA path is taken when
+// every run's cell offset is a multiple of its nv (so that it starts on a
+// row), the tile is at most 256 elements along each axis (the box limit), the
+// driver exposes cuTensorMapEncodeTiled and VG_SWEEP_NO_TMA is unset or "0";
+// otherwise the x-drift loads its tiles with ordinary loads.
+int sweep_setup_tma(vg_sweep* s) {
+  s->use_tma = false;
+  const char* off = std::getenv("VG_SWEEP_NO_TMA");
+  if (off && *off && std::strcmp(off, "0") != 0) return VG_OK;
+  for (const SweepRunDev& r : s->runs_h)
+    if (r.g_off % r.nv != 0 || r.W % 4 != 0) return VG_OK;
+  int dev = 0;
+  SW_CHECK(cuda_status(cudaGetDevice(&dev), "device"));
+  SW_CHECK(cuda_status(cudaDeviceGetAttribute(&s->n_sm, cudaDevAttrMultiProcessorCount, dev), "device"));
+  void* fn = nullptr;
+  cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+  if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+      q != cudaDriverEntryPointSuccess || !fn) {
+    cudaGetLastError();
+    return VG_OK;
+  }
+  EncodeTiledFn encode = reinterpret_cast<EncodeTiledFn>(fn);
+  s->tmaps.assign(s->col_nx.size(), SweepTmaps{});
+  s->tma_x.assign(s->col_nx.size(), 0);
+  for (size_t xc = 0; xc < s->col_nx.size(); ++xc) {
+    const int nx = s->col_nx[xc];
+    std::memset(&s->tmaps[xc], 0, sizeof(SweepTmaps));
+    if (sweep_col_w(nx) > 256 || nx > 256) continue;  // a TMA box is at most 256 along each axis
+    for (size_t c = 0; c < s->nv_of_class.size(); ++c) {
+      const int nv = s->nv_of_class[c];
+      if (sweep_col_w(nx) > nv) continue;  // no run of this nx has this nv (nv >= W for every run)
+      const cuuint64_t dims[2] = {(cuuint64_t)nv, (cuuint64_t)(s->cells / nv)};
+      const cuuint64_t strides[1] = {(cuuint64_t)nv * sizeof(float)};
+      const cuuint32_t box[2] = {(cuuint32_t)sweep_col_w(nx), (cuuint32_t)nx};
+      const cuuint32_t estr[2] = {1, 1};
+      const CUresult rc = encode(&s->tmaps[xc].m[c], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, s->g, dims, strides, box,
+                                 estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                 CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+      if (rc != CUDA_SUCCESS) {
+        set_error("cuTensorMapEncodeTiled failed (" + std::to_string((int)rc) + ") for the x-drift tile of nx=" +
+                  std::to_string(nx) + ", nv=" + std::to_string(nv));
+        return VG_ERR_CUDA;
+      }
+    }
+    s->tma_x[xc] = 1;
+    s->use_tma = true;
   }
   return VG_OK;
 }
@@ -935,6 +1151,8 @@ int vg_sweep_create(const vg_sweep_desc* d, vg_sweep** out) {
   s->n_field = (int)field.size();
   s->field_smem = field_smem;
   SW_TRY(cuda_status(ensure_smem((const void*)k_sweep_field, field_smem), "sweep smem"));
+  SW_TRY(sw_alloc<int>(s, &s->err, 1, nullptr, "sweep status"));
+  SW_TRY(sweep_setup_tma(s));
   SW_TRY(cuda_status(cudaDeviceSynchronize(), "sweep setup"));
 #undef SW_TRY
   *out = s;
@@ -1069,6 +1287,23 @@ int vg_sweep_damping(vg_sweep* s, const double* e_hist, int32_t rows, double t0,
   k_sweep_damping<<<s->n_runs, 256, smem, st>>>(s->runs, e_hist, (int)s->x_points, rows, t0, s->dt, t_min, t_max,
                                                  rate_out, freq_out);
   return cuda_status(cudaGetLastError(), "sweep damping");
+}
+
+int vg_sweep_status(vg_sweep* s, int32_t* flags, int32_t* uses_tma) {
+  if (!s) {
+    set_error("null sweep");
+    return VG_ERR_ARG;
+  }
+  int h = 0;
+  SW_CHECK(cuda_status(cudaDeviceSynchronize(), "sweep status"));
+  SW_CHECK(cuda_status(cudaMemcpy(&h, s->err, sizeof(int), cudaMemcpyDeviceToHost), "sweep status"));
+  if (flags) *flags = h;
+  if (uses_tma) *uses_tma = s->use_tma ? 1 : 0;
+  if (h) {
+    set_error("a bounded wait of the TMA x-drift ran out");
+    return VG_ERR_TIMEOUT;
+  }
+  return VG_OK;
 }
 
 int vg_sweep_state_ptr(vg_sweep* s, float** g, double** e) {

@@ -176,6 +176,15 @@ class Sweep:
         o = int(self.x_offsets[i])
         return e_hist[:, o:o + self.runs[i]["nx"]]
 
+    def status(self):
+        """(flags, uses_tma) after synchronising the device: the bounded-wait
+        events of the TMA x-drift since creation (a VlagpuError with
+        VG_ERR_TIMEOUT when there were any) and whether the x-drift loads its
+        tiles through the TMA."""
+        flags, tma = C.c_int32(), C.c_int32()
+        check(self._lib.vg_sweep_status(self._h, C.byref(flags), C.byref(tma)), "sweep status")
+        return int(flags.value), bool(tma.value)
+
     def profile(self, enable):
         check(self._lib.vg_sweep_profile_enable(self._h, int(bool(enable))), "profile")
 

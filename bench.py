@@ -43,6 +43,8 @@ WORKLOADS = {
     "landau": dict(nx=32, nv=512, k=0.3, vmax=6.4, dt=0.1, nu=0.0, op="dg", kind="landau"),
     # the learned path's network alone: one correction of 2048 coarse runs x 64 x rows
     "corrector": dict(kind="corrector", n_runs=2048, nx=64, vmax=6.4),
+    # the plain FP64 GPU method on the sweep's runs: the batched FP64 step alone
+    "fp64sweep": dict(kind="fp64sweep", n_runs=4096, seed=20261203, vmax=6.4, dt=0.1),
 }
 
 
@@ -312,6 +314,27 @@ def run_sweep_gpu(args, w, rank, world, global_rank=0):
     return ms, prof, clk, (e2e_sec, 0, d2h), sw
 
 
+def single_run_summary(args, name, precision, steps=10, warmup=3):
+    """One of the single-run workloads (large: 4096 x 8192 two-stream; driven:
+    64 x 1024 with the sin^2 driver) timed as the main bench times its
+    workload: CUDA events around a graph of `steps` steps, then one profiled
+    step, then e2e through the C-ABI call with the step's time and driver row
+    copied in from pinned host memory and its stored fields and series read
+    back, every step."""
+    w = WORKLOADS[name]
+    sub = argparse.Namespace(steps=steps, warmup=warmup, prof_steps=1, precision=precision)
+    ms, prof, clk, e2e, plan = run_gpu(sub, w, 0, 1)
+    cells = w["nx"] * w["nv"]
+    e2e_sec, h2d, d2h = e2e
+    out = {"precision": precision, "ms_per_step": ms / steps, "value": cells * steps / (ms / 1e3),
+           "unit": "cell-updates/s",
+           "e2e": {"value": cells * steps / e2e_sec, "unit": "cell-updates/s", "h2d_bytes_per_step": h2d,
+                   "d2h_bytes_per_step": d2h},
+           "kernels_ms_per_step": {k: d["total_ms"] for k, d in prof.items()}}
+    plan.close()
+    return out
+
+
 def fp64_plain_sweep(w, steps=2):
     """Plain FP64 GPU method on the whole sweep: every run of the workload in
     one batched FP64 step (vg_batch: the reference's FP64 step per run, the
@@ -372,12 +395,10 @@ def learned_path(args, w):
     """The learned coarse-velocity path (runs of the sweep distribution at
     nx = 64): train the corrector on pairs from fine (nv = 1024) runs, judge
     the corrected coarse (nv = 128) runs against the fine runs on held-out
-    seeds, and time the corrected coarse step against the fine FP32 sweep
-    and the plain FP64 step of the same runs."""
+    seeds against fine FP64 runs, and time the corrected coarse step against
+    the fine FP32 sweep and the batched FP64 step of the same runs."""
     import torch
     from vlapy_gb300 import corrector as cm
-    from vlapy_gb300 import initializers as I
-    from vlapy_gb300.plan import Plan
     from vlapy_gb300.sweep import Sweep
     nsteps, nx = SWEEP_STEPS, 64
     t0 = time.perf_counter()
@@ -399,8 +420,20 @@ def learned_path(args, w):
     zero.close()
     loss = cm.evaluate(corr, held)
     del held
-    # held-out rollouts: fine FP32 sweep (the judge), coarse, corrected coarse
+    # held-out rollouts: fine FP64 (the judge: the batched FP64 step, the
+    # reference's arithmetic), fine FP32 sweep, coarse, corrected coarse
+    from vlapy_gb300.batch import Batch64
     ev = cm.corrector_runs(n_eval, seed=6)
+    judge = Batch64([dict(r, nv=1024) for r in ev], vmax=w["vmax"], dt=w["dt"])
+    fj, ej = judge.initial_state()
+    eh64, sh64 = judge.history(nsteps)
+    chunk = 100
+    t64 = time.perf_counter()
+    for c0 in range(0, nsteps, chunk):
+        judge.run_steps(fj, ej, min(chunk, nsteps - c0), eh64, sh64, row0=c0)
+    torch.cuda.synchronize()
+    fp64_eval_s = time.perf_counter() - t64
+    del fj, ej
     fine, coarse, corrected = (Sweep([dict(r, nv=nv) for r in ev]) for nv in (1024, cm.NV, cm.NV))
     hists = []
     for sw in (fine, coarse):
@@ -413,10 +446,15 @@ def learned_path(args, w):
     cm.run_corrected(corrected, corr, nsteps, ek, sk)
     torch.cuda.synchronize()
     t = w["dt"] * np.arange(1, nsteps + 1)
-    dr_c = _damping_errors(t, fine, hists[0][0], coarse, hists[1][0])
-    dr_k = _damping_errors(t, fine, hists[0][0], corrected, ek)
+    dr_f = _damping_errors(t, judge, eh64, fine, hists[0][0])
+    dr_c = _damping_errors(t, judge, eh64, coarse, hists[1][0])
+    dr_k = _damping_errors(t, judge, eh64, corrected, ek)
+    # mean e^2 per run and step; the batch's series rows are in its stored order
+    e2_64 = sh64[:, torch.as_tensor(judge.slot, device=sh64.device), 3].cpu().numpy()
     e2 = [h[1][:, :, 3].cpu().numpy() for h in hists] + [sk[:, :, 3].cpu().numpy()]
-    e2_err = [np.linalg.norm(e - e2[0], axis=0) / np.linalg.norm(e2[0], axis=0) for e in e2[1:]]
+    e2_err = [np.linalg.norm(e - e2_64, axis=0) / np.linalg.norm(e2_64, axis=0) for e in e2]
+    judge.close()
+    del eh64, sh64
 
     def stats(a):
         a = a[np.isfinite(a)]
@@ -463,35 +501,33 @@ def learned_path(args, w):
                                                     "projection; padded channels counted as issued"}
             big.close()
         sw.close()
-    # plain FP64 GPU step of one 64x1024 run of the distribution
-    r = runs[0]
-    dx, x, kx, inv = I.initialize_spatial_quantities(0.0, 2 * np.pi / r["k"], nx)
-    dv, v, kv = I.initialize_velocity_quantities(w["vmax"], 1024)
-    pl = Plan(nx, 1024, x, v, kx, kv, inv, dx, dv, dt=w["dt"], nu=max(r["nu"], 1e-4), collision="dg")
-    f = torch.as_tensor(I.initialize_distribution(nx, 1024, w["vmax"]) * (1 + r["amplitude"] * np.cos(r["k"] * x))[:, None],
-                        device="cuda")
-    e = torch.zeros(nx, dtype=torch.float64, device="cuda")
-    tb = torch.as_tensor(w["dt"] * np.arange(8), device="cuda")
-    pl.run_steps(f, e, None, tb, None, 0, 2, use_graph=False)
+    # plain FP64 GPU method on the same 2048 runs: the batched FP64 step
+    b64 = Batch64([dict(r, nv=1024) for r in runs], vmax=w["vmax"], dt=w["dt"])
+    fb, eb = b64.initial_state()
+    b64.run_steps(fb, eb, 1)
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
-    pl.run_steps(f, e, None, tb, None, 0, 3, use_graph=False)
+    b64.run_steps(fb, eb, 3)
     e1.record()
     torch.cuda.synchronize()
     fp64_ms = e0.elapsed_time(e1) / 3
-    pl.close()
-    out["plain_fp64"] = {"ms_per_run_step": fp64_ms, "runs_per_s": 1.0 / (fp64_ms / 1e3 * nsteps)}
+    b64.close()
+    del fb, eb
+    out["plain_fp64_batched"] = {"ms_per_step": fp64_ms, "runs_per_s": len(runs) / (fp64_ms / 1e3 * nsteps)}
     return {
         "workload": "%d training runs (seed 5), 64 validation runs (seed 7) choosing among 3 trained seeds, "
                     "%d held-out runs (seed 6) of the sweep distribution at nx=64; fine nv=1024, coarse nv=128, "
                     "vmax=6.4, dt=0.1, %d steps" % (args.learned_train, n_eval, nsteps),
         "pairs_s": gen_s, "train_s": train_s, "model_selection": selection, "tau": tau,
         "heldout_one_step_loss": {"uncorrected": base_loss, "corrected": loss, "ratio": loss / base_loss},
-        "damping_rate_rel_err_vs_fine": {"coarse": stats(dr_c), "corrected": stats(dr_k)},
-        "field_energy_history_rel_err_vs_fine": {"coarse": stats(e2_err[0]), "corrected": stats(e2_err[1])},
+        "damping_rate_rel_err_vs_fine_fp64": {"fine_fp32": stats(dr_f), "coarse": stats(dr_c),
+                                               "corrected": stats(dr_k)},
+        "field_energy_history_rel_err_vs_fine_fp64": {"fine_fp32": stats(e2_err[0]), "coarse": stats(e2_err[1]),
+                                                      "corrected": stats(e2_err[2])},
         "throughput_2048_runs": out,
-        "judge": "fine runs of the FP32 batched sweep (the GPU tests hold it to the FP64 oracle)",
+        "judge": "fine (nv = 1024) runs of the batched FP64 step (vg_batch: the reference's FP64 arithmetic), "
+                 "%d runs x %d steps in %.1f s" % (n_eval, nsteps, fp64_eval_s),
     }
 
 
@@ -650,6 +686,28 @@ def cpu_baseline(w, steps, reps_cap=3):
     return nx * nv * n / dt, n, dt
 
 
+def main_fp64sweep(args, w, rank, world):
+    """The batched FP64 step on the sweep's runs (the plain FP64 GPU method)
+    as its own workload: K graph-replayed steps timed with CUDA events after
+    one untimed step, then one profiled step.  The default workload reports
+    the same measurement as fp64_plain_gpu; this one exists to profile the
+    FP64 kernels alone."""
+    import torch
+    from vlapy_gb300 import _lib
+    if rank != 0:
+        return
+    _lib.load()
+    out = fp64_plain_sweep(w, steps=args.steps)
+    cells = out["cells_per_s"] * out["ms_per_step"] / 1e3
+    line = {"metric": "cell-updates/s", "value": out["cells_per_s"], "unit": "cell-updates/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": 1, "ms_per_step": out["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "fp64sweep", "n_runs": w["n_runs"], "seed": w["seed"], "cells": cells},
+            "runs_per_s": out["runs_per_s"], "kernels_ms_per_step": out["kernels_ms_per_step"]}
+    print(json.dumps(line))
+    torch.cuda.synchronize()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -676,6 +734,8 @@ def main():
         return main_sweep(args, w, rank, world)
     if w["kind"] == "corrector":
         return main_corrector(args, w, rank, world)
+    if w["kind"] == "fp64sweep":
+        return main_fp64sweep(args, w, rank, world)
     cells = w["nx"] * w["nv"]
     metric = "cell-updates/s"
     cfg = {"workload": args.workload, "nx": w["nx"], "nv": w["nv"], "dt": w["dt"], "nu": w["nu"],
@@ -770,6 +830,7 @@ def main_sweep(args, w, rank, world):
     replicas.init(world)
     ms, prof, clk, e2e, sw = run_sweep_gpu(args, w, int(os.environ.get("LOCAL_RANK", rank)), world, rank)
     cells = sw.cells
+    tma_flags, tma = sw.status()
     # every rank advances its own shard: units summed, time the slowest rank's
     t_max, total_cells, value = replicas.aggregate(ms, cells * args.steps, world)
     runs_per_s = world * sw.n_runs / (t_max / args.steps / 1e3 * SWEEP_STEPS)
@@ -788,6 +849,14 @@ def main_sweep(args, w, rank, world):
     if not args.no_fp64_compare:
         fp64 = fp64_plain_sweep(w)
     learned = None if args.no_learned else learned_path(args, w)
+    singles = None
+    if not args.no_fp64_compare:
+        import torch
+        singles = {}
+        for name, prec, k in (("large", "fp32-deltaf", 20), ("large", "fp64", 3), ("driven", "fp32-deltaf", 50),
+                              ("driven", "fp64", 20)):
+            singles["%s_%s" % (name, prec)] = single_run_summary(args, name, prec, steps=k)
+            torch.cuda.empty_cache()
     cpu = None
     if not args.no_cpu_baseline:
         cval, crps, cores, n, steps, wall = cpu_baseline_sweep(w, n_sample=36, steps=360)
@@ -800,6 +869,8 @@ def main_sweep(args, w, rank, world):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": cfg,
         "runs_per_s": runs_per_s,
         "fp64_plain_gpu": fp64,
+        "single_runs": singles,
+        "x_drift_tma": tma,
         "learned_path": learned,
         "e2e": {"value": e2e_value, "unit": "cell-updates/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},

@@ -102,62 +102,6 @@ __device__ __forceinline__ int sp_step(int spbase, int base, int m) {
   else return sp<T>(base + m * S);
 }
 
-// FP32 rotation by exp(-+i pi j / 16), j = 1..15 except 8, with the exact
-// constants split as hi + lo and applied as c_hi x + (c_lo x + ...), so each
-// component is rounded (nearly) once from the exact product.  The nearest
-// floats to cos and sin alone carry errors of up to 6e-8 in phase and in
-// magnitude (for every j their |c + i s| is below 1), and an FFT applies these
-// constants on every pass of every transform: a state transformed back and
-// forth thousands of times (the kicks transform every row twice per step)
-// accumulates them as a drift of its spectrum.
-template <int Q>
-struct Rot32 {  // cos, sin of pi Q / 16, Q = 1..7
-  static constexpr double C = Q == 1 ? 0.98078528040323044913 : Q == 2 ? 0.92387953251128675613
-                            : Q == 3 ? 0.83146961230254523708 : Q == 4 ? 0.70710678118654752440
-                            : Q == 5 ? 0.55557023301960222474 : Q == 6 ? 0.38268343236508977173
-                            : 0.19509032201612826785;
-  static constexpr double S = Q == 1 ? 0.19509032201612826785 : Q == 2 ? 0.38268343236508977173
-                            : Q == 3 ? 0.55557023301960222474 : Q == 4 ? 0.70710678118654752440
-                            : Q == 5 ? 0.83146961230254523708 : Q == 6 ? 0.92387953251128675613
-                            : 0.98078528040323044913;
-  static constexpr float CH = (float)C;
-  static constexpr float SH = (float)S;
-  static constexpr float CL = (float)(C - (double)(float)C);
-  static constexpr float SL = (float)(S - (double)(float)S);
-};
-template <int Q, bool NEG_C, bool INV>
-__device__ __forceinline__ cx<float> rot32_f32(cx<float> a) {
-  using K = Rot32<Q>;
-  // c = +-cos, s = sin of the rotation angle pi j / 16
-  constexpr float ch = NEG_C ? -K::CH : K::CH, sh = K::SH;
-  constexpr float cl = NEG_C ? -K::CL : K::CL, sl = K::SL;
-  if (INV)
-    return {fmaf(ch, a.x, fmaf(-sh, a.y, fmaf(cl, a.x, -sl * a.y))),
-            fmaf(sh, a.x, fmaf(ch, a.y, fmaf(sl, a.x, cl * a.y)))};
-  return {fmaf(ch, a.x, fmaf(sh, a.y, fmaf(cl, a.x, sl * a.y))),
-          fmaf(ch, a.y, fmaf(-sh, a.x, fmaf(cl, a.y, -sl * a.x)))};
-}
-template <bool INV>
-__device__ __forceinline__ cx<float> rot_const_f32(int j, cx<float> a) {
-  switch (j) {
-    case 1: return rot32_f32<1, false, INV>(a);
-    case 2: return rot32_f32<2, false, INV>(a);
-    case 3: return rot32_f32<3, false, INV>(a);
-    case 4: return rot32_f32<4, false, INV>(a);
-    case 5: return rot32_f32<5, false, INV>(a);
-    case 6: return rot32_f32<6, false, INV>(a);
-    case 7: return rot32_f32<7, false, INV>(a);
-    // j = 9..15: cos(pi j / 16) = -cos(pi (16 - j) / 16), equal sines
-    case 9: return rot32_f32<7, true, INV>(a);
-    case 10: return rot32_f32<6, true, INV>(a);
-    case 11: return rot32_f32<5, true, INV>(a);
-    case 12: return rot32_f32<4, true, INV>(a);
-    case 13: return rot32_f32<3, true, INV>(a);
-    case 14: return rot32_f32<2, true, INV>(a);
-    default: return rot32_f32<1, true, INV>(a);
-  }
-}
-
 // multiply by exp(-+2 pi i k / R), forward sign '-' unless INV
 template <typename T, int R, bool INV>
 __device__ __forceinline__ cx<T> rot_const(int k, cx<T> a) {
@@ -165,13 +109,9 @@ __device__ __forceinline__ cx<T> rot_const(int k, cx<T> a) {
   if (k == 0) return a;
   if (4 * k == R) return INV ? cx<T>{-a.y, a.x} : cx<T>{a.y, -a.x};
   const int j = (32 / R) * k;
-  if constexpr (sizeof(T) == 4) {
-    return rot_const_f32<INV>(j, a);
-  } else {
-    const T c = (T)cos32(j), s = (T)sin32(j);
-    if (INV) return {a.x * c - a.y * s, a.x * s + a.y * c};
-    return {a.x * c + a.y * s, a.y * c - a.x * s};
-  }
+  const T c = (T)cos32(j), s = (T)sin32(j);
+  if (INV) return {a.x * c - a.y * s, a.x * s + a.y * c};
+  return {a.x * c + a.y * s, a.y * c - a.x * s};
 }
 
 template <typename T, int R, bool INV>

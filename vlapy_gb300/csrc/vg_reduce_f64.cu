@@ -2,8 +2,9 @@
 //
 // Every trapz over v and every mean over x is evaluated with NumPy's pairwise
 // summation tree (a table built at plan creation): leaves of <= 128 terms are
-// summed with eight interleaved accumulators, one leaf per thread, and one
-// thread per moment replays the post-order combine program.  Products use
+// summed with eight interleaved accumulators (one thread per accumulator chain
+// in the row moments), and one thread per moment replays the post-order
+// combine program.  Products use
 // explicitly rounded intrinsics so nvcc cannot contract them into FMAs.  With
 // f equal, densities and moments are then bit-identical to the reference's
 // np.trapz (vlapy/core/field.py:36, vlapy/core/step.py:164-223).
@@ -13,37 +14,83 @@
 namespace vg {
 
 
+// One CTA per row.  The work of a NumPy pairwise sum is spread over the
+// threads without changing a single rounding: (A) the integrand products of a
+// group of qg moments are formed once per element into shared memory; (B)
+// every leaf of <= 128 terms is NumPy's eight interleaved accumulators, each
+// a serial chain that one thread runs; (C) one thread per leaf adds the eight
+// in NumPy's order plus the tail terms; then one thread per moment replays
+// the combine program over the leaves.  Moments of the second phase
+// (MOM_DG2) use the vbar the first phase produced.
 __global__ void k_row_moments_f64(const double* __restrict__ f, int nv, const double* __restrict__ v,
                                   const double* __restrict__ v_pow, MomSpec spec,
                                   const int* __restrict__ table, double dv,
-                                  double* __restrict__ out, int ostride) {
+                                  double* __restrict__ out, int ostride, int qg) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  double* row = reinterpret_cast<double*>(smem_raw);
   const int nl = table[0];
-  double* leaf = row + nv;               // [nm][nl]
+  double* prod = reinterpret_cast<double*>(smem_raw);  // [qg][nv]
+  double* acc = prod + (size_t)qg * nv;               // [qg][nl][8]
+  double* leaf = acc + (size_t)qg * nl * 8;           // [nm][nl]
   __shared__ double res[MOM_STRIDE];
   const size_t r = blockIdx.x;
-  for (int j = threadIdx.x; j < nv; j += blockDim.x) row[j] = f[r * nv + j];
-  __syncthreads();
+  const double* fr = f + r * nv;
   const int* leaves = table + 2;
+  const int nm = spec.nm;
   for (int phase = 0; phase < 2; ++phase) {
-    for (int idx = threadIdx.x; idx < spec.nm * nl; idx += blockDim.x) {
-      const int q = idx / nl, L = idx - q * nl;
-      const int kind = spec.kind[q];
-      if ((kind == MOM_DG2) != (phase == 1)) continue;
-      const int arg = spec.arg[q];
-      const double vbar = kind == MOM_DG2 ? res[arg] : 0.0;
-      auto term = [&](int j) {
-        const double p0 = mom_product(kind, arg, row[j], j, v, v_pow, nv, vbar);
-        const double p1 = mom_product(kind, arg, row[j + 1], j + 1, v, v_pow, nv, vbar);
-        return mul_rn(dv, add_rn(p1, p0)) * 0.5;
-      };
-      leaf[q * nl + L] = leaf_sum(leaves[2 * L], leaves[2 * L + 1], term);
+    for (int q0 = 0; q0 < nm; q0 += qg) {
+      auto active = [&](int q) { return q < nm && (spec.kind[q] == MOM_DG2) == (phase == 1); };
+      // (A) products p_q(j)
+      for (int idx = threadIdx.x; idx < qg * nv; idx += blockDim.x) {
+        const int qq = idx / nv, j = idx - qq * nv, q = q0 + qq;
+        if (!active(q)) continue;
+        const int kind = spec.kind[q], arg = spec.arg[q];
+        const double vbar = kind == MOM_DG2 ? res[arg] : 0.0;
+        prod[idx] = mom_product(kind, arg, fr[j], j, v, v_pow, nv, vbar);
+      }
+      __syncthreads();
+      // trapz term j: (dv * (p(j + 1) + p(j))) / 2
+      auto term = [&](const double* pq, int j) { return mul_rn(dv, add_rn(pq[j + 1], pq[j])) * 0.5; };
+      // (B) the accumulator chains
+      for (int idx = threadIdx.x; idx < qg * nl * 8; idx += blockDim.x) {
+        const int qq = idx / (nl * 8), rem = idx - qq * nl * 8, L = rem >> 3, a = rem & 7;
+        if (!active(q0 + qq) || nv < 2) continue;
+        const double* pq = prod + (size_t)qq * nv;
+        const int st = leaves[2 * L], len = leaves[2 * L + 1];
+        if (len < 8) {
+          if (a == 0) {
+            double x = 0.0;
+            for (int i = 0; i < len; ++i) x = add_rn(x, term(pq, st + i));
+            acc[(size_t)qq * nl * 8 + L * 8] = x;
+          }
+          continue;
+        }
+        const int stop = len - (len % 8);
+        double x = term(pq, st + a);
+        for (int i = 8 + a; i < stop; i += 8) x = add_rn(x, term(pq, st + i));
+        acc[(size_t)qq * nl * 8 + L * 8 + a] = x;
+      }
+      __syncthreads();
+      // (C) the leaves
+      for (int idx = threadIdx.x; idx < qg * nl; idx += blockDim.x) {
+        const int qq = idx / nl, L = idx - qq * nl, q = q0 + qq;
+        if (!active(q) || nv < 2) continue;
+        const double* pq = prod + (size_t)qq * nv;
+        const double* ac = acc + (size_t)qq * nl * 8 + L * 8;
+        const int st = leaves[2 * L], len = leaves[2 * L + 1];
+        double x;
+        if (len < 8) {
+          x = ac[0];
+        } else {
+          x = add_rn(add_rn(add_rn(ac[0], ac[1]), add_rn(ac[2], ac[3])), add_rn(add_rn(ac[4], ac[5]), add_rn(ac[6], ac[7])));
+          for (int i = len - (len % 8); i < len; ++i) x = add_rn(x, term(pq, st + i));
+        }
+        leaf[(size_t)q * nl + L] = x;
+      }
+      __syncthreads();
     }
-    __syncthreads();
-    for (int q = threadIdx.x; q < spec.nm; q += blockDim.x) {
+    for (int q = threadIdx.x; q < nm; q += blockDim.x) {
       if ((spec.kind[q] == MOM_DG2) != (phase == 1)) continue;
-      const double val = nv > 1 ? combine_leaves(table, leaf + q * nl) : 0.0;
+      const double val = nv > 1 ? combine_leaves(table, leaf + (size_t)q * nl) : 0.0;
       res[q] = val;
       out[r * ostride + q] = val;
     }
@@ -53,10 +100,15 @@ __global__ void k_row_moments_f64(const double* __restrict__ f, int nv, const do
 
 cudaError_t launch_row_moments_f64(const vg_plan& p, const double* f, const MomSpec& spec,
                                    double* out, int out_stride, cudaStream_t s) {
-  const size_t smem = ((size_t)p.nv + (size_t)spec.nm * p.pw_v_leaves) * sizeof(double);
+  // products of as many moments at once as fit in 64 KB (at least one)
+  const int nm = spec.nm;
+  int qg = (int)(65536 / ((size_t)p.nv * sizeof(double)));
+  qg = qg < 1 ? 1 : (qg > nm ? nm : qg);
+  const size_t nl = (size_t)p.pw_v_leaves;
+  const size_t smem = ((size_t)qg * p.nv + (size_t)qg * nl * 8 + (size_t)nm * nl) * sizeof(double);
   cudaError_t err = ensure_smem((const void*)k_row_moments_f64, smem);
   if (err != cudaSuccess) return err;
-  k_row_moments_f64<<<p.nx, 256, smem, s>>>(f, p.nv, p.v, p.v_pow, spec, p.pw_v, p.dv, out, out_stride);
+  k_row_moments_f64<<<p.nx, 256, smem, s>>>(f, p.nv, p.v, p.v_pow, spec, p.pw_v, p.dv, out, out_stride, qg);
   return cudaGetLastError();
 }
 

@@ -261,13 +261,14 @@ __global__ void __launch_bounds__(SWEEP_BLOCK, sweep_col_radix(NX) == 16 ? VG_CO
 // For each x class, one tensor map per nv class views the whole state as
 // rows of nv floats (every run starts on a row: its cell offset is a multiple
 // of its nv), with a box of NX rows x W columns: one (run, tile) item.
-// Persistent CTAs walk their items with two tile stages in shared memory: the
-// load of item i + 2 strides is issued (one thread, cp.async.bulk.tensor,
+// Persistent CTAs walk their items with one tile stage in shared memory: the
+// load of a CTA's next item is issued (one thread, cp.async.bulk.tensor,
 // completion counted on the stage's mbarrier) as soon as every thread has
-// taken item i's elements into registers, so it overlaps the transforms of
-// items i and i + 1.  Every wait is bounded: after TMA_WAIT_NS of the global
-// timer without the stage's bytes the CTA records the event in *err, waits
-// (again bounded) for its copies in flight and stops.
+// taken the current item's elements into registers, so it overlaps the
+// current item's transforms; one stage keeps the kernel at the plain
+// kernel's CTAs per SM.  Every wait is bounded: after TMA_WAIT_NS of the
+// global timer without the stage's bytes the CTA records the event in *err,
+// waits (again bounded) for its copy in flight and stops.
 struct SweepTmaps {
   CUtensorMap m[SWEEP_MAX_CLASSES];
 };
@@ -297,15 +298,15 @@ template <int NX>
 __host__ __device__ constexpr size_t sweep_col_tile_bytes() {
   return (size_t)NX * sweep_col_w(NX) * sizeof(float);
 }
-// dynamic shared memory of the TMA kernel: two tile stages (128-byte
-// aligned), the item work area, two mbarriers
+// dynamic shared memory of the TMA kernel: the tile stage (128-byte
+// aligned), the item work area, the mbarrier
 template <int NX>
 __host__ __device__ constexpr size_t sweep_col_tma_smem() {
-  return 128 + 2 * sweep_col_tile_bytes<NX>() + sweep_col_work_bytes<NX>() + 16;
+  return 128 + sweep_col_tile_bytes<NX>() + sweep_col_work_bytes<NX>() + 16;
 }
 
 template <int NX>
-__global__ void __launch_bounds__(SWEEP_BLOCK, sweep_col_radix(NX) == 16 ? 2 : VG_COL_MIN_BLOCKS) k_sweep_col_tma(
+__global__ void __launch_bounds__(SWEEP_BLOCK, sweep_col_radix(NX) == 16 ? VG_COL_MIN_BLOCKS_R16 : VG_COL_MIN_BLOCKS) k_sweep_col_tma(
     const SweepRunDev* __restrict__ runs, const int2* __restrict__ items, int n_items, float* g,
     const SweepConsts* __restrict__ scp, const cx<float>* __restrict__ tw, float2* dpart,
     const __grid_constant__ SweepTmaps maps, int* err) {
@@ -313,64 +314,54 @@ __global__ void __launch_bounds__(SWEEP_BLOCK, sweep_col_radix(NX) == 16 ? 2 : V
   constexpr uint32_t TILE = (uint32_t)sweep_col_tile_bytes<NX>();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   unsigned char* base = smem_raw + ((128 - (reinterpret_cast<uintptr_t>(smem_raw) & 127)) & 127);
-  float* tiles = reinterpret_cast<float*>(base);
-  unsigned char* work = base + 2 * TILE;
-  const uint32_t bar0 = (uint32_t)__cvta_generic_to_shared(work + sweep_col_work_bytes<NX>());
-  const uint32_t tile0 = (uint32_t)__cvta_generic_to_shared(tiles);
+  const float* tile = reinterpret_cast<const float*>(base);
+  unsigned char* work = base + TILE;
+  const uint32_t bar = (uint32_t)__cvta_generic_to_shared(work + sweep_col_work_bytes<NX>());
+  const uint32_t tile0 = (uint32_t)__cvta_generic_to_shared(base);
   if (threadIdx.x == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar0) : "memory");
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar0 + 8) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
   __syncthreads();
   // one thread: expect the stage's bytes, then load item idx's box into it
-  auto issue = [&](int idx, int stage) {
+  auto issue = [&](int idx) {
     const int2 it = items[idx];
     const SweepRunDev r = runs[it.x];
-    const uint32_t bar = bar0 + 8 * stage;
     const int cx0 = it.y * W, row0 = (int)(r.g_off / r.nv);
     asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"(TILE) : "memory");
     asm volatile(
         "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];\n" ::"r"(
-            tile0 + stage * TILE),
+            tile0),
         "l"(reinterpret_cast<uint64_t>(&maps.m[r.cls])), "r"(cx0), "r"(row0), "r"(bar)
         : "memory");
   };
   const int stride = gridDim.x;
-  if (threadIdx.x == 0) {
-    if ((int)blockIdx.x < n_items) issue(blockIdx.x, 0);
-    if ((int)blockIdx.x + stride < n_items) issue(blockIdx.x + stride, 1);
-  }
-  int iter = 0;
-  for (int idx = blockIdx.x; idx < n_items; idx += stride, ++iter) {
-    const int stage = iter & 1;
-    const uint32_t parity = (uint32_t)((iter >> 1) & 1);
-    const bool ok = mbar_wait_bounded(bar0 + 8 * stage, parity, TMA_WAIT_NS);
+  if (threadIdx.x == 0 && (int)blockIdx.x < n_items) issue(blockIdx.x);
+  uint32_t parity = 0;
+  for (int idx = blockIdx.x; idx < n_items; idx += stride, parity ^= 1u) {
+    const bool ok = mbar_wait_bounded(bar, parity, TMA_WAIT_NS);
     if (__syncthreads_or(!ok)) {
-      // the stage never filled: record it, let the copies in flight land, stop
+      // the stage never filled: record it, let the copy in flight land, stop
       if (threadIdx.x == 0) {
         atomicOr(err, 1);
-        int q = iter;
-        for (int j = idx; j < n_items && q < iter + 2; j += stride, ++q)
-          mbar_wait_bounded(bar0 + 8 * (q & 1), (uint32_t)((q >> 1) & 1), TMA_WAIT_NS);
+        mbar_wait_bounded(bar, parity, TMA_WAIT_NS);
       }
       __syncthreads();
       return;
     }
     const int2 it = items[idx];
     const SweepRunDev r = runs[it.x];
-    const float* tb = tiles + (size_t)stage * (TILE / sizeof(float));
     sweep_col_item<NX>(r, it.y, g, scp, tw, dpart, work, [&](auto& io, int x0, int xs, int col) {
 #pragma unroll
       for (int i = 0; i < (int)(sizeof(io) / sizeof(io[0])); ++i) {
-        const float2 q = *reinterpret_cast<const float2*>(tb + (size_t)(x0 + i * xs) * W + col);
+        const float2 q = *reinterpret_cast<const float2*>(tile + (size_t)(x0 + i * xs) * W + col);
         io[i].x = q.x;
         io[i].y = q.y;
       }
-      // every thread has its elements: the stage is free for item idx + 2 strides
+      // every thread has its elements: the stage is free for the next item
       __syncthreads();
-      if (threadIdx.x == 0 && idx + 2 * stride < n_items) issue(idx + 2 * stride, stage);
+      if (threadIdx.x == 0 && idx + stride < n_items) issue(idx + stride);
     });
   }
 }

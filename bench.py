@@ -132,11 +132,10 @@ class ClockSampler:
 
 
 # DRAM bytes of the sweep row pass per cell (dram__bytes_read.sum +
-# dram__bytes_write.sum), measured by ncu on the nv = 1024 launch of the
-# 800-run sweep (2592 CTAs x 4 row pairs x 2048 cells = 21.23 M cells):
-# 85.22 MB read, 27.92 MB written.  The full 4096-run pass is scaled from
-# it per cell.
-ROW_PASS_DRAM_BYTES_PER_CELL = (85217792 + 27923712) / 21233664
+# dram__bytes_write.sum), measured by ncu on the three full row-pass launches
+# of the 4096-run sweep (one per nv class; 179,806,208 cells in all):
+# 256: 106.42 + 53.45 MB, 512: 210.23 + 159.97 MB, 1024: 405.17 + 348.15 MB.
+ROW_PASS_DRAM_BYTES_PER_CELL = (106419456 + 53448192 + 210234880 + 159967232 + 405168640 + 348153344) / 179806208
 
 
 def peaks():
@@ -876,9 +875,9 @@ def main_sweep(args, w, rank, world):
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": ROW_PASS_DRAM_BYTES_PER_CELL * cells if dom_name == "sweep_row_pass" else None,
-                     "traffic_source": "ncu dram bytes of the nv=1024 row launch of the 800-run sweep, scaled per cell; "
-                                       "below the algorithmic 8 B/cell because written rows stay in L2 past the "
-                                       "launch",
+                     "traffic_source": "ncu dram bytes of the three full row-pass launches of the 4096-run sweep, "
+                                       "per cell; below the algorithmic 8 B/cell because some written rows stay in L2 "
+                                       "past the launch",
                      "kernel": dom_name, "peak_source": peak_kind, "kernel_ms": avg_ms,
                      "bytes_per_launch": dom["bytes_per_launch"]},
         "kernels": {k: {"launches": d["launches"], "avg_ms": d["total_ms"] / d["launches"]} for k, d in prof.items()},

@@ -839,9 +839,12 @@ def main_sweep(args, w, rank, world):
     avg_ms = dom["total_ms"] / dom["launches"]
     peak, peak_kind = peaks()
     achieved = dom["bytes_per_launch"] / (avg_ms / 1e3) / 1e9
-    launches_per_step = 0.0
-    for k, d in prof.items():
-        launches_per_step += d["launches"] / args.prof_steps
+    # kernel launches in the timed graph of K steps: per step one x-drift
+    # launch per nx class, the field solve, one row-pass launch per nv class
+    # and the store; per call one kick-only launch per nv class
+    n_x = len({r["nx"] for r in sw.runs})
+    n_v = len({r["nv"] for r in sw.runs})
+    timed_launches = args.steps * (n_x + 1 + n_v + 1) + n_v
     if rank != 0:
         return
     fp64 = None
@@ -881,7 +884,7 @@ def main_sweep(args, w, rank, world):
                      "kernel": dom_name, "peak_source": peak_kind, "kernel_ms": avg_ms,
                      "bytes_per_launch": dom["bytes_per_launch"]},
         "kernels": {k: {"launches": d["launches"], "avg_ms": d["total_ms"] / d["launches"]} for k, d in prof.items()},
-        "gpu_launches": int(round(launches_per_step * args.steps)),
+        "gpu_launches": timed_launches,
         "clocks": clk,
         "cpu_baseline": cpu,
         "state_bytes": cells * 4,

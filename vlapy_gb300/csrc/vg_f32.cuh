@@ -213,7 +213,8 @@ __device__ __forceinline__ void group_df_sum(df32 (&v)[NQ], df32* red, int G, in
 // ---- tridiagonal solve: partition (interior Thomas) + reduced system -----
 // Solves rows j = 0..N-1: l(j) x[j-1] + b x[j] + u(j) x[j+1] = x_in[j]
 // (l(0) and u(N-1) ignored).  x is one component of a padded complex-float
-// sequence in shared memory (element j at float offset 2*sp<float>(j)); thread
+// sequence in shared memory (element j at float offset 2*sp<float, PS>(j),
+// PS = row_pad_shift(M), the layout of the row kernels); thread
 // t of the G threads of a group owns the contiguous chunk [t*M, t*M+M),
 // M >= 2.  Each chunk is reduced by an interior Thomas sweep to two equations
 // in its end values x_s, x_e (the 2G-row boundary system).  One cyclic-
@@ -235,7 +236,7 @@ __device__ __forceinline__ void partition_solve(float* x, int t, float b, LFn lf
   // hold the x_s influence al and the pivots cp).
   float al[M > 2 ? M - 2 : 1], cp[M > 2 ? M - 2 : 1];
   float be_last = 0.f, be0 = 0.f, y_last = 0.f, y0 = 0.f;
-  float r_s = x[2 * sp<float>(s)], r_e = x[2 * sp<float>(e)];
+  float r_s = x[2 * sp<float, row_pad_shift(M)>(s)], r_e = x[2 * sp<float, row_pad_shift(M)>(e)];
   float RA0, RB0, RC0, RD0, RA1, RB1, RC1, RD1;
   const float l_s = (s == 0) ? 0.f : lf(s);
   const float u_s = uf(s);
@@ -250,9 +251,9 @@ __device__ __forceinline__ void partition_solve(float* x, int t, float b, LFn lf
       const float den = (i == 0) ? b : b - lj * cp[i - 1];
       const float inv = __fdividef(1.f, den);
       cp[i] = uj * inv;
-      const float rj = x[2 * sp<float>(j)];
+      const float rj = x[2 * sp<float, row_pad_shift(M)>(j)];
       y_last = (i == 0) ? rj * inv : (rj - lj * y_last) * inv;
-      x[2 * sp<float>(j)] = y_last;
+      x[2 * sp<float, row_pad_shift(M)>(j)] = y_last;
       al[i] = (i == 0) ? -lj * inv : (-lj * al[i - 1]) * inv;
       if (i == M - 3) be_last = -uj * inv;
     }
@@ -260,7 +261,7 @@ __device__ __forceinline__ void partition_solve(float* x, int t, float b, LFn lf
     y0 = y_last;
 #pragma unroll
     for (int i = M - 4; i >= 0; --i) {
-      float* xj = x + 2 * sp<float>(s + 1 + i);
+      float* xj = x + 2 * sp<float, row_pad_shift(M)>(s + 1 + i);
       y0 = *xj - cp[i] * y0;
       *xj = y0;
       al[i] -= cp[i] * al[i + 1];
@@ -372,14 +373,14 @@ __device__ __forceinline__ void partition_solve(float* x, int t, float b, LFn lf
     xe_lo = fetch(v, -1).x;
   }
   const float xs = __fdividef(RD0 - (t > 0 ? RA0 * xe_lo : 0.f) - RC0 * xe, RB0);
-  x[2 * sp<float>(s)] = xs;
-  x[2 * sp<float>(e)] = xe;
+  x[2 * sp<float, row_pad_shift(M)>(s)] = xs;
+  x[2 * sp<float, row_pad_shift(M)>(e)] = xe;
   if (M > 2) {
     float bi = be_last;
 #pragma unroll
     for (int i = M - 3; i >= 0; --i) {
       if (i < M - 3) bi = -cp[i] * bi;
-      float* xj = x + 2 * sp<float>(s + 1 + i);
+      float* xj = x + 2 * sp<float, row_pad_shift(M)>(s + 1 + i);
       *xj = *xj + al[i] * xs + bi * xe;
     }
   }

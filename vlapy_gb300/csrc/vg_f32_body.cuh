@@ -126,7 +126,7 @@ __device__ __forceinline__ double row_moment(const double* __restrict__ slots, i
 
 // rotation of one packed row pair with the delta-f background term; the 1/N of
 // the inverse transform is folded in.  ha/hb: half-angle per kv index.
-template <int N>
+template <int N, int PS = pad_shift<float>()>
 __device__ __forceinline__ void kick_rotate(cx<float>* s, int t, int G, Ang ha, Ang hb,
                                             const cx<float>* __restrict__ F0) {
   const float sc = 1.f / N;
@@ -143,19 +143,19 @@ __device__ __forceinline__ void kick_rotate(cx<float>* s, int t, int G, Ang ha, 
     const float pb_m1r = -2.f * sb * sb, pb_i = 2.f * sb * cb, pb_r = 1.f + pb_m1r;
     const cx<float> f0 = F0[k];
     if (k == 0 || 2 * k == N) {
-      const cx<float> z = s[sp<float>(k)];
+      const cx<float> z = s[sp<float, PS>(k)];
       // real bins: only Re(P) survives
-      s[sp<float>(k)] = {(pa_r * z.x + pa_m1r * f0.x) * sc, (pb_r * z.y + pb_m1r * f0.x) * sc};
+      s[sp<float, PS>(k)] = {(pa_r * z.x + pa_m1r * f0.x) * sc, (pb_r * z.y + pb_m1r * f0.x) * sc};
     } else {
-      const cx<float> zk = s[sp<float>(k)], zm = s[sp<float>(N - k)];
+      const cx<float> zk = s[sp<float, PS>(k)], zm = s[sp<float, PS>(N - k)];
       const cx<float> fa = {(zk.x + zm.x) * 0.5f, (zk.y - zm.y) * 0.5f};
       const cx<float> fb = {(zk.y + zm.y) * 0.5f, (zm.x - zk.x) * 0.5f};
       const cx<float> ga = {(pa_r * fa.x - pa_i * fa.y + pa_m1r * f0.x - pa_i * f0.y) * sc,
                             (pa_r * fa.y + pa_i * fa.x + pa_m1r * f0.y + pa_i * f0.x) * sc};
       const cx<float> gb = {(pb_r * fb.x - pb_i * fb.y + pb_m1r * f0.x - pb_i * f0.y) * sc,
                             (pb_r * fb.y + pb_i * fb.x + pb_m1r * f0.y + pb_i * f0.x) * sc};
-      s[sp<float>(k)] = {ga.x - gb.y, ga.y + gb.x};
-      s[sp<float>(N - k)] = {ga.x + gb.y, gb.x - ga.y};
+      s[sp<float, PS>(k)] = {ga.x - gb.y, ga.y + gb.x};
+      s[sp<float, PS>(N - k)] = {ga.x + gb.y, gb.x - ga.y};
     }
     const float na = sa * cga + ca * sga, nca = ca * cga - sa * sga;
     const float nb = sb * cgb + cb * sgb, ncb = cb * cgb - sb * sgb;
@@ -174,15 +174,16 @@ __device__ __forceinline__ void kick_io(cx<float>* s, int t, float hk, float ea,
                                         const cx<float>* __restrict__ F0, const cx<float>* __restrict__ tw,
                                         const Sync& sync, cx<float> (&io)[R]) {
   constexpr int G = N / R;
-  block_fft_io<float, N, false, R, IO & 1>(s, t, tw, sync, io);
+  constexpr int PS = row_pad_shift(R);
+  block_fft_io<float, N, false, R, IO & 1, Sync, PS>(s, t, tw, sync, io);
   // theta(k) = -kv_k dt e = k * (-dkv dt e); hk = -dkv dt / 2 gives the half
   // angle for P - 1.  The kick angle stays O(10) rad, so an FP32 product is
   // accurate to ~1e-6 rad here
   const Ang ha = {hk * ea, 0.f};
   const Ang hb = {hk * eb, 0.f};
-  kick_rotate<N>(s, t, G, ha, hb, F0);
+  kick_rotate<N, PS>(s, t, G, ha, hb, F0);
   sync();
-  block_fft_io<float, N, true, R, IO & 2>(s, t, tw, sync, io);
+  block_fft_io<float, N, true, R, IO & 2, Sync, PS>(s, t, tw, sync, io);
 }
 
 // Per-row collision scalars from the row's raw moment sums (sum w g v^p,
@@ -227,7 +228,7 @@ __device__ __forceinline__ void collide_pair(cx<float>* s, int t, const RowConst
     for (int i = 0; i < R; ++i) {
       const int j = t + i * G;
       const float w = (j == 0 || j == N - 1) ? 0.5f : 1.f;
-      const cx<float> z = s[sp<float>(j)];
+      const cx<float> z = s[sp<float, row_pad_shift(R)>(j)];
       const float vj = rc.v[j];
       const float ga = w * z.x, gb = w * z.y;
       m[0] += ga;
@@ -263,10 +264,10 @@ __device__ __forceinline__ void collide_pair(cx<float>* s, int t, const RowConst
   for (int i = 0; i < R; ++i) {
     const int j = t + i * G;
     const float S = rc.S[j], Mv = rc.Mv[j], D = rc.D[j];
-    cx<float> z = s[sp<float>(j)];
+    cx<float> z = s[sp<float, row_pad_shift(R)>(j)];
     z.x -= -sa[3] * S + cm * Mv - sa[4] * D;
     z.y -= -sb[3] * S + cm * Mv - sb[4] * D;
-    s[sp<float>(j)] = z;
+    s[sp<float, row_pad_shift(R)>(j)] = z;
   }
   sync();
   // off-diagonals at v[j -+ 1] of the uniform grid v[j] = v[0] + j dv,
@@ -299,7 +300,7 @@ __device__ __forceinline__ void row_pair(const RowArgs& a, int pair, unsigned ch
                                          int P, int grp, int t, const Sync& sync = Sync()) {
   constexpr int G = N / R;
   cx<float>* s = reinterpret_cast<cx<float>*>(grp_base);
-  constexpr size_t seq_bytes = row32_seq_bytes(N);
+  constexpr size_t seq_bytes = row32_seq_bytes(N, R);
   static_assert(seq_bytes % 16 == 0 && row32_group_bytes(N, R) % 16 == 0 &&
                     seq_bytes + 8 * G * sizeof(float) + round16((G / 32 + 1) * 9 * sizeof(df32)) ==
                         row32_group_bytes(N, R),
@@ -349,7 +350,7 @@ __device__ __forceinline__ void row_pair(const RowArgs& a, int pair, unsigned ch
       }
     } else {
 #pragma unroll
-      for (int i = 0; i < R; ++i) io[i] = s[sp<float>(t + i * G)];
+      for (int i = 0; i < R; ++i) io[i] = s[sp<float, row_pad_shift(R)>(t + i * G)];
     }
     if (hk != 0.f) {
       kick_io<N, R, 3>(s, t, hk, ea, eb, a.F0, a.tw, sync, io);
@@ -369,7 +370,7 @@ __device__ __forceinline__ void row_pair(const RowArgs& a, int pair, unsigned ch
     // every thread's last kick pass has read it)
     sync();
 #pragma unroll
-    for (int i = 0; i < R; ++i) s[sp<float>(t + i * G)] = io[i];
+    for (int i = 0; i < R; ++i) s[sp<float, row_pad_shift(R)>(t + i * G)] = io[i];
     sync();
     if (a.fp) {
       collide_pair<N, R>(s, t, *a.rc, a.nudt2, a.nudt_f, a.dougherty, red, pcr, sync);
@@ -385,7 +386,7 @@ __device__ __forceinline__ void row_pair(const RowArgs& a, int pair, unsigned ch
         const int j = t + i * G;  // consecutive threads, consecutive j: coalesced loads
         const float w = (j == 0 || j == N - 1) ? 0.5f : 1.f;
         const float vj = a.rc->v[j], f0j = a.rc->f0[j];
-        const cx<float> z = s[sp<float>(j)];
+        const cx<float> z = s[sp<float, row_pad_shift(R)>(j)];
         float pa = w * z.x, pb = w * z.y;
   #pragma unroll
         for (int p = 0; p < NPOW; ++p) {
@@ -459,7 +460,7 @@ __device__ __forceinline__ void row_pair(const RowArgs& a, int pair, unsigned ch
               if (vb) sincospif(-2.f * (float)((mq * rb) % a.nx) / (float)a.nx, &swb, &cwb);
               for (int i = 0; i < R; ++i) {
                 const int n = t + i * G;
-                const cx<float> z = s[sp<float>(n)];
+                const cx<float> z = s[sp<float, row_pad_shift(R)>(n)];
                 cx<float>& acc = macc[(size_t)mq * N + n];
                 acc.x += z.x * cwa + z.y * cwb;
                 acc.y += z.x * swa + z.y * swb;

@@ -83,9 +83,11 @@ __host__ __device__ constexpr int row32_block(int n, int r) { return (n / r) >= 
 // the layout the row kernels index), boundary-solve scratch of 8G floats
 // (2 x G float4), double-float reduction slots
 __host__ __device__ constexpr size_t round16(size_t b) { return (b + 15) & ~(size_t)15; }
-__host__ __device__ constexpr size_t row32_seq_bytes(int n) { return round16((size_t)sp_len<float>(n) * 8 + 16); }
+__host__ __device__ constexpr size_t row32_seq_bytes(int n, int r) {
+  return round16((size_t)(n + (n >> row_pad_shift(r))) * 8 + 16);
+}
 __host__ __device__ constexpr size_t row32_group_bytes(int n, int r) {
-  return row32_seq_bytes(n) + (size_t)8 * (n / r) * 4 + round16((size_t)((n / r) / 32 + 1) * 9 * 8);
+  return row32_seq_bytes(n, r) + (size_t)8 * (n / r) * 4 + round16((size_t)((n / r) / 32 + 1) * 9 * 8);
 }
 
 constexpr int F32_MAX_MODES = 4;

@@ -83,10 +83,15 @@ __host__ __device__ constexpr int col_seqs(int nx) {
 #endif
 template <typename T>
 __host__ __device__ constexpr int pad_shift() { return sizeof(T) == 8 ? 3 : VG_PAD_SHIFT_F32; }
-template <typename T>
-__device__ __forceinline__ int sp(int i) { return i + (i >> pad_shift<T>()); }
-template <typename T>
-__host__ __device__ constexpr int sp_len(int n) { return n + (n >> pad_shift<T>()); }
+template <typename T, int PS = pad_shift<T>()>
+__device__ __forceinline__ int sp(int i) { return i + (i >> PS); }
+template <typename T, int PS = pad_shift<T>()>
+__host__ __device__ constexpr int sp_len(int n) { return n + (n >> PS); }
+// The FP32 row kernels on radix-32 passes pad one element per 32 instead:
+// their stride-32 accesses (the first pass's stores, the solve's 32-element
+// chunks) then step 33 elements, an odd count, and fall in distinct bank pairs,
+// where the one-per-16 layout makes them step 34 (a 4-way bank conflict).
+__host__ __device__ constexpr int row_pad_shift(int r) { return r == 32 ? 5 : pad_shift<float>(); }
 // Padded offset of element base + m * S, m = 0..r-1, as sp(base) plus a
 // compile-time constant per m wherever the pad pattern allows (CASE):
 //  1: S a multiple of the pad period P: sp(base) + m (S + S/P);
@@ -94,12 +99,12 @@ __host__ __device__ constexpr int sp_len(int n) { return n + (n >> pad_shift<T>(
 //     no pad boundary falls between base and base + m S other than those
 //     of m S itself, so sp(base) + m S + (m S) / P;
 //  0: otherwise the element's own sp().
-template <typename T, int S, int CASE>
+template <typename T, int S, int CASE, int PS = pad_shift<T>()>
 __device__ __forceinline__ int sp_step(int spbase, int base, int m) {
-  constexpr int P = 1 << pad_shift<T>();
+  constexpr int P = 1 << PS;
   if constexpr (CASE == 1) return spbase + m * (S + S / P);
-  else if constexpr (CASE == 2) return spbase + m * S + ((m * S) >> pad_shift<T>());
-  else return sp<T>(base + m * S);
+  else if constexpr (CASE == 2) return spbase + m * S + ((m * S) >> PS);
+  else return sp<T, PS>(base + m * S);
 }
 
 // multiply by exp(-+2 pi i k / R), forward sign '-' unless INV
@@ -170,7 +175,7 @@ __device__ __forceinline__ cx<T> twiddle(const cx<T>* __restrict__ tw, int q, bo
 // exactly what that pass reads) instead of shared memory; bit 1: the last
 // pass leaves its outputs in io (again elements t + i N/R) instead of
 // writing them back.  Either saves one round trip through shared memory.
-template <typename T, int N, int R, bool INV, int NS, int IO = 0>
+template <typename T, int N, int R, bool INV, int NS, int IO = 0, int PS = pad_shift<T>()>
 struct StockhamPass {
   template <typename Sync>
   static __device__ __forceinline__ void run(cx<T>* s, int t, const cx<T>* __restrict__ tw, const Sync& sync,
@@ -182,7 +187,7 @@ struct StockhamPass {
     constexpr bool from_regs = (IO & 1) && NS == 1;
     constexpr bool to_regs = (IO & 2) && NS * r == N;
     static_assert(!from_regs || (BPT == 1 && r == R), "the first pass reads one radix-R butterfly per thread");
-    constexpr int PP = 1 << pad_shift<T>();
+    constexpr int PP = 1 << PS;
     // loads: element j + m NB; NB a multiple of the pad period makes the
     // offsets constant past sp(j)
     constexpr int LCASE = (NB % PP == 0) ? 1 : 0;
@@ -194,11 +199,11 @@ struct StockhamPass {
     for (int b = 0; b < BPT; ++b) {
       const int j = t + b * G;
       const int k = j & (NS - 1);
-      const int spj = sp<T>(j);
+      const int spj = sp<T, PS>(j);
 #pragma unroll
       for (int m = 0; m < r; ++m) {
         if constexpr (from_regs) a[b][m] = io[m];
-        else a[b][m] = s[sp_step<T, NB, LCASE>(spj, j, m)];
+        else a[b][m] = s[sp_step<T, NB, LCASE, PS>(spj, j, m)];
       }
       if (NS > 1) {
         // twiddles w^m: the power-of-two m from the table, the others as
@@ -227,17 +232,17 @@ struct StockhamPass {
         const int j = t + b * G;
         const int k = j & (NS - 1);
         const int base = (j - k) * r + k;
-        const int spb = sp<T>(base);
+        const int spb = sp<T, PS>(base);
 #pragma unroll
-        for (int m = 0; m < r; ++m) s[sp_step<T, NS, SCASE>(spb, base, m)] = a[b][m];
+        for (int m = 0; m < r; ++m) s[sp_step<T, NS, SCASE, PS>(spb, base, m)] = a[b][m];
       }
       sync();
-      StockhamPass<T, N, R, INV, NS * r, IO>::run(s, t, tw, sync, io);
+      StockhamPass<T, N, R, INV, NS * r, IO, PS>::run(s, t, tw, sync, io);
     }
   }
 };
-template <typename T, int N, int R, bool INV, int IO>
-struct StockhamPass<T, N, R, INV, N, IO> {
+template <typename T, int N, int R, bool INV, int IO, int PS>
+struct StockhamPass<T, N, R, INV, N, IO, PS> {
   template <typename Sync>
   static __device__ __forceinline__ void run(cx<T>*, int, const cx<T>* __restrict__, const Sync&, cx<T> (&)[R]) {}
 };
@@ -254,11 +259,11 @@ __device__ __forceinline__ void block_fft(cx<T>* s, int t, const cx<T>* __restri
 // The same with register input (IO = 1: io holds elements t + i N/R, s need
 // not hold the sequence) or register output (IO = 2: the result's elements
 // t + i N/R end in io and s is left as scratch).
-template <typename T, int N, bool INV, int R, int IO, typename Sync>
+template <typename T, int N, bool INV, int R, int IO, typename Sync, int PS = pad_shift<T>()>
 __device__ __forceinline__ void block_fft_io(cx<T>* s, int t, const cx<T>* __restrict__ tw, const Sync& sync,
                                              cx<T> (&io)[R]) {
   static_assert(R <= N, "radix larger than the sequence");
-  StockhamPass<T, N, R, INV, 1, IO>::run(s, t, tw, sync, io);
+  StockhamPass<T, N, R, INV, 1, IO, PS>::run(s, t, tw, sync, io);
 }
 
 // Two real sequences a, b packed as z = a + i b; s holds Z = FFT(z).  Replace

@@ -331,7 +331,69 @@ def single_run_summary(args, name, precision, steps=10, warmup=3):
                    "d2h_bytes_per_step": d2h},
            "kernels_ms_per_step": {k: d["total_ms"] for k, d in prof.items()}}
     plan.close()
+    if w["kind"] == "driven":
+        out["dropin"] = dropin_summary(w, precision)
     return out
+
+
+def dropin_summary(w, precision, batch=100, calls=100):
+    """The single-run workload through the reference-facing Python entry
+    points (vlapy/outer_loop.py:248-281 and vlapy/core/step.py:286-328): the
+    inner loop over a batch of `batch` steps, with the host time and driver
+    arrays copied in and the batch's sim_config brought back to host memory
+    as StorageManager.batch_update receives it, and the per-step closure
+    timestep(temp_storage, i) called `calls` times.  Wall-clock seconds with
+    a device synchronise at both ends, after one untimed call of each."""
+    import torch
+    from vlapy_gb300 import field_driver, outer_loop, storage
+    from vlapy_gb300.core import step
+    st = initial_state(w)
+    nx = w["nx"]
+    pl = pulses_of(w)
+    drv = field_driver.PulseDriver(st["x"], {"p": dict(pl[0], envelope="sin2")}) if pl else None
+    rules = {"time": "first-last", "space": ["k0", "k1"]}
+    stuff = {"nx": nx, "nv": w["nv"], "x": st["x"], "v": st["v"], "kx": st["kx"], "kv": st["kv"],
+             "one_over_kx": st["inv"], "dv": st["dv"], "dt": w["dt"], "nu": w["nu"], "driver_function": drv,
+             "rules_to_store_f": rules, "f": st["f"], "e": np.zeros(nx)}
+    params = {"nu": w["nu"], "fokker-planck": {"type": w["op"], "solver": "batched_tridiagonal"},
+              "vlasov-poisson": {"time": "leapfrog", "vdfdx": "exponential", "edfdv": "exponential",
+                                 "poisson": "spectral"},
+              "backend": {"core": "gb300", "precision": precision}}
+    t_host = w["dt"] * np.arange(2 * batch)
+    d_host = field_driver.make_driver_array(drv, st["x"], t_host) if drv else np.zeros((2 * batch, nx))
+    sc, inner = outer_loop.get_sim_config_and_inner_loop_step(params, stuff, batch, rules)
+    sc = inner(t_host[:batch], d_host[:batch], sc)  # captures the batch's graph
+    outer_loop.post_inner_loop_update(sc)
+    storage.get_batched_data_from_sim_config(sc)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sc = inner(t_host[batch:], d_host[batch:], sc)
+    outer_loop.post_inner_loop_update(sc)
+    host = storage.get_batched_data_from_sim_config(sc)
+    torch.cuda.synchronize()
+    loop_s = time.perf_counter() - t0
+    h2d = t_host[batch:].nbytes + d_host[batch:].nbytes
+    d2h = sum(a.nbytes for a in host[0].values()) + host[1].nbytes + host[2].nbytes + \
+        sum(a.nbytes for a in host[3].values()) + host[4].nbytes
+    ts = step.get_timestep(params, stuff)
+    sc2 = outer_loop.get_arrays_for_inner_loop(stuff, calls + 1, rules)
+    sc2["time_batch"] = torch.as_tensor(w["dt"] * np.arange(calls + 1), device="cuda")
+    sc2["driver_array_batch"] = torch.as_tensor(
+        field_driver.make_driver_array(drv, st["x"], w["dt"] * np.arange(calls + 1)) if drv
+        else np.zeros((calls + 1, nx)), device="cuda")
+    sc2, _ = ts(sc2, 0)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in range(1, calls + 1):
+        sc2, _ = ts(sc2, i)
+    torch.cuda.synchronize()
+    step_s = time.perf_counter() - t0
+    return {"inner_loop_ms_per_step": loop_s / batch * 1e3, "inner_loop_batch": batch,
+            "inner_loop_h2d_bytes_per_batch": int(h2d), "inner_loop_d2h_bytes_per_batch": int(d2h),
+            "timestep_ms_per_call": step_s / calls * 1e3,
+            "how": "wall clock: outer_loop inner loop over %d steps (host time/driver arrays in, the sim_config "
+                   "to host as batch_update receives it) and %d calls of core.step.get_timestep's closure"
+                   % (batch, calls)}
 
 
 def fp64_plain_sweep(w, steps=2):

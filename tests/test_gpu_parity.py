@@ -332,3 +332,44 @@ def test_unsupported_sizes_raise():
     p2, _ = make_plan(2, 4100)
     with pytest.raises(NotImplementedError):
         p2.edfdv(cuda(np.ones((2, 4100))), cuda(np.zeros(2)), 0.1)
+
+
+def test_dropin_fp32_resident_deviation():
+    """The reference-facing per-step closure and inner loop in the FP32
+    delta-f mode, on the driven-wave fixture: the FP32 deviation g = f - f0
+    stays resident between calls (f is written from it once a step and never
+    read back), the per-step closure and the graph-captured inner loop agree,
+    both follow the reference's FP64 steps to the FP32 mode's error, and a
+    caller that writes f restarts from the f it wrote."""
+    from vlapy_gb300 import outer_loop
+    d, m, stuff, params, rules, step, arrays = _golden_run("driven_sin2_dg_64x1024")
+    params = dict(params, backend={"core": "gb300", "precision": "fp32-deltaf"})
+    nsteps = int(m["nsteps"])
+    ts = step.get_timestep(params, stuff)
+    sc = arrays(stuff, nsteps, rules)
+    sc["time_batch"] = cuda(d["time"])
+    sc["driver_array_batch"] = cuda(d["driver_array"])
+    resident, f_after_1 = None, None
+    for i in range(nsteps):
+        sc, _ = ts(sc, i)
+        if i == 0:
+            resident = sc["_g"][0]
+            f_after_1 = sc["f"].clone()
+        assert sc["_g"][0] is resident
+    f_step = sc["f"].cpu().numpy()
+    sc2, inner = outer_loop.get_sim_config_and_inner_loop_step(params, stuff, nsteps, rules)
+    sc2 = inner(d["time"], d["driver_array"], sc2)
+    torch.cuda.synchronize()
+    f_loop = sc2["f"].cpu().numpy()
+    f_ref = d["f_%d" % nsteps]
+    pert = np.linalg.norm(f_ref - d["f0"].mean(axis=0)[None, :])
+    assert np.linalg.norm(f_step - f_loop) <= 1e-5 * pert
+    assert np.linalg.norm(f_step - f_ref) <= 1e-4 * pert
+    np.testing.assert_allclose(sc["e"].cpu().numpy(), sc2["e"].cpu().numpy(), rtol=0,
+                               atol=1e-5 * np.abs(d["e_%d" % nsteps]).max())
+    # the caller writes f (and e): the next step starts from them
+    sc["f"].copy_(cuda(d["f0"]))
+    sc["e"].zero_()
+    sc, _ = ts(sc, 0)
+    assert sc["_g"][0] is not resident
+    torch.testing.assert_close(sc["f"], f_after_1, rtol=0, atol=0)

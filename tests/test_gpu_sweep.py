@@ -307,3 +307,56 @@ def test_sweep_full_size_properties():
         e_hist = sw.e_of(eh, i).cpu().numpy()
         assert np.linalg.norm(e_hist - e_ref) / np.linalg.norm(e_ref) <= 1e-4, (i, r)
     assert len(seen) == 9
+
+
+def test_sweep_full_horizon_against_fp64():
+    """The benchmarked horizon (2000 steps) of the sweep workload, 16 runs of
+    each of the nine shape classes drawn from the workload's own run list
+    (collisional and collisionless), against the batched FP64 step (the
+    reference's arithmetic, held to the oracle at 1e-12 in test_gpu_batch):
+    each run's Landau damping rate (peak-envelope fit of |E_1| on t in [5, 60])
+    within 1 %, its field-energy history within 1 %, and its final f within
+    a stated bound of the perturbation."""
+    from vlapy_gb300.batch import Batch64
+    from vlapy_gb300.diagnostics import damping_fit, mode_amplitude
+    from vlapy_gb300.sweep import Sweep, sweep_config
+    pool = sweep_config(4096, 20261203)
+    runs, count = [], {}
+    for r in pool:
+        key = (r["nx"], r["nv"])
+        if count.get(key, 0) < 16:
+            count[key] = count.get(key, 0) + 1
+            runs.append(r)
+    assert len(runs) == 144 and any(r["nu"] == 0.0 for r in runs) and any(r["nu"] > 0.0 for r in runs)
+    nsteps = 2000
+    sw = Sweep(runs)
+    sw.reset()
+    eh, sh = sw.history(nsteps)
+    sw.run_steps(nsteps, eh, sh)
+    judge = Batch64(runs)
+    f64, e64 = judge.initial_state()
+    eh64, sh64 = judge.history(nsteps)
+    for c0 in range(0, nsteps, 250):
+        judge.run_steps(f64, e64, 250, eh64, sh64, row0=c0)
+    torch.cuda.synchronize()
+    t = 0.1 * np.arange(1, nsteps + 1)
+    rate_err, e2_err, f_err = [], [], []
+    for i, r in enumerate(runs):
+        rf, _ = damping_fit(t, mode_amplitude(judge.e_of(eh64, i).cpu().numpy()), t_min=5.0, t_max=60.0)
+        rg, _ = damping_fit(t, mode_amplitude(sw.e_of(eh, i).cpu().numpy()), t_min=5.0, t_max=60.0)
+        assert np.isfinite(rf) and rf < 0.0, (i, r, rf)
+        rate_err.append(abs(rg - rf) / abs(rf))
+        e2_ref = judge.series_of(sh64, i)[:, 3].cpu().numpy()
+        e2 = sh[:, i, 3].cpu().numpy()
+        e2_err.append(np.linalg.norm(e2 - e2_ref) / np.linalg.norm(e2_ref))
+        f_ref = judge.f_of(f64, i).cpu().numpy()
+        f0 = vo.maxwellian(1, r["nv"], 6.4)[0]
+        f_err.append(np.linalg.norm(sw.read_run(i)[0].cpu().numpy() - f_ref) / np.linalg.norm(f_ref - f0[None, :]))
+    rate_err, e2_err, f_err = map(np.asarray, (rate_err, e2_err, f_err))
+    print("horizon 2000 steps, 144 runs: damping rate rel err median %.2e max %.2e; field energy median %.2e "
+          "max %.2e; final f (of |f - f0|) median %.2e max %.2e"
+          % (np.median(rate_err), rate_err.max(), np.median(e2_err), e2_err.max(), np.median(f_err), f_err.max()))
+    assert rate_err.max() <= 0.01, (int(rate_err.argmax()), runs[int(rate_err.argmax())])
+    assert e2_err.max() <= 0.01, (int(e2_err.argmax()), runs[int(e2_err.argmax())])
+    assert f_err.max() <= 0.02, (int(f_err.argmax()), runs[int(f_err.argmax())])
+    judge.close()

@@ -71,12 +71,42 @@ def to_deviation(plan, f):
 
 
 def from_deviation(plan, g, out=None):
-    """f = g + f0 as float64 (into out if given)."""
+    """f = g + f0 as float64 (into out if given: one pass, no temporary)."""
     f0 = torch.as_tensor(plan._fbg, device="cuda")
-    f = g.to(torch.float64) + f0[None, :]
     if out is not None:
-        out.copy_(f)
-        return out
+        return torch.add(g, f0[None, :], out=out)
+    return g.to(torch.float64) + f0[None, :]
+
+
+_RESIDENT = "_g"
+
+
+def resident_deviation(plan, temp_storage):
+    """The FP32 deviation g = f - f0 of temp_storage["f"], kept with
+    temp_storage between calls.  It is reused while temp_storage["f"] is the
+    tensor that publish_deviation last wrote and nothing has written to it
+    since (its version counter is unchanged); otherwise it is formed again
+    from f, so a caller that replaces or edits f restarts from its f."""
+    f = temp_storage["f"]
+    held = temp_storage.get(_RESIDENT)
+    if held is not None and isinstance(f, torch.Tensor):
+        g, f_ref, version = held
+        if f_ref is f and f._version == version:
+            return g
+    g = to_deviation(plan, f)
+    if isinstance(f, torch.Tensor):
+        temp_storage[_RESIDENT] = (g, f, f._version)
+    return g
+
+
+def publish_deviation(plan, temp_storage, g):
+    """Write f = g + f0 into temp_storage["f"] (a float64 CUDA tensor, made
+    one if it is not) and mark g as its resident deviation."""
+    f = temp_storage["f"]
+    if not (isinstance(f, torch.Tensor) and f.is_cuda and f.dtype == torch.float64 and f.is_contiguous()):
+        f = temp_storage["f"] = torch.empty(g.shape, dtype=torch.float64, device=g.device)
+    from_deviation(plan, g, out=f)
+    temp_storage[_RESIDENT] = (g, f, f._version)
     return f
 
 

@@ -16,7 +16,7 @@ import torch
 from ..field_driver import PulseDriver
 from ..plan import history_struct
 from . import collisions, field, vlasov, vlasov_poisson
-from ._plans import as_device, from_deviation, plan_for, to_deviation
+from ._plans import as_device, plan_for, publish_deviation, resident_deviation
 
 
 def get_vlasov_poisson_step(all_params, stuff_for_time_loop):
@@ -101,11 +101,12 @@ def get_timestep(all_params, stuff_for_time_loop):
             f, e = temp_storage["f"], temp_storage["e"]
             hist = history_struct(temp_storage, plan.nx, n_modes)
             if plan.precision == "fp32-deltaf":
-                # the delta-f state lives in FP32; f is refreshed from it after the step
-                g = to_deviation(plan, f)
+                # the delta-f state stays resident in FP32 between calls; f is
+                # refreshed from it after the step
+                g = resident_deviation(plan, temp_storage)
                 plan.run_steps(g, e, hist, temp_storage["time_batch"], temp_storage["driver_array_batch"],
                                i, 1, use_graph=False)
-                from_deviation(plan, g, out=f)
+                publish_deviation(plan, temp_storage, g)
             else:
                 plan.run_steps(f, e, hist, temp_storage["time_batch"], temp_storage["driver_array_batch"],
                                i, 1, use_graph=False)

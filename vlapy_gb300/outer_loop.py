@@ -14,7 +14,7 @@ import torch
 
 from . import field_driver, initializers
 from .core import step
-from .core._plans import as_device, from_deviation, plan_for, to_deviation
+from .core._plans import as_device, plan_for, publish_deviation, resident_deviation
 from .field_driver import PulseDriver
 from .plan import history_struct, require_cuda
 
@@ -131,11 +131,9 @@ def get_inner_loop_stepper(all_params, stuff_for_time_loop, steps_in_loop):
             hist = history_struct(temp_storage, plan.nx, n_modes)
             state = temp_storage["f"]
             if plan.precision == "fp32-deltaf":
-                # FP32 deviation from the run's fixed background, kept across batches
-                g = temp_storage.get("_g")
-                if g is None:
-                    g = temp_storage["_g"] = to_deviation(plan, temp_storage["f"])
-                state = g
+                # FP32 deviation from the run's fixed background, kept across
+                # batches while the caller leaves f alone
+                state = resident_deviation(plan, temp_storage)
             cur = torch.cuda.current_stream()
             side.wait_stream(cur)
             with torch.cuda.stream(side):
@@ -144,7 +142,7 @@ def get_inner_loop_stepper(all_params, stuff_for_time_loop, steps_in_loop):
                                stream=side)
             cur.wait_stream(side)
             if plan.precision == "fp32-deltaf":
-                from_deviation(plan, state, out=temp_storage["f"])
+                publish_deviation(plan, temp_storage, state)
         else:
             for it in range(steps_in_loop):
                 temp_storage, _ = one_step(temp_storage, it)

@@ -125,6 +125,37 @@ def test_sweep_tma_x_drift_equals_plain_loads():
     assert float(torch.linalg.norm((ga - gb).double())) <= 1e-6 * float(torch.linalg.norm(gb.double()))
 
 
+def test_sweep_classes_side_by_side_equal_serial():
+    """The size classes of each phase launched side by side (branches from
+    the caller's stream, the default) give bit for bit what one stream gives
+    (VG_SWEEP_SERIAL=1), directly and through the captured graph: each class
+    works on its own runs."""
+    import os
+    from vlapy_gb300.sweep import Sweep, sweep_config
+    runs = mixed_runs() + sweep_config(300, seed=11)
+    a = Sweep(runs)
+    os.environ["VG_SWEEP_SERIAL"] = "1"
+    try:
+        b = Sweep(runs)
+    finally:
+        del os.environ["VG_SWEEP_SERIAL"]
+    for use_graph in (False, True):
+        for sw in (a, b):
+            sw.reset()
+        ea, sa = a.history(5)
+        eb, sb = b.history(5)
+        s = torch.cuda.Stream()
+        s.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(s):
+            a.run_steps(5, ea, sa, use_graph=use_graph, stream=s)
+            b.run_steps(5, eb, sb, use_graph=use_graph, stream=s)
+        torch.cuda.synchronize()
+        assert torch.isfinite(ea).all()
+        assert torch.equal(ea, eb)
+        torch.testing.assert_close(sa, sb, rtol=0, atol=0, equal_nan=True)
+        assert torch.equal(a.get_state()[0], b.get_state()[0])
+
+
 def test_sweep_config_distribution():
     from vlapy_gb300.sweep import sweep_config
     runs = sweep_config(4096)

@@ -689,6 +689,12 @@ struct vg_sweep {
   std::vector<SweepTmaps> tmaps;  // per x class, one map per nv class
   int* err = nullptr;             // bounded-wait events of the TMA x-drift
   int n_sm = 0;
+  // the size classes of a phase run side by side: side streams that branch
+  // from the caller's stream and join it again, and the events that do it
+  // ([0] the branch point, [q] the end of side stream q - 1)
+  bool concurrent = false;
+  std::vector<cudaStream_t> side;
+  std::vector<cudaEvent_t> ev;
 };
 
 namespace {
@@ -820,6 +826,8 @@ int sweep_class(vg_sweep* s, int cls, int nv) {
 void free_sweep(vg_sweep* s) {
   if (!s) return;
   for (auto& kv : s->graphs) cudaGraphExecDestroy(kv.second);
+  for (cudaStream_t q : s->side) cudaStreamDestroy(q);
+  for (cudaEvent_t e : s->ev) cudaEventDestroy(e);
   for (void* p : s->owned)
     if (p) cudaFree(p);
   delete s;
@@ -862,6 +870,56 @@ cudaError_t sweep_row_launch(vg_sweep* s, int c, const SweepRowArgs& a, cudaStre
   return cudaGetLastError();
 }
 
+// launch(c, stream) for each of the n size classes of one phase (classes in
+// ascending size).  With side streams the classes run side by side: the
+// largest on st, each other on a side stream that first waits for st's work
+// so far, and st waits for every side stream before the next phase (inside a
+// stream capture the classes become parallel branches of the graph).  The
+// largest class goes first, so its CTAs take the SMs and the smaller classes
+// fill what its last wave leaves idle.  The classes touch disjoint runs, so
+// the results do not depend on how their kernels overlap.
+template <typename Fn>
+cudaError_t over_classes(vg_sweep* s, int n, cudaStream_t st, Fn launch) {
+  if (!s->concurrent || n <= 1 || n > (int)s->ev.size()) {
+    for (int c = 0; c < n; ++c) {
+      const cudaError_t err = launch(c, st);
+      if (err != cudaSuccess) return err;
+    }
+    return cudaSuccess;
+  }
+  cudaError_t err = cudaEventRecord(s->ev[0], st);
+  for (int q = 0; q < n && err == cudaSuccess; ++q) {
+    cudaStream_t sq = q == 0 ? st : s->side[q - 1];
+    if (q > 0) err = cudaStreamWaitEvent(sq, s->ev[0], 0);
+    if (err == cudaSuccess) err = launch(n - 1 - q, sq);
+    if (err == cudaSuccess && q > 0) err = cudaEventRecord(s->ev[q], sq);
+  }
+  // join every side stream that branched, also after an error
+  for (int q = 1; q < n; ++q) {
+    const cudaError_t j = cudaStreamWaitEvent(st, s->ev[q], 0);
+    if (err == cudaSuccess) err = j;
+  }
+  return err;
+}
+
+int sweep_setup_streams(vg_sweep* s) {
+  const char* off = std::getenv("VG_SWEEP_SERIAL");
+  const int n = (int)std::max(s->row_nv.size(), s->col_nx.size());
+  if ((off && *off && std::strcmp(off, "0") != 0) || n <= 1) return VG_OK;
+  for (int q = 1; q < n; ++q) {
+    cudaStream_t side = nullptr;
+    SW_CHECK(cuda_status(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking), "sweep streams"));
+    s->side.push_back(side);
+  }
+  for (int q = 0; q < n; ++q) {
+    cudaEvent_t e = nullptr;
+    SW_CHECK(cuda_status(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "sweep events"));
+    s->ev.push_back(e);
+  }
+  s->concurrent = true;
+  return VG_OK;
+}
+
 int sweep_sequence(vg_sweep* s, int nsteps, double* e_hist, double* s_hist, int rows, int row0,
                    cudaStream_t st) {
   const double dt = s->dt;
@@ -878,7 +936,7 @@ int sweep_sequence(vg_sweep* s, int nsteps, double* e_hist, double* s_hist, int 
     a.dougherty = dg;
     a.tw = s->tw32;
     return cuda_status(prof_call(&s->prof, kind, st, [&] {
-                         for (size_t c = 0; c < s->row_nv.size(); ++c) {
+                         return over_classes(s, (int)s->row_nv.size(), st, [&](int c, cudaStream_t cs) {
                            cudaError_t err = cudaSuccess;
                            SweepRowArgs ac = a;
                            const int cls = (int)(std::find(s->nv_of_class.begin(), s->nv_of_class.end(),
@@ -889,7 +947,7 @@ int sweep_sequence(vg_sweep* s, int nsteps, double* e_hist, double* s_hist, int 
                            const bool kick = kind == SK_KICK;
 #define VG_ROW_CASE(NV)                                                                       \
   case NV:                                                                                    \
-    err = kick ? sweep_row_launch<NV, true>(s, (int)c, ac, st) : sweep_row_launch<NV>(s, (int)c, ac, st); \
+    err = kick ? sweep_row_launch<NV, true>(s, c, ac, cs) : sweep_row_launch<NV>(s, c, ac, cs); \
     break;
                            switch (s->row_nv[c]) {
                              VG_ROW_CASE(64)
@@ -897,33 +955,29 @@ int sweep_sequence(vg_sweep* s, int nsteps, double* e_hist, double* s_hist, int 
                              VG_ROW_CASE(256)
                              VG_ROW_CASE(512)
                              VG_ROW_CASE(1024)
-                             default: err = kick ? sweep_row_launch<2048, true>(s, (int)c, ac, st)
-                                                 : sweep_row_launch<2048>(s, (int)c, ac, st);
+                             default: err = kick ? sweep_row_launch<2048, true>(s, c, ac, cs)
+                                                 : sweep_row_launch<2048>(s, c, ac, cs);
                                       break;
                            }
 #undef VG_ROW_CASE
-                           if (err != cudaSuccess) return err;
-                         }
-                         return cudaSuccess;
+                           return err;
+                         });
                        }),
                        "sweep row pass");
   };
   SW_CHECK(row(0.5 * dt, 0.0, 0, 0, SK_KICK));
   for (int k = 0; k < nsteps; ++k) {
     SW_CHECK(cuda_status(prof_call(&s->prof, SK_X_DRIFT, st, [&] {
-                           for (size_t c = 0; c < s->col_nx.size(); ++c) {
-                             cudaError_t err = cudaSuccess;
+                           return over_classes(s, (int)s->col_nx.size(), st, [&](int c, cudaStream_t cs) {
                              switch (s->col_nx[c]) {
-                               case 8: err = sweep_col_launch<8>(s, (int)c, st); break;
-                               case 16: err = sweep_col_launch<16>(s, (int)c, st); break;
-                               case 32: err = sweep_col_launch<32>(s, (int)c, st); break;
-                               case 64: err = sweep_col_launch<64>(s, (int)c, st); break;
-                               case 128: err = sweep_col_launch<128>(s, (int)c, st); break;
-                               default: err = sweep_col_launch<256>(s, (int)c, st); break;
+                               case 8: return sweep_col_launch<8>(s, c, cs);
+                               case 16: return sweep_col_launch<16>(s, c, cs);
+                               case 32: return sweep_col_launch<32>(s, c, cs);
+                               case 64: return sweep_col_launch<64>(s, c, cs);
+                               case 128: return sweep_col_launch<128>(s, c, cs);
+                               default: return sweep_col_launch<256>(s, c, cs);
                              }
-                             if (err != cudaSuccess) return err;
-                           }
-                           return cudaSuccess;
+                           });
                          }),
                          "sweep x drift"));
     SW_CHECK(cuda_status(prof_call(&s->prof, SK_FIELD, st, [&] {
@@ -1144,6 +1198,7 @@ int vg_sweep_create(const vg_sweep_desc* d, vg_sweep** out) {
   SW_TRY(cuda_status(ensure_smem((const void*)k_sweep_field, field_smem), "sweep smem"));
   SW_TRY(sw_alloc<int>(s, &s->err, 1, nullptr, "sweep status"));
   SW_TRY(sweep_setup_tma(s));
+  SW_TRY(sweep_setup_streams(s));
   SW_TRY(cuda_status(cudaDeviceSynchronize(), "sweep setup"));
 #undef SW_TRY
   *out = s;

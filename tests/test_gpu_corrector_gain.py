@@ -6,9 +6,10 @@ on 64 held-out runs (seed 6) against the fine runs:
 - the one-step error on held-out pairs drops well below the uncorrected one;
 - the field-energy history of corrected coarse runs is closer to the fine
   runs than that of uncorrected coarse runs, on average over the runs;
-- the damping rate stays within 1% of the fine runs for the median run.
-The fine runs are the FP32 batched sweep, which the sweep tests hold to the
-FP64 oracle."""
+- the damping rate stays within 1% of the fine runs for the median run, and
+  as many runs are within 1% as without the correction.
+The fine runs are plain fine-grid FP64 runs: the batched FP64 step, which
+test_gpu_batch holds to the oracle at 1e-12."""
 
 import numpy as np
 import pytest
@@ -45,34 +46,49 @@ def test_one_step_error_drops_on_held_out_pairs(trained):
 
 def test_rollouts_against_fine_runs(trained):
     from vlapy_gb300 import corrector as cm
+    from vlapy_gb300.batch import Batch64
     from vlapy_gb300.diagnostics import damping_fit, mode_amplitude
     from vlapy_gb300.sweep import Sweep
     corr, _ = trained
     ev = cm.corrector_runs(64, seed=6)
-    fine = Sweep([dict(r, nv=1024) for r in ev])
+    fine = Batch64([dict(r, nv=1024) for r in ev])
+    f64, e64 = fine.initial_state()
+    ef, sf = fine.history(NSTEPS)
+    for c0 in range(0, NSTEPS, 500):
+        fine.run_steps(f64, e64, 500, ef, sf, row0=c0)
     coarse = Sweep([dict(r, nv=128) for r in ev])
     corrected = Sweep([dict(r, nv=128) for r in ev])
-    out = []
-    for sw in (fine, coarse):
-        sw.reset()
-        eh, sh = sw.history(NSTEPS)
-        sw.run_steps(NSTEPS, eh, sh)
-        out.append((eh, sh))
+    coarse.reset()
+    ec, sc = coarse.history(NSTEPS)
+    coarse.run_steps(NSTEPS, ec, sc)
     corrected.reset()
     ek, sk = corrected.history(NSTEPS)
     cm.run_corrected(corrected, corr, NSTEPS, ek, sk)
     torch.cuda.synchronize()
-    e2f, e2c, e2k = (s[:, :, 3].cpu().numpy() for s in (out[0][1], out[1][1], sk))
+    e2f = sf[:, torch.as_tensor(fine.slot, device=sf.device), 3].cpu().numpy()
+    e2c, e2k = (s[:, :, 3].cpu().numpy() for s in (sc, sk))
     assert np.isfinite(e2k).all()
     err_c = np.linalg.norm(e2c - e2f, axis=0) / np.linalg.norm(e2f, axis=0)
     err_k = np.linalg.norm(e2k - e2f, axis=0) / np.linalg.norm(e2f, axis=0)
     assert err_k.mean() < 0.5 * err_c.mean(), (err_k.mean(), err_c.mean())
     t = 0.1 * np.arange(1, NSTEPS + 1)
-    rel = []
+    rel, rel_c = [], []
     for i in range(len(ev)):
-        rf, _ = damping_fit(t, mode_amplitude(fine.e_of(out[0][0], i).cpu().numpy()), t_min=5.0, t_max=60.0)
+        rf, _ = damping_fit(t, mode_amplitude(fine.e_of(ef, i).cpu().numpy()), t_min=5.0, t_max=60.0)
         rk, _ = damping_fit(t, mode_amplitude(corrected.e_of(ek, i).cpu().numpy()), t_min=5.0, t_max=60.0)
-        if np.isfinite(rf) and np.isfinite(rk):
+        rc, _ = damping_fit(t, mode_amplitude(coarse.e_of(ec, i).cpu().numpy()), t_min=5.0, t_max=60.0)
+        if np.isfinite(rf) and np.isfinite(rk) and np.isfinite(rc):
             rel.append(abs(rk - rf) / abs(rf))
-    assert len(rel) > 48
+            rel_c.append(abs(rc - rf) / abs(rf))
+    rel, rel_c = np.array(rel), np.array(rel_c)
+    print("field energy mean error: corrected %.3e, coarse %.3e; damping median: corrected %.2e, coarse %.2e; "
+          "within 1%%: corrected %d, coarse %d of %d"
+          % (err_k.mean(), err_c.mean(), np.median(rel), np.median(rel_c), (rel <= 0.01).sum(),
+             (rel_c <= 0.01).sum(), rel.size))
+    assert rel.size > 48
     assert np.median(rel) <= 0.01, np.median(rel)
+    # the correction leaves the early-time damping rate as accurate as the
+    # uncorrected coarse grid has it
+    assert (rel <= 0.01).sum() >= (rel_c <= 0.01).sum()
+    assert np.median(rel) <= 1.5 * np.median(rel_c), (np.median(rel), np.median(rel_c))
+    fine.close()

@@ -271,10 +271,11 @@ class PairData:
                 self.feat[idx].contiguous())
 
 
-def generate_pairs(runs, n_steps=2000, every=50, first=50, dt=0.1, vmax=6.4):
+def generate_pairs(runs, n_steps=2000, every=50, first=50, dt=0.1, vmax=6.4, stride=1):
     """Training pairs from fine runs: at steps first, first+every, ... the fine
-    state is restricted and advanced one coarse step while the fine run
-    advances one fine step and is restricted (the target)."""
+    state is restricted and advanced `stride` coarse steps while the fine run
+    advances `stride` fine steps and is restricted (the target); a network
+    trained on them corrects every `stride` steps (run_corrected)."""
     pr = Pairing(runs, vmax=vmax, dt=dt)
     pr.fine.reset()
     xs, ps, ts = [], [], []
@@ -289,10 +290,10 @@ def generate_pairs(runs, n_steps=2000, every=50, first=50, dt=0.1, vmax=6.4):
         g, _ = pr.fine.get_state(e_out=ef)
         gc = pr.restrict(g)
         pr.coarse.set_state(gc.view(-1), ef)
-        pr.coarse.run_steps(1)
+        pr.coarse.run_steps(stride)
         x, _ = pr.coarse.get_state()
-        pr.fine.run_steps(1)
-        n += 1
+        pr.fine.run_steps(stride)
+        n += stride
         g1, _ = pr.fine.get_state()
         xs.append(x.view(pr.rows, NV).clone())
         ps.append(gc)
@@ -355,10 +356,10 @@ def train(corr, data, epochs=4, batch_runs=128, lr=1e-3, seed=0, log=None):
     return history
 
 
-def run_corrected(sweep, corr, nsteps, e_hist=None, series_hist=None, row0=0, stream=None):
+def run_corrected(sweep, corr, nsteps, e_hist=None, series_hist=None, row0=0, stream=None, stride=1):
     """Advance a coarse sweep (all runs nv = 128, one nx) by nsteps steps,
-    correcting every run after each step in place; histories as
-    Sweep.run_steps."""
+    correcting every run in place after every `stride` steps (the stride of
+    the network's training pairs); histories as Sweep.run_steps."""
     nx = {r["nx"] for r in sweep.runs}
     if len(nx) != 1 or any(r["nv"] != NV for r in sweep.runs):
         raise ValueError("the corrected path needs runs of one nx and nv = 128")
@@ -373,9 +374,12 @@ def run_corrected(sweep, corr, nsteps, e_hist=None, series_hist=None, row0=0, st
         feat = torch.as_tensor(np.repeat(nu_feature([r["nu"] for r in sweep.runs]), nx), dtype=torch.float32,
                                device="cuda")
         sweep._corr_feat = feat
-    for i in range(nsteps):
+    if stride < 1:
+        raise ValueError("stride must be at least 1")
+    for i in range(0, nsteps, stride):
+        n = min(stride, nsteps - i)
         prev.copy_(g)
-        sweep.run_steps(1, e_hist, series_hist, row0=row0 + i, stream=stream)
+        sweep.run_steps(n, e_hist, series_hist, row0=row0 + i, stream=stream)
         corr.apply(g, prev, feat, out=g, group_rows=nx, stream=stream)
     corr.check_status()
     return sweep
@@ -392,14 +396,14 @@ def fine_reference(runs, nsteps=2000, vmax=6.4, dt=0.1):
     return e2
 
 
-def rollout_error(corr, runs, e2_fine, vmax=6.4, dt=0.1):
+def rollout_error(corr, runs, e2_fine, vmax=6.4, dt=0.1, stride=1):
     """Per-run relative L2 error of the corrected coarse runs' field-energy
     history against the fine runs' (float64 CPU tensor [runs])."""
     nsteps = e2_fine.shape[0]
     sw = Sweep([dict(r, nv=NV) for r in runs], vmax=vmax, dt=dt)
     sw.reset()
     eh, sh = sw.history(nsteps)
-    run_corrected(sw, corr, nsteps, eh, sh)
+    run_corrected(sw, corr, nsteps, eh, sh, stride=stride)
     e2 = sh[:, :, 3]
     err = torch.linalg.norm(e2 - e2_fine, dim=0) / torch.linalg.norm(e2_fine, dim=0)
     sw.close()
@@ -407,7 +411,7 @@ def rollout_error(corr, runs, e2_fine, vmax=6.4, dt=0.1):
 
 
 def train_selected(data, val_runs, seeds=(0, 1, 2), epochs=4, batch_runs=128, lr=1e-3, max_rows=None,
-                   protect_modes=PROTECT_MODES, log=None):
+                   protect_modes=PROTECT_MODES, log=None, stride=1):
     """Train one network per seed (initialisation and shuffling) and keep the
     one whose corrected coarse runs follow the fine runs best on validation
     runs (the mean field-energy-history error over 2000 steps).  Training one
@@ -421,7 +425,7 @@ def train_selected(data, val_runs, seeds=(0, 1, 2), epochs=4, batch_runs=128, lr
     for seed in seeds:
         corr = Corrector(rows, tau=tau, seed=seed, protect_modes=protect_modes)
         hist = train(corr, data, epochs=epochs, batch_runs=batch_runs, lr=lr, seed=seed)
-        err = rollout_error(corr, val_runs, e2_fine)
+        err = rollout_error(corr, val_runs, e2_fine, stride=stride)
         score = float(err.mean())
         report.append({"seed": seed, "train_loss": hist[-1], "val_field_energy_err_mean": score,
                        "val_within_1pct": float((err <= 0.01).double().mean())})

@@ -237,18 +237,36 @@ def run_e2e(plan, f, e, storage, hist, tb_host, drv_host, W, K, stream, torch):
     sk = ("mean_n", "mean_j", "mean_T", "mean_e2", "mean_de2", "mean_f2", "mean_flogf")
     h2d = pin_t[0].numel() * 8 + pin_d[0].numel() * 8
     d2h = out_fields.numel() * 8 + out_series.numel() * 8
+    # the step's inputs go in on the compute stream; its stored fields and
+    # series come out on a copy stream while the next step runs, into one of
+    # two pinned buffers, and the host waits for every step's result one step
+    # later (the last one before the clock stops)
+    out_f = [out_fields, torch.empty_like(out_fields).pin_memory()]
+    out_s = [out_series, torch.empty_like(out_series).pin_memory()]
+    copy_stream = torch.cuda.Stream()
+    ev_step = [torch.cuda.Event() for _ in range(2)]
+    ev_copy = [torch.cuda.Event() for _ in range(2)]
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    with torch.cuda.stream(stream):
-        for i in range(W, W + K):
+    for n, i in enumerate(range(W, W + K)):
+        b = n % 2
+        with torch.cuda.stream(stream):
             tb[i].copy_(pin_t[i], non_blocking=True)
             db[i].copy_(pin_d[i], non_blocking=True)
             plan.run_steps(f, e, hist, tb, db, i, 1, use_graph=False, stream=stream)
+        ev_step[b].record(stream)
+        copy_stream.wait_event(ev_step[b])
+        if n >= 2:
+            ev_copy[b].synchronize()  # the host buffer b is free again
+        with torch.cuda.stream(copy_stream):
             for q, k in enumerate(fk):
-                out_fields[q].copy_(storage["fields"][k][i], non_blocking=True)
+                out_f[b][q].copy_(storage["fields"][k][i], non_blocking=True)
             for q, k in enumerate(sk):
-                out_series[q:q + 1].copy_(storage["series"][k][i:i + 1], non_blocking=True)
-            stream.synchronize()
+                out_s[b][q:q + 1].copy_(storage["series"][k][i:i + 1], non_blocking=True)
+        ev_copy[b].record(copy_stream)
+        if n > 0:
+            ev_copy[1 - b].synchronize()
+    ev_copy[(K - 1) % 2].synchronize()
     t1 = time.perf_counter()
     return (t1 - t0), h2d, d2h
 
@@ -295,21 +313,40 @@ def run_sweep_gpu(args, w, rank, world, global_rank=0):
     prof = sw.profile_read()
     sw.profile(False)
     # e2e: one C-ABI call per step (replaying its cached one-step graph), the
-    # step's e row and series read back to pinned memory
-    out_e = torch.empty(sw.x_points, dtype=torch.float64).pin_memory()
-    out_s = torch.empty((sw.n_runs, 7), dtype=torch.float64).pin_memory()
+    # step's e row and series read back to pinned host memory.  Steps write two
+    # history rows in turn; a copy stream takes each step's row to the host
+    # while the next step runs, and the host waits for every step's result
+    # one step later (the last one before the clock stops).  A step does not
+    # start before the copy of the row it overwrites has finished.
+    eh2, sh2 = sw.history(2)
+    out_e = [torch.empty(sw.x_points, dtype=torch.float64).pin_memory() for _ in range(2)]
+    out_s = [torch.empty((sw.n_runs, 7), dtype=torch.float64).pin_memory() for _ in range(2)]
+    copy_stream = torch.cuda.Stream()
+    ev_step = [torch.cuda.Event() for _ in range(2)]
+    ev_copy = [torch.cuda.Event() for _ in range(2)]
     with torch.cuda.stream(stream):
-        sw.run_steps(1, eh, sh, row0=0, use_graph=True, stream=stream)  # capture, untimed
+        for b in range(2):  # capture both rows' graphs, untimed
+            sw.run_steps(1, eh2, sh2, row0=b, use_graph=True, stream=stream)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    with torch.cuda.stream(stream):
-        for i in range(K):
-            sw.run_steps(1, eh, sh, row0=0, use_graph=True, stream=stream)
-            out_e.copy_(eh[0], non_blocking=True)
-            out_s.copy_(sh[0], non_blocking=True)
-            stream.synchronize()
+    for i in range(K):
+        b = i % 2
+        stream.wait_event(ev_copy[b])
+        with torch.cuda.stream(stream):
+            sw.run_steps(1, eh2, sh2, row0=b, use_graph=True, stream=stream)
+        ev_step[b].record(stream)
+        copy_stream.wait_event(ev_step[b])
+        with torch.cuda.stream(copy_stream):
+            out_e[b].copy_(eh2[b], non_blocking=True)
+            out_s[b].copy_(sh2[b], non_blocking=True)
+        ev_copy[b].record(copy_stream)
+        if i > 0:
+            ev_copy[1 - b].synchronize()
+    ev_copy[(K - 1) % 2].synchronize()
     e2e_sec = time.perf_counter() - t0
-    d2h = out_e.numel() * 8 + out_s.numel() * 8
+    if not (torch.equal(out_e[(K - 1) % 2], eh2[(K - 1) % 2].cpu()) and np.isfinite(out_e[0].numpy()).all()):
+        raise RuntimeError("e2e: the host copy of the last step's field differs from the device")
+    d2h = out_e[0].numel() * 8 + out_s[0].numel() * 8
     return ms, prof, clk, (e2e_sec, 0, d2h), sw
 
 

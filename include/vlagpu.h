@@ -259,6 +259,12 @@ int vg_sweep_reset(vg_sweep* sweep, vg_stream stream);
  * driver^2, f^2, f log f), for rows < hist_rows. */
 int vg_sweep_run_steps(vg_sweep* sweep, int32_t nsteps, double* e_hist, double* series_hist,
                        int32_t hist_rows, int32_t hist_row0, int32_t use_graph, vg_stream stream);
+/* Caller-created CUDA events (cudaEvent_t, as void*) that each following
+ * vg_sweep_run_steps call records on its stream after step k (k < n) has
+ * stored its history row, so that another stream can take that row to the
+ * host while the later steps run; n = 0 clears them.  The events must stay
+ * valid while they are set; graphs captured with them record them too. */
+int vg_sweep_set_step_events(vg_sweep* sweep, void* const* events, int32_t n);
 /* f = g + f0 of one run as float64 [nx][nv] and its e[nx] (DEVICE pointers) */
 int vg_sweep_read_run(vg_sweep* sweep, int32_t run, double* f_out, double* e_out, vg_stream stream);
 /* copy every run's FP32 deviation g = f - f0 (runs back to back, [nx][nv]

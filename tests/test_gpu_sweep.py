@@ -156,6 +156,41 @@ def test_sweep_classes_side_by_side_equal_serial():
         assert torch.equal(a.get_state()[0], b.get_state()[0])
 
 
+def test_sweep_step_events_stream_rows_out():
+    """Step events: one run_steps call records a caller event after each
+    step's history row is stored, so a copy stream can take row k to the host
+    while the later steps run.  Every row copied that way equals the final
+    history, and the events change nothing in the results."""
+    from vlapy_gb300.sweep import Sweep
+    runs = mixed_runs()
+    a, b = Sweep(runs), Sweep(runs)
+    for sw in (a, b):
+        sw.reset()
+    n = 6
+    ea, sa = a.history(n)
+    eb, sb = b.history(n)
+    events = [torch.cuda.Event() for _ in range(n)]
+    a.set_step_events(events)
+    stream, copy_stream = torch.cuda.Stream(), torch.cuda.Stream()
+    stream.wait_stream(torch.cuda.current_stream())
+    host_e = torch.zeros((n, a.x_points), dtype=torch.float64).pin_memory()
+    host_s = torch.zeros((n, a.n_runs, 7), dtype=torch.float64).pin_memory()
+    with torch.cuda.stream(stream):
+        a.run_steps(n, ea, sa, stream=stream)
+    for k in range(n):
+        copy_stream.wait_event(events[k])
+        with torch.cuda.stream(copy_stream):
+            host_e[k].copy_(ea[k], non_blocking=True)
+            host_s[k].copy_(sa[k], non_blocking=True)
+    a.set_step_events([])
+    b.run_steps(n, eb, sb)
+    torch.cuda.synchronize()
+    assert torch.equal(host_e, ea.cpu()) and torch.equal(ea, eb)
+    torch.testing.assert_close(host_s, sa.cpu(), rtol=0, atol=0, equal_nan=True)
+    torch.testing.assert_close(sa, sb, rtol=0, atol=0, equal_nan=True)
+    assert torch.equal(a.get_state()[0], b.get_state()[0])
+
+
 def test_sweep_config_distribution():
     from vlapy_gb300.sweep import sweep_config
     runs = sweep_config(4096)

@@ -115,6 +115,7 @@ EXPORTS = {
     "vg_sweep_damping": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_double, C.c_double, C.c_double,
                                    C.c_void_p, C.c_void_p, C.c_void_p]),
     "vg_sweep_status": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    "vg_sweep_set_step_events": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.c_int32]),
     "vg_sweep_profile_enable": (C.c_int, [C.c_void_p, C.c_int32]),
     "vg_sweep_profile_read": (C.c_int, [C.c_void_p, C.POINTER(VgProfEntry), C.c_int32, C.POINTER(C.c_int32)]),
     "vg_profile_enable": (C.c_int, [C.c_void_p, C.c_int32]),

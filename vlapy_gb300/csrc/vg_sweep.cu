@@ -681,7 +681,12 @@ struct vg_sweep {
   int2* row_items;
   std::vector<int> row_nv, row_first, row_count;
   size_t field_smem;
-  std::map<std::tuple<int, const void*, const void*, int, int, cudaStream_t>, cudaGraphExec_t> graphs;
+  std::map<std::tuple<int, const void*, const void*, int, int, cudaStream_t, unsigned>, cudaGraphExec_t> graphs;
+  // caller events recorded after each step of a vg_sweep_run_steps call
+  // (step k of the call records step_events[k]); events_gen tells the graphs
+  // captured with one set of events from those of another
+  std::vector<cudaEvent_t> step_events;
+  unsigned events_gen = 0;
   ProfState prof;
   // x-drift through the tensor-memory accelerator, per x class
   bool use_tma = false;           // some x class loads its tiles through the TMA
@@ -998,6 +1003,8 @@ int sweep_sequence(vg_sweep* s, int nsteps, double* e_hist, double* s_hist, int 
                            }),
                            "sweep store"));
     }
+    if (k < (int)s->step_events.size() && s->step_events[k])
+      SW_CHECK(cuda_status(cudaEventRecord(s->step_events[k], st), "sweep step event"));
   }
   return VG_OK;
 }
@@ -1254,7 +1261,8 @@ int vg_sweep_run_steps(vg_sweep* s, int32_t nsteps, double* e_hist, double* seri
     set_error("graph mode needs a non-default stream");
     return VG_ERR_ARG;
   }
-  const auto key = std::make_tuple(nsteps, (const void*)e_hist, (const void*)series_hist, hist_rows, hist_row0, st);
+  const auto key =
+      std::make_tuple(nsteps, (const void*)e_hist, (const void*)series_hist, hist_rows, hist_row0, st, s->events_gen);
   auto it = s->graphs.find(key);
   if (it == s->graphs.end()) {
     SW_CHECK(cuda_status(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed), "begin capture"));
@@ -1273,6 +1281,17 @@ int vg_sweep_run_steps(vg_sweep* s, int32_t nsteps, double* e_hist, double* seri
     it = s->graphs.emplace(key, exec).first;
   }
   return cuda_status(cudaGraphLaunch(it->second, st), "graph launch");
+}
+
+int vg_sweep_set_step_events(vg_sweep* s, void* const* events, int32_t n) {
+  if (!s || n < 0 || (n > 0 && !events)) {
+    set_error("null sweep, negative count or null event array");
+    return VG_ERR_ARG;
+  }
+  s->step_events.assign(n, nullptr);
+  for (int k = 0; k < n; ++k) s->step_events[k] = (cudaEvent_t)events[k];
+  ++s->events_gen;
+  return VG_OK;
 }
 
 int vg_sweep_read_run(vg_sweep* s, int32_t run, double* f_out, double* e_out, vg_stream stream) {

@@ -185,6 +185,21 @@ class Sweep:
         check(self._lib.vg_sweep_status(self._h, C.byref(flags), C.byref(tma)), "sweep status")
         return int(flags.value), bool(tma.value)
 
+    def set_step_events(self, events):
+        """torch.cuda.Event objects that each following run_steps call records
+        after step k has stored its history row (k < len(events)), so that
+        another stream can copy that row out while the later steps run; an
+        empty list clears them.  The events are recorded once here on the
+        current stream (which creates them) and must outlive their use."""
+        events = list(events)
+        for ev in events:
+            ev.record()
+        handles = (C.c_void_p * max(1, len(events)))(*[C.c_void_p(ev.cuda_event) for ev in events])
+        if any(h is None or h == 0 for h in (ev.cuda_event for ev in events)):
+            raise ValueError("every step event must be a created CUDA event")
+        check(self._lib.vg_sweep_set_step_events(self._h, handles, len(events)), "sweep step events")
+        self._step_events = events  # keep them alive while they are set
+
     def profile(self, enable):
         check(self._lib.vg_sweep_profile_enable(self._h, int(bool(enable))), "profile")
 

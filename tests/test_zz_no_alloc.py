@@ -91,3 +91,38 @@ def test_noalloc_on_a_second_stream(lib):
     torch.cuda.synchronize()
     a, b = out.cpu().numpy(), ref.cpu().numpy()
     assert np.linalg.norm(a - b) <= TOL * np.linalg.norm(b)
+
+
+def test_noalloc_call_captured_in_a_graph(lib):
+    """After the set-up call, a call copies nothing from host memory and only
+    launches kernels on the caller's stream, so it can be recorded into a CUDA
+    graph: two replays on new inputs give the plan-based field each time."""
+    from vlapy_gb300._lib import check
+    from vlapy_gb300.plan import Plan, ptr
+    nx, nv = 64, 512
+    f, drv, (x, v, kx, kv, inv, dx, dv) = _case(nx, nv, 11)
+    plan = Plan(nx, nv, x, v, kx, kv, inv, dx, dv)
+    ft, dt_, inv_t = (torch.as_tensor(a, device="cuda") for a in (f, drv, inv))
+    out = torch.zeros(nx, dtype=torch.float64, device="cuda")
+    check(lib.vg_field_solve_noalloc(ptr(ft), nx, nv, C.c_double(dv), ptr(inv_t), ptr(dt_), ptr(out),
+                                     C.c_void_p(torch.cuda.current_stream().cuda_stream)), "set-up call")
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        with torch.cuda.graph(graph, stream=s):
+            st = lib.vg_field_solve_noalloc(ptr(ft), nx, nv, C.c_double(dv), ptr(inv_t), ptr(dt_), ptr(out),
+                                            C.c_void_p(s.cuda_stream))
+    assert st == 0, lib.vg_last_error()
+    ref = torch.empty(nx, dtype=torch.float64, device="cuda")
+    for seed in (12, 13):
+        f2, drv2, _ = _case(nx, nv, seed)
+        ft.copy_(torch.as_tensor(f2))
+        dt_.copy_(torch.as_tensor(drv2))
+        out.fill_(float("nan"))
+        graph.replay()
+        plan.field_solve(ft, dt_, ref)
+        torch.cuda.synchronize()
+        a, b = out.cpu().numpy(), ref.cpu().numpy()
+        assert np.linalg.norm(a - b) <= TOL * np.linalg.norm(b), seed

@@ -484,6 +484,47 @@ def _damping_errors(t, sw_ref, e_ref, sw, e_hist, t_max=60.0):
     return np.array(out)
 
 
+def corrector_training_flops(rows):
+    """Tensor-core FLOPs one training step issues on the tcgen05 engine, per
+    batch of rows: forward (layer 1: 5 taps x K = 16 at N = 64; layers 2, 3:
+    5 taps x K = 64; layer 4: 5 taps x K = 64 at N = 16), data gradients
+    (layer 4: K = 16; layers 3, 2: K = 64; all N = 64) and weight gradients
+    (M = 128 stacks two taps (one for the input layer's five, padded): 3
+    groups x 8 K-steps at N = 16 and N = 64, one group at N = 64)."""
+    mma = lambda n, k_steps: 2.0 * 128 * n * 16 * k_steps  # noqa: E731
+    fwd = mma(64, 5) + 2 * mma(64, 20) + mma(16, 20)
+    dgrad = mma(64, 5) + 2 * mma(64, 20)
+    wgrad = mma(16, 24) + 2 * mma(64, 24) + mma(64, 8)
+    return rows * (fwd + dgrad + wgrad)
+
+
+def training_step_timing(cm, data, corr, torch, batch_runs=128, steps=20):
+    """ms per Adam step on one batch of batch_runs whole runs (batch_runs x nx
+    rows), on each engine, with CUDA events after two untimed steps."""
+    x, p, t, f = next(cm._batches(data, batch_runs))
+    rows = x.shape[0]
+    out = {"rows": rows}
+    for engine in ("tcgen05", "mma.sync"):
+        c = cm.Corrector(rows, params=corr.params, tau=corr.tau)
+        c.set_engine(engine)
+        for _ in range(2):
+            c.train_step(x, t, p, f, lr=1e-4, group_rows=data.nx)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            c.train_step(x, t, p, f, lr=1e-4, group_rows=data.nx)
+        e1.record()
+        torch.cuda.synchronize()
+        c.check_status()
+        ms = e0.elapsed_time(e1) / steps
+        out[engine] = {"ms_per_step": ms}
+        if engine == "tcgen05":
+            out[engine]["tensor_tflops_issued"] = corrector_training_flops(rows) / (ms / 1e3) / 1e12
+        c.close()
+    return out
+
+
 def learned_path(args, w):
     """The learned coarse-velocity path (runs of the sweep distribution at
     nx = 64): train the corrector on pairs from fine (nv = 1024) runs, judge
@@ -506,6 +547,7 @@ def learned_path(args, w):
     tau = corr.tau
     torch.cuda.synchronize()
     train_s = time.perf_counter() - t0
+    train_step = training_step_timing(cm, data, corr, torch)
     del data
     held = cm.generate_pairs(cm.corrector_runs(n_eval, seed=6), n_steps=nsteps)
     zero = cm.Corrector(128 * nx, params=np.zeros(corr.n_params, np.float32), tau=tau)
@@ -612,7 +654,7 @@ def learned_path(args, w):
         "workload": "%d training runs (seed 5), 64 validation runs (seed 7) choosing among 3 trained seeds, "
                     "%d held-out runs (seed 6) of the sweep distribution at nx=64; fine nv=1024, coarse nv=128, "
                     "vmax=6.4, dt=0.1, %d steps" % (args.learned_train, n_eval, nsteps),
-        "pairs_s": gen_s, "train_s": train_s, "model_selection": selection, "tau": tau,
+        "pairs_s": gen_s, "train_s": train_s, "train_step": train_step, "model_selection": selection, "tau": tau,
         "heldout_one_step_loss": {"uncorrected": base_loss, "corrected": loss, "ratio": loss / base_loss},
         "damping_rate_rel_err_vs_fine_fp64": {"fine_fp32": stats(dr_f), "coarse": stats(dr_c),
                                                "corrected": stats(dr_k)},

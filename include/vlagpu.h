@@ -351,14 +351,16 @@ int vg_corr_set_tau(vg_corrector* corr, float tau);
 int vg_corr_get_params(vg_corrector* corr, float* host_out);
 /* also clears the optimiser state */
 int vg_corr_set_params(vg_corrector* corr, const float* host_in);
-/* g_out may alias batch->g (in-place correction).  Engine 0 (default): one
- * fused persistent kernel per call on the tcgen05 tensor cores (weights and
- * activations in shared memory, accumulators in TMEM, bounded waits that
- * raise vg_corr_status).  Engine 1: the per-layer mma.sync kernels that the
- * training calls use. */
+/* g_out may alias batch->g (in-place correction).  Engine 0 (default), the
+ * tcgen05 tensor cores: apply is one fused persistent kernel per call
+ * (weights and activations in shared memory, accumulators in TMEM); the
+ * training calls (loss, gradients, train step) run one tcgen05 kernel per
+ * layer, forward, data gradient and weight gradient, keeping the activations
+ * in HBM for the backward pass.  Every wait is bounded and a wait that ran
+ * out raises vg_corr_status.  Engine 1: the same layers on mma.sync. */
 int vg_corr_apply(vg_corrector* corr, const vg_corr_batch* batch, float* g_out, vg_stream stream);
 int vg_corr_set_engine(vg_corrector* corr, int32_t engine);
-/* synchronises; VG_ERR_TIMEOUT (flags != 0) if a bounded wait of the fused
+/* synchronises; VG_ERR_TIMEOUT (flags != 0) if a bounded wait of a tcgen05
  * kernel ran out since the corrector was created */
 int vg_corr_status(vg_corrector* corr, int32_t* flags);
 /* loss only (synchronises the stream) */

@@ -117,14 +117,19 @@ def test_engines_agree_on_many_rows():
     assert float(torch.linalg.norm(da - db) / torch.linalg.norm(db)) <= 1e-3
 
 
+@pytest.mark.parametrize("engine", ["tcgen05", "mma.sync"])
 @pytest.mark.parametrize("group,modes", [(0, 0), (60, 32), (60, 0)])
-def test_gradients_match_oracle(group, modes):
+def test_gradients_match_oracle(group, modes, engine):
+    """Loss and every parameter's gradient against the CPU oracle, for the
+    training layers on either engine (tcgen05: forward, data-gradient and
+    weight-gradient kernels per layer; mma.sync: the legacy kernels)."""
     from vlapy_gb300.corrector import Corrector
     p = random_params(2)
     rows = 300
     g, t, feat, prev = random_rows(rows, 3, with_prev=True)
     tau = 2e-3
     corr = Corrector(rows, params=p, tau=tau, protect_modes=modes)
+    corr.set_engine(engine)
     gt, tt, ft, pt = (torch.as_tensor(a, device="cuda") for a in (g, t, feat, prev))
     loss, grad = corr.gradients(gt, tt, prev=pt, feat=ft, group_rows=group)
     loss_e, grad_e = co.loss_and_grads(p, g, feat, t, 6.4, tau, emulate=True, group_rows=group, protect_modes=modes,
@@ -151,6 +156,31 @@ def test_gradients_match_oracle(group, modes):
             # rounding flips differ; plain FP64: the BF16 quantisation itself
             assert rel(a, e) <= 5e-3, (name, rel(a, e))
             assert rel(a, x) <= 0.15, (name, rel(a, x))
+        o += n
+
+
+def test_training_engines_agree_on_many_rows():
+    """The tcgen05 training layers against the mma.sync ones on more rows than
+    the persistent CTAs' slots (every slot loops) and than the weight
+    gradient's row chunks hold (every chunk accumulates many rows in TMEM):
+    the same BF16 operands, so only the FP32 accumulation order and rare BF16
+    rounding flips of the activations separate their gradients."""
+    from vlapy_gb300.corrector import Corrector
+    p = random_params(6)
+    rows = 64 * 200
+    g, t, feat, prev = random_rows(rows, 12, with_prev=True)
+    gt, tt, ft, pt = (torch.as_tensor(a, device="cuda") for a in (g, t, feat, prev))
+    corr = Corrector(rows, params=p, tau=2e-3, protect_modes=32)
+    la, ga = corr.gradients(gt, tt, prev=pt, feat=ft, group_rows=64)
+    corr.check_status()
+    corr.set_engine("mma.sync")
+    lb, gb = corr.gradients(gt, tt, prev=pt, feat=ft, group_rows=64)
+    assert abs(la - lb) <= 1e-4 * lb
+    o = 0
+    for name, shape in co.SHAPES:
+        n = int(np.prod(shape))
+        if name != "b4":  # b4: noise of no fixed value under the projected loss
+            assert rel(ga[o:o + n], gb[o:o + n]) <= 5e-3, (name, rel(ga[o:o + n], gb[o:o + n]))
         o += n
 
 

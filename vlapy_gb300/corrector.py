@@ -151,13 +151,15 @@ class Corrector:
         self._tau = float(value)
 
     def set_engine(self, engine):
-        """"tcgen05" (default): the fused forward on the 5th-generation tensor
-        cores; "mma.sync": the per-layer kernels the training path uses."""
+        """"tcgen05" (default): the 5th-generation tensor cores, the fused
+        forward for apply and one kernel per layer (forward, data gradient,
+        weight gradient) for training; "mma.sync": the same layers on the
+        legacy warp-level MMA."""
         code = {"tcgen05": 0, "mma.sync": 1}[engine]
         check(self._lib.vg_corr_set_engine(self._h, code), "corrector engine")
 
     def check_status(self):
-        """Raise if a bounded wait of the fused kernel ran out (synchronises)."""
+        """Raise if a bounded wait of a tcgen05 kernel ran out (synchronises)."""
         flags = C.c_int32()
         check(self._lib.vg_corr_status(self._h, C.byref(flags)), "corrector status")
 

@@ -1062,6 +1062,343 @@ __global__ void k_pack_tc(const float* __restrict__ w, __nv_bfloat16* __restrict
   }
 }
 
+// ---------------------------------------------------------------------------
+// Training layers on the tensor cores (tcgen05).
+//
+// The training forward keeps every activation in HBM for the backward pass,
+// so it runs one layer per launch, and so do the data gradients (the same
+// convolution with the transposed, tap-flipped weights and the ReLU mask of
+// the forward activation).  k_conv_tc: persistent CTAs of TRN_SLOTS slots of
+// 4 warps; a slot takes one row at a time into its tile (the fused forward's
+// K-major layout with 2-row halos), its elected thread issues the layer's
+// MMAs (M = 128 positions, N = COUT, K = 5 taps x CIN; a tap is the tile
+// descriptor moved by 16 t bytes) into the slot's TMEM columns, and the
+// slot's epilogue writes the row channels-last to HBM.
+//
+// The weight gradients reduce over positions:
+// dW[o][c][t] = sum_rows sum_p dy[p][o] x[p + t - 2][c].  k_wgrad_tc makes
+// the position the MMA's K and keeps both operands in the MN-major layout,
+// which is the channels-last tile itself: 8 channels in 16 bytes, one
+// position per 16-byte row, so a tap shift along K is again the descriptor
+// moved by 16 t bytes.  M = 128 stacks copies of the input tile, copy q
+// shifted by q rows, so that one MMA covers taps (g NCOPY + q); N is the
+// output channels of dy.  Each CTA accumulates a chunk of rows in TMEM and
+// writes its partial sums; k_wgrad_reduce adds the chunks in a fixed order.
+// ---------------------------------------------------------------------------
+
+// descriptor of an MN-major operand (no swizzle): core matrices of 8 K rows
+// (positions) x 16 bytes (8 MN elements: channels); the leading-dimension
+// offset is the stride between 8-position groups along K and the stride
+// offset the one between 8-channel groups along MN (the gradient tests
+// against the CPU oracle hold this assignment; the swapped one fails them)
+__device__ __forceinline__ uint64_t tc_desc_mn(uint32_t addr, uint32_t mn_stride, uint32_t k_stride) {
+  return tc_desc(addr, k_stride, mn_stride);
+}
+
+constexpr int TRN_SLOTS = 4;
+constexpr int TRN_THREADS = 128 * TRN_SLOTS;
+
+__host__ __device__ constexpr int tmem_cols_for(int n) { return n <= 32 ? 32 : (n <= 64 ? 64 : (n <= 128 ? 128 : (n <= 256 ? 256 : 512))); }
+
+template <int CIN, int COUT>
+__host__ __device__ constexpr int trn_conv_wbytes() { return 5 * COUT * CIN * 2; }
+template <int CIN, int COUT>
+__host__ __device__ constexpr int trn_conv_smem() {
+  return trn_conv_wbytes<CIN, COUT>() + TRN_SLOTS * (CIN / 8) * TC_LBO_ACT + 8 * TRN_SLOTS + 16;
+}
+
+// MODE 0: out = relu(conv + b) (bf16); MODE 1: out[p] = conv + b, channel 0
+// only (fp32); MODE 2: out = conv * (mask > 0) (bf16, no bias).
+// w: bf16 [5][WROWS][CIN] (rows WROWS..COUT - 1 are zero)
+template <int CIN, int COUT, int WROWS, int MODE>
+__global__ void __launch_bounds__(TRN_THREADS, 1)
+    k_conv_tc(const __nv_bfloat16* __restrict__ x, const __nv_bfloat16* __restrict__ w,
+              const float* __restrict__ bias, const __nv_bfloat16* __restrict__ mask, void* out, int rows,
+              int* __restrict__ err) {
+  static_assert(CIN % 16 == 0 && COUT % 16 == 0 && WROWS <= COUT, "layer shape");
+  constexpr int WTAP = COUT * CIN * 2;
+  constexpr int W_BYTES = trn_conv_wbytes<CIN, COUT>();
+  constexpr int TILE = (CIN / 8) * TC_LBO_ACT;
+  constexpr int TMEM_COLS = tmem_cols_for(TRN_SLOTS * COUT);
+  extern __shared__ __align__(128) unsigned char smem[];
+  const uint32_t s_base = (uint32_t)__cvta_generic_to_shared(smem);
+  const uint32_t bar0 = s_base + W_BYTES + TRN_SLOTS * TILE;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + W_BYTES + TRN_SLOTS * TILE + 8 * TRN_SLOTS);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
+                     bar0 + 8 * TRN_SLOTS),
+                 "r"(TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+  }
+  if (threadIdx.x == 0) {
+    for (int q = 0; q < TRN_SLOTS; ++q)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar0 + 8 * q) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  // weights: tap t, output row n, input chunk j -> t WTAP + tc_off(n, 8 j, 16 COUT)
+  for (int i = threadIdx.x; i < 5 * COUT * (CIN / 8); i += TRN_THREADS) {
+    const int j = i % (CIN / 8), n = (i / (CIN / 8)) % COUT, t = i / ((CIN / 8) * COUT);
+    const uint4 v = n < WROWS ? reinterpret_cast<const uint4*>(w + ((size_t)t * WROWS + n) * CIN)[j]
+                              : make_uint4(0u, 0u, 0u, 0u);
+    *reinterpret_cast<uint4*>(smem + t * WTAP + tc_off(n, 8 * j, 16 * COUT)) = v;
+  }
+  // halo rows (0, 1, 130, 131) of every slot's tile stay zero
+  for (int i = threadIdx.x; i < TRN_SLOTS * 4 * (CIN / 8); i += TRN_THREADS) {
+    const int j = i % (CIN / 8), hr = (i / (CIN / 8)) % 4, sl = i / (4 * (CIN / 8));
+    const int hrow = hr < 2 ? hr : CROWS - 4 + hr;
+    *reinterpret_cast<uint4*>(smem + W_BYTES + sl * TILE + tc_off(hrow, 8 * j, TC_LBO_ACT)) =
+        make_uint4(0u, 0u, 0u, 0u);
+  }
+  fence_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+  const int slot = warp >> 2, quarter = warp & 3;
+  const int p = 32 * quarter + lane;
+  const bool issuer = (p == 0);
+  unsigned char* tile = smem + W_BYTES + slot * TILE;
+  const uint32_t tile_s = s_base + W_BYTES + slot * TILE;
+  const uint32_t td = tmem + COUT * slot, lane_base = (uint32_t)(quarter * 32) << 16;
+  const uint32_t bar = bar0 + 8 * slot;
+  uint32_t phase = 0;
+  int commits = 0;
+  bool ok = true;
+  for (int row = blockIdx.x * TRN_SLOTS + slot; row < rows; row += gridDim.x * TRN_SLOTS) {
+    const size_t q = (size_t)row * CP + p;
+    const uint4* src = reinterpret_cast<const uint4*>(x + q * CIN);
+#pragma unroll
+    for (int j = 0; j < CIN / 8; ++j)
+      *reinterpret_cast<uint4*>(tile + tc_off(p + CHALO, 8 * j, TC_LBO_ACT)) = src[j];
+    fence_async_smem();
+    tc_fence_before();
+    slot_sync(slot);
+    if (issuer) {
+      tc_fence_after();
+      tc_layer_issue<CIN, COUT>(td, tile_s, s_base);
+      tc_commit(bar);
+    }
+    ++commits;
+    const bool done = mbar_wait(bar, phase);
+    phase ^= 1u;
+    if (slot_any(slot, !done)) {
+      ok = false;
+      break;
+    }
+    tc_fence_after();
+#pragma unroll
+    for (int c0 = 0; c0 < (MODE == 1 ? 16 : COUT); c0 += 16) {
+      float v[16];
+      tc_ld16(td + lane_base + c0, v);
+      if (MODE == 1) {
+        static_cast<float*>(out)[q] = v[0] + bias[0];
+      } else {
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          uint32_t wv[4];
+          uint4 mk = make_uint4(0u, 0u, 0u, 0u);
+          if (MODE == 2) mk = reinterpret_cast<const uint4*>(mask + q * COUT + c0 + 8 * h)[0];
+          const __nv_bfloat162* m2 = reinterpret_cast<const __nv_bfloat162*>(&mk);
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const int c = c0 + 8 * h + 2 * j;
+            float a = v[8 * h + 2 * j], b = v[8 * h + 2 * j + 1];
+            if (MODE == 0) {
+              a = fmaxf(a + bias[c], 0.f);
+              b = fmaxf(b + bias[c + 1], 0.f);
+            } else {
+              if (!(__bfloat162float(m2[j].x) > 0.f)) a = 0.f;
+              if (!(__bfloat162float(m2[j].y) > 0.f)) b = 0.f;
+            }
+            const __nv_bfloat162 pr = __floats2bfloat162_rn(a, b);
+            wv[j] = *reinterpret_cast<const uint32_t*>(&pr);
+          }
+          reinterpret_cast<uint4*>(static_cast<__nv_bfloat16*>(out) + q * COUT + c0 + 8 * h)[0] =
+              make_uint4(wv[0], wv[1], wv[2], wv[3]);
+        }
+      }
+    }
+    // every thread of the slot has read its TMEM lanes before the next row's
+    // MMAs overwrite them
+    tc_fence_before();
+    slot_sync(slot);
+  }
+  if (!ok) {
+    if (p == 0) atomicOr(err, 1);
+    // no MMA of this slot may still write TMEM when it is freed
+    if (commits > 0) mbar_wait(bar, (uint32_t)((commits - 1) & 1));
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+  }
+}
+
+// weight-gradient shapes: NCOPY taps per MMA group (copies of the input tile
+// in M = 128), NGROUP groups for the five taps, R rows per copy
+template <int CIN>
+struct WgradShape {
+  static constexpr int NCOPY = CIN == 64 ? 2 : 5;
+  static constexpr int COPIES = 128 / CIN;  // copies in M (those >= NCOPY stay zero)
+  static constexpr int NGROUP = (5 + NCOPY - 1) / NCOPY;
+  static constexpr int R = CP + (NGROUP - 1) * NCOPY;
+  static constexpr int A_BYTES = 16 * R * 16;  // 16 chunks of 8 (copy, channel) rows
+};
+template <int CIN, int COUTP>
+__host__ __device__ constexpr int trn_wgrad_stage() {
+  return WgradShape<CIN>::A_BYTES + (COUTP / 8) * CP * 16;
+}
+template <int CIN, int COUTP>
+__host__ __device__ constexpr int trn_wgrad_smem() {
+  return 2 * trn_wgrad_stage<CIN, COUTP>() + 16 + 16;
+}
+
+// one CTA of 128 threads (thread p: position p of a row, then TMEM lane p)
+// per chunk of rows; two row stages, so that the tiles of a row are written
+// while the previous row's MMAs run.  part[chunk][t][o][c], bpart[chunk][o].
+template <int CIN, int COUTP>
+__global__ void __launch_bounds__(128, 1)
+    k_wgrad_tc(const __nv_bfloat16* __restrict__ x, const __nv_bfloat16* __restrict__ dy, int rows,
+               int rows_per_chunk, float* __restrict__ part, float* __restrict__ bpart, int* __restrict__ err) {
+  using S = WgradShape<CIN>;
+  static_assert(CIN == 64 || CIN == 16, "input channels");
+  static_assert(COUTP % 16 == 0 && COUTP <= 64, "output channels");
+  constexpr int STAGE = trn_wgrad_stage<CIN, COUTP>();
+  constexpr int TMEM_COLS = tmem_cols_for(S::NGROUP * COUTP);
+  constexpr uint32_t MN_A = (uint32_t)S::R * 16, MN_B = (uint32_t)CP * 16;
+  constexpr uint32_t idesc = tc_idesc(128, COUTP) | (1u << 15) | (1u << 16);  // A and B MN-major
+  extern __shared__ __align__(128) unsigned char smem[];
+  const uint32_t s_base = (uint32_t)__cvta_generic_to_shared(smem);
+  const uint32_t bar0 = s_base + 2 * STAGE;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + 2 * STAGE + 16);
+  const int warp = threadIdx.x >> 5, p = threadIdx.x;
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(bar0 + 16),
+                 "r"(TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+  }
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar0) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar0 + 8) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  // both stages zero: the rows a shifted copy never receives, and the copies
+  // beyond NCOPY, stay zero
+  for (int i = threadIdx.x; i < 2 * STAGE / 16; i += 128) reinterpret_cast<uint4*>(smem)[i] = make_uint4(0u, 0u, 0u, 0u);
+  fence_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+  const int r_begin = blockIdx.x * rows_per_chunk;
+  const int r_end = min(rows, r_begin + rows_per_chunk);
+  float bsum = 0.f;
+  uint32_t phase[2] = {0u, 0u};
+  bool pending[2] = {false, false};
+  bool ok = true;
+  int n = 0;
+  for (int row = r_begin; row < r_end; ++row, ++n) {
+    const int st = n & 1;
+    unsigned char* A = smem + st * STAGE;
+    unsigned char* B = A + S::A_BYTES;
+    if (pending[st]) {  // the MMAs of two rows ago read this stage
+      const bool done = mbar_wait(bar0 + 8 * st, phase[st]);
+      phase[st] ^= 1u;
+      pending[st] = false;
+      if (__syncthreads_or(!done)) {
+        ok = false;
+        break;
+      }
+      tc_fence_after();
+    }
+    const size_t q = (size_t)row * CP + p;
+    const uint4* xs = reinterpret_cast<const uint4*>(x + q * CIN);
+    const uint4* ys = reinterpret_cast<const uint4*>(dy + q * COUTP);
+#pragma unroll
+    for (int j = 0; j < CIN / 8; ++j) {
+      const uint4 v = xs[j];
+      // copy c holds x[r + c - 2] at row r
+#pragma unroll
+      for (int c = 0; c < S::NCOPY; ++c) {
+        const int r = p + CHALO - c;
+        if (r >= 0 && r < S::R) *reinterpret_cast<uint4*>(A + (c * (CIN / 8) + j) * MN_A + r * 16) = v;
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < COUTP / 8; ++j) *reinterpret_cast<uint4*>(B + j * MN_B + p * 16) = ys[j];
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      tc_fence_after();
+      const uint32_t a_s = s_base + st * STAGE, b_s = a_s + S::A_BYTES;
+#pragma unroll
+      for (int g = 0; g < S::NGROUP; ++g) {
+#pragma unroll
+        for (int ks = 0; ks < CP / 16; ++ks) {
+          const uint64_t a = tc_desc_mn(a_s + 16 * (g * S::NCOPY) + 256 * ks, MN_A, 128);
+          const uint64_t b = tc_desc_mn(b_s + 256 * ks, MN_B, 128);
+          tc_mma(tmem + g * COUTP, a, b, idesc, (row > r_begin || ks > 0) ? 1 : 0);
+        }
+      }
+      tc_commit(bar0 + 8 * st);
+    }
+    pending[st] = true;
+    // bias gradient: column sums of dy over the row's positions
+    if (threadIdx.x < COUTP) {
+      const int o = threadIdx.x;
+      const unsigned char* col = B + (o >> 3) * MN_B + (o & 7) * 2;
+      float rs = 0.f;
+      for (int pp = 0; pp < CP; ++pp) rs += __bfloat162float(*reinterpret_cast<const __nv_bfloat16*>(col + pp * 16));
+      bsum += rs;
+    }
+  }
+  // the outstanding commits of both stages
+  for (int st = 0; st < 2; ++st)
+    if (pending[st]) {
+      const bool done = mbar_wait(bar0 + 8 * st, phase[st]);
+      if (!done) ok = false;
+    }
+  ok = !__syncthreads_or(!ok);
+  tc_fence_after();
+  if (ok && r_end > r_begin) {
+    const int c = p % CIN, cp = p / CIN;  // TMEM lane p = (copy, channel)
+    const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+#pragma unroll
+    for (int g = 0; g < S::NGROUP; ++g) {
+#pragma unroll
+      for (int c0 = 0; c0 < COUTP; c0 += 16) {
+        float v[16];
+        tc_ld16(tmem + lane_base + g * COUTP + c0, v);
+        const int t = g * S::NCOPY + cp;
+        if (cp < S::NCOPY && t < 5) {
+          float* dst = part + (((size_t)blockIdx.x * 5 + t) * COUTP + c0) * CIN + c;
+#pragma unroll
+          for (int j = 0; j < 16; ++j) dst[(size_t)j * CIN] = v[j];
+        }
+      }
+    }
+    if (threadIdx.x < COUTP) bpart[(size_t)blockIdx.x * COUTP + threadIdx.x] = bsum;
+  } else if (r_end > r_begin) {
+    if (threadIdx.x == 0) atomicOr(err, 1);
+  } else {
+    // an empty chunk contributes zeros
+    for (int i = threadIdx.x; i < 5 * COUTP * CIN; i += 128) part[(size_t)blockIdx.x * 5 * COUTP * CIN + i] = 0.f;
+    if (threadIdx.x < COUTP) bpart[(size_t)blockIdx.x * COUTP + threadIdx.x] = 0.f;
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+  }
+}
+
 }  // namespace vg
 
 using namespace vg;
@@ -1082,7 +1419,7 @@ struct vg_corrector {
   float *pred, *scale, *part, *bpart, *loss_part;
   float2 *gmean, *tmean, *pmean;  // group means [groups][128] as double-float pairs
   float vmax, tau;
-  int engine;               // 0: fused tcgen05 forward, 1: per-layer mma.sync kernels
+  int engine;               // 0: tcgen05 (fused inference, per-layer training), 1: mma.sync kernels
   int n_sm;
   __nv_bfloat16* wtc;       // the fused kernel's weight image [TC_W_BYTES / 2]
   cx<double>* tw64;         // FFT twiddles of the projection
@@ -1141,6 +1478,34 @@ cudaError_t wgrad(vg_corrector* c, const __nv_bfloat16* x, const __nv_bfloat16* 
   return cudaGetLastError();
 }
 
+// the training layers on the tensor cores (engine 0)
+template <int CIN, int COUT, int WROWS, int MODE>
+cudaError_t conv_tc(vg_corrector* c, const __nv_bfloat16* x, const __nv_bfloat16* w, const float* b,
+                    const __nv_bfloat16* mask, void* out, int rows, cudaStream_t s) {
+  constexpr int smem = trn_conv_smem<CIN, COUT>();
+  cudaError_t err = ensure_smem((const void*)k_conv_tc<CIN, COUT, WROWS, MODE>, smem);
+  if (err != cudaSuccess) return err;
+  const int grid = std::max(1, std::min(c->n_sm, div_up(rows, TRN_SLOTS)));
+  k_conv_tc<CIN, COUT, WROWS, MODE><<<grid, TRN_THREADS, smem, s>>>(x, w, b, mask, out, rows, c->err);
+  return cudaGetLastError();
+}
+
+template <int CIN, int COUTP>
+cudaError_t wgrad_tc(vg_corrector* c, const __nv_bfloat16* x, const __nv_bfloat16* dy, int rows, int cout, float* dw,
+                     float* db, cudaStream_t s) {
+  const int chunks = wgrad_chunks(rows);
+  const int per = div_up(rows, chunks);
+  constexpr int smem = trn_wgrad_smem<CIN, COUTP>();
+  cudaError_t err = ensure_smem((const void*)k_wgrad_tc<CIN, COUTP>, smem);
+  if (err != cudaSuccess) return err;
+  k_wgrad_tc<CIN, COUTP><<<chunks, 128, smem, s>>>(x, dy, rows, per, c->part, c->bpart, c->err);
+  err = cudaGetLastError();
+  if (err != cudaSuccess) return err;
+  k_wgrad_reduce<<<div_up(cout * CIN * 5 + cout, 256), 256, 0, s>>>(c->part, c->bpart, chunks, COUTP, CIN, cout, dw,
+                                                                   db);
+  return cudaGetLastError();
+}
+
 int pack_all(vg_corrector* c, cudaStream_t s) {
   struct L {
     int off, cout, cin, frows, bcols;
@@ -1172,10 +1537,18 @@ int forward(vg_corrector* c, const vg_corr_batch& b, cudaStream_t s) {
   k_features<<<rows, CP, 0, s>>>(b.g, c->gmean, b.g_prev, c->pmean, group_rows, b.row_feat, rows, c->vmax, c->x0,
                                  c->scale);
   CR_CHECK(cuda_status(cudaGetLastError(), "corrector features"));
-  CR_CHECK(cuda_status(conv<L1_IN, HID, 0>(c->x0, c->w1f, c->params + OFF_B1, nullptr, c->a1, rows, s), "conv1"));
-  CR_CHECK(cuda_status(conv<HID, HID, 0>(c->a1, c->w2f, c->params + OFF_B2, nullptr, c->a2, rows, s), "conv2"));
-  CR_CHECK(cuda_status(conv<HID, HID, 0>(c->a2, c->w3f, c->params + OFF_B3, nullptr, c->a3, rows, s), "conv3"));
-  CR_CHECK(cuda_status(conv<HID, L4_OUT, 1>(c->a3, c->w4f, c->params + OFF_B4, nullptr, c->pred, rows, s), "conv4"));
+  const float* P = c->params;
+  if (c->engine == 0) {
+    CR_CHECK(cuda_status(conv_tc<L1_IN, HID, HID, 0>(c, c->x0, c->w1f, P + OFF_B1, nullptr, c->a1, rows, s), "conv1"));
+    CR_CHECK(cuda_status(conv_tc<HID, HID, HID, 0>(c, c->a1, c->w2f, P + OFF_B2, nullptr, c->a2, rows, s), "conv2"));
+    CR_CHECK(cuda_status(conv_tc<HID, HID, HID, 0>(c, c->a2, c->w3f, P + OFF_B3, nullptr, c->a3, rows, s), "conv3"));
+    CR_CHECK(cuda_status(conv_tc<HID, 16, L4_OUT, 1>(c, c->a3, c->w4f, P + OFF_B4, nullptr, c->pred, rows, s), "conv4"));
+    return VG_OK;
+  }
+  CR_CHECK(cuda_status(conv<L1_IN, HID, 0>(c->x0, c->w1f, P + OFF_B1, nullptr, c->a1, rows, s), "conv1"));
+  CR_CHECK(cuda_status(conv<HID, HID, 0>(c->a1, c->w2f, P + OFF_B2, nullptr, c->a2, rows, s), "conv2"));
+  CR_CHECK(cuda_status(conv<HID, HID, 0>(c->a2, c->w3f, P + OFF_B3, nullptr, c->a3, rows, s), "conv3"));
+  CR_CHECK(cuda_status(conv<HID, L4_OUT, 1>(c->a3, c->w4f, P + OFF_B4, nullptr, c->pred, rows, s), "conv4"));
   return VG_OK;
 }
 
@@ -1203,6 +1576,16 @@ int read_loss(vg_corrector* c, int rows, double* loss_out, cudaStream_t s) {
 // gradients of the loss into c->grads (after forward and loss)
 int backward(vg_corrector* c, int rows, cudaStream_t s) {
   float* G = c->grads;
+  if (c->engine == 0) {
+    CR_CHECK(cuda_status(wgrad_tc<HID, 16>(c, c->a3, c->dy4, rows, 1, G + OFF_W4, G + OFF_B4, s), "wgrad4"));
+    CR_CHECK(cuda_status(conv_tc<16, HID, HID, 2>(c, c->dy4, c->w4b, nullptr, c->a3, c->d3, rows, s), "dgrad4"));
+    CR_CHECK(cuda_status(wgrad_tc<HID, HID>(c, c->a2, c->d3, rows, HID, G + OFF_W3, G + OFF_B3, s), "wgrad3"));
+    CR_CHECK(cuda_status(conv_tc<HID, HID, HID, 2>(c, c->d3, c->w3b, nullptr, c->a2, c->d2, rows, s), "dgrad3"));
+    CR_CHECK(cuda_status(wgrad_tc<HID, HID>(c, c->a1, c->d2, rows, HID, G + OFF_W2, G + OFF_B2, s), "wgrad2"));
+    CR_CHECK(cuda_status(conv_tc<HID, HID, HID, 2>(c, c->d2, c->w2b, nullptr, c->a1, c->d1, rows, s), "dgrad2"));
+    CR_CHECK(cuda_status(wgrad_tc<L1_IN, HID>(c, c->x0, c->d1, rows, HID, G + OFF_W1, G + OFF_B1, s), "wgrad1"));
+    return VG_OK;
+  }
   CR_CHECK(cuda_status(wgrad<HID, 16>(c, c->a3, c->dy4, rows, 1, G + OFF_W4, G + OFF_B4, s), "wgrad4"));
   CR_CHECK(cuda_status(conv<16, HID, 2>(c->dy4, c->w4b, nullptr, c->a3, c->d3, rows, s), "dgrad4"));
   CR_CHECK(cuda_status(wgrad<HID, HID>(c, c->a2, c->d3, rows, HID, G + OFF_W3, G + OFF_B3, s), "wgrad3"));
@@ -1414,7 +1797,7 @@ int vg_corr_apply(vg_corrector* c, const vg_corr_batch* b, float* g_out, vg_stre
 
 int vg_corr_set_engine(vg_corrector* c, int32_t engine) {
   if (!c || engine < 0 || engine > 1) {
-    set_error("corrector: engine must be 0 (fused tcgen05) or 1 (per-layer mma.sync)");
+    set_error("corrector: engine must be 0 (tcgen05) or 1 (per-layer mma.sync)");
     return VG_ERR_ARG;
   }
   c->engine = engine;

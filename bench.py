@@ -45,6 +45,8 @@ WORKLOADS = {
     "corrector": dict(kind="corrector", n_runs=2048, nx=64, vmax=6.4),
     # the plain FP64 GPU method on the sweep's runs: the batched FP64 step alone
     "fp64sweep": dict(kind="fp64sweep", n_runs=4096, seed=20261203, vmax=6.4, dt=0.1),
+    # one Adam step of the corrector on a training batch of 128 runs x 64 rows
+    "corrector-train": dict(kind="corrector-train", n_runs=128, nx=64, vmax=6.4),
 }
 
 
@@ -741,6 +743,72 @@ def main_corrector(args, w, rank, world):
     print(json.dumps(line))
 
 
+def main_corrector_train(args, w, rank, world):
+    """Time one training step (vg_corr_train_step: forward layers, projected
+    loss, data and weight gradients, Adam, weight packing) of the corrector on
+    a batch of 128 runs x 64 rows (seeded synthetic rows, targets and
+    weights), on the tcgen05 engine and, for comparison, on mma.sync."""
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps({"impl": "reference", "unavailable": "the corrector has no reference counterpart"}))
+        return
+    import torch
+    from vlapy_gb300 import corrector as cm
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", rank)) % max(1, torch.cuda.device_count()))
+    nx, runs = w["nx"], w["n_runs"]
+    rows = runs * nx
+    rng = np.random.default_rng(12)
+    v = -w["vmax"] + 2 * w["vmax"] / cm.NV * (np.arange(cm.NV) + 0.5)
+    base = np.exp(-v ** 2 / 2)[None, :]
+    g = torch.as_tensor((1e-3 * base * rng.standard_normal((rows, cm.NV))).astype(np.float32), device="cuda")
+    prev = (g * 0.99).contiguous()
+    target = (g + 1e-5 * torch.as_tensor(rng.standard_normal((rows, cm.NV)).astype(np.float32), device="cuda"))
+    feat = torch.full((rows,), 0.5, dtype=torch.float32, device="cuda")
+    K, W = args.steps, args.warmup
+    out = {}
+    clk = None
+    for engine in ("tcgen05", "mma.sync"):
+        corr = cm.Corrector(rows, params=cm.init_params(3), tau=0.02)
+        corr.set_engine(engine)
+        for _ in range(W):
+            corr.train_step(g, target, prev, feat, lr=1e-4, group_rows=nx)
+        torch.cuda.synchronize()
+        if engine == "tcgen05":
+            clocks = ClockSampler(torch.cuda.current_device())
+            clocks.start()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(K):
+            corr.train_step(g, target, prev, feat, lr=1e-4, group_rows=nx)
+        e1.record()
+        torch.cuda.synchronize()
+        if engine == "tcgen05":
+            clk = clocks.stop()
+        corr.check_status()
+        out[engine] = e0.elapsed_time(e1) / K
+        corr.close()
+    if rank != 0:
+        return
+    ms = out["tcgen05"]
+    flops = corrector_training_flops(rows)
+    pk = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["bf16_tflops"] if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else 1900.0
+    tf = flops / (ms / 1e3) / 1e12
+    line = {"metric": "trained rows/s", "value": rows / (ms / 1e3), "unit": "rows/s", "n_gpus": 1, "steps": K,
+            "warmup": W, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "bf16", "data": "synthetic",
+            "config": {"workload": "corrector-train", "rows": rows, "nv": cm.NV,
+                       "engine": "tcgen05 per-layer forward, data- and weight-gradient kernels"},
+            "mma_sync_ms_per_step": out["mma.sync"],
+            "roofline": {"bound": "tensor", "achieved": tf, "peak": pk, "unit": "TFLOP/s", "frac": tf / pk,
+                         "traffic": None, "peak_source": "measured" if pk != 1900.0 else "fallback",
+                         "flops_per_step": flops,
+                         "note": "issued MMA FLOPs of the nine layer kernels; they are bound by their activation "
+                                 "traffic in HBM, not by the MMAs"},
+            "e2e": None, "gpu_launches": None, "clocks": clk, "cpu_baseline": None}
+    print(json.dumps(line))
+
+
 def _oracle_sweep_sample(args):
     """One pool task: oracle steps of one sampled sweep run (host cores)."""
     r, steps, vmax, dt = args
@@ -869,6 +937,8 @@ def main():
         return main_sweep(args, w, rank, world)
     if w["kind"] == "corrector":
         return main_corrector(args, w, rank, world)
+    if w["kind"] == "corrector-train":
+        return main_corrector_train(args, w, rank, world)
     if w["kind"] == "fp64sweep":
         return main_fp64sweep(args, w, rank, world)
     cells = w["nx"] * w["nv"]

@@ -38,6 +38,7 @@ struct RowArgs {
   double* mom;      // [nx][8] slots, each the raw double-float sum (df32) of one moment
   int n_modes;
   cx<float>* mpart; // [grid][n_modes][nv] per-CTA partial x modes
+  int macc_global;  // the CTA accumulates its x modes in its mpart slice (else in shared memory)
   const cx<float>* F0;  // [nv/2+1] unnormalised FFT_v(f0)
   const cx<float>* tw;
   // the row constants in device memory: a kernel that built a RowConsts
@@ -77,7 +78,10 @@ __host__ __device__ constexpr int col32_seqs(int nx, int r) {
   return (nx / r) * col32_seqs_raw(nx / r) <= 512 ? col32_seqs_raw(nx / r)
                                                    : (512 / (nx / r) > 1 ? 512 / (nx / r) : 1);
 }
-__host__ __device__ constexpr int row32_radix(int n) { return n <= 8 ? n : (n <= 4096 ? 8 : 16); }
+// row radix of the single-run kernels: radix 8 up to 4096; radix 32 above
+// (8192 = 32 x 32 x 8: three passes, and a 256-thread row-pair group that
+// leaves room for a second CTA on the SM to hide the passes' barriers)
+__host__ __device__ constexpr int row32_radix(int n) { return n <= 8 ? n : (n <= 4096 ? 8 : 32); }
 __host__ __device__ constexpr int row32_block(int n, int r) { return (n / r) >= 256 ? (n / r) : 256; }
 // per row-pair group, each part 16-byte aligned: padded sequence (sp_len,
 // the layout the row kernels index), boundary-solve scratch of 8G floats

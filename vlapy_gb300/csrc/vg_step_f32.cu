@@ -114,21 +114,27 @@ __global__ void __launch_bounds__(fft_threads<float>(NX)) k_field_f32(
 
 // KICK: a launch that only kicks (no collision, no moments, no trailing
 // kick), a lighter instantiation at two CTAs per SM
+// (radix 32: two CTAs of 128 registers a thread per SM)
 template <int N, int R, bool KICK = false>
-__global__ void __launch_bounds__(row32_block(N, R), KICK ? 2 : 1) k_row_f32(RowArgs a) {
+__global__ void __launch_bounds__(row32_block(N, R), (KICK || R == 32) ? 2 : 1) k_row_f32(RowArgs a) {
   constexpr int G = N / R;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int P = blockDim.x / G;
   const int grp = threadIdx.x / G, t = threadIdx.x - grp * G;
   const size_t grp_bytes = row32_group_bytes(N, R);
-  cx<float>* macc = reinterpret_cast<cx<float>*>(smem_raw + (size_t)P * grp_bytes);  // [n_modes][N]
   const int nm = a.want_mom ? a.n_modes : 0;
+  // x-mode accumulators [n_modes][N]: in shared memory, or (long rows, where
+  // they would crowd the row-pair groups out) in this CTA's slice of the
+  // mode partials, where they stay in L2; element n is only touched by the
+  // threads t = n mod G, in turns of the CTA's groups
+  cx<float>* macc = a.macc_global ? a.mpart + (size_t)blockIdx.x * nm * N
+                                  : reinterpret_cast<cx<float>*>(smem_raw + (size_t)P * grp_bytes);
   for (int q = threadIdx.x; q < nm * N; q += blockDim.x) macc[q] = {0.f, 0.f};
   const int npairs = (a.nx + 1) / 2;
   const int ngroups = (npairs + P - 1) / P;
   for (int pg = blockIdx.x; pg < ngroups; pg += gridDim.x)
     row_pair<N, R, CtaSync, 6, KICK>(a, pg * P + grp, smem_raw + (size_t)grp * grp_bytes, macc, P, grp, t);
-  if (nm > 0) {
+  if (nm > 0 && !a.macc_global) {
     __syncthreads();
     for (int q = threadIdx.x; q < nm * N; q += blockDim.x)
       a.mpart[(size_t)blockIdx.x * nm * N + q] = macc[q];
@@ -180,30 +186,40 @@ __global__ void k_store_series_f32(const float2* __restrict__ spart, int nb, int
 // stored x-modes of one step: thread (j, m) adds mode m of velocity j over
 // the row kernel's per-CTA partials, in four interleaved double-float chains
 // (partials p = 0, 4, 8, ... in the first, and so on) joined in a fixed order
-__global__ void k_store_modes_f32(const cx<float>* __restrict__ mpart, int npart, int nm, int nv, int nx,
-                                  const double* __restrict__ f0, int n_slots, int i, cx<float>* __restrict__ out) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+// stored x modes of one step: the CTAs' mode partials summed in double-float.
+// A block is 32 bins x STORE_MODE_SPLIT slice ranges: thread (jx, gy) sums
+// the slices of range gy for bin j (consecutive jx, consecutive j: coalesced),
+// then the ranges are added in order (deterministic)
+constexpr int STORE_MODE_SPLIT = 8;
+__global__ void __launch_bounds__(32 * STORE_MODE_SPLIT) k_store_modes_f32(
+    const cx<float>* __restrict__ mpart, int npart, int nm, int nv, int nx, const double* __restrict__ f0,
+    int n_slots, int i, cx<float>* __restrict__ out) {
+  __shared__ df32 part_re[STORE_MODE_SPLIT][32], part_im[STORE_MODE_SPLIT][32];
+  const int jx = threadIdx.x & 31, gy = threadIdx.x >> 5;
+  const int j = blockIdx.x * 32 + jx;
   const int m = blockIdx.y;
-  if (j >= nv || m >= nm || m >= n_slots) return;
-  cx<float>* dst = out + (size_t)i * n_slots * nv;
-  df32 re[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
-  df32 im[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
-  int p = 0;
-  for (; p + 4 <= npart; p += 4) {
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const cx<float> z = mpart[((size_t)(p + u) * nm + m) * nv + j];
+  const bool live = j < nv && m < nm && m < n_slots;
+  df32 re[2] = {{0.f, 0.f}, {0.f, 0.f}}, im[2] = {{0.f, 0.f}, {0.f, 0.f}};
+  if (live) {
+    const int per = (npart + STORE_MODE_SPLIT - 1) / STORE_MODE_SPLIT;
+    const int p0 = gy * per, p1 = min(npart, p0 + per);
+    int p = p0, u = 0;
+    for (; p < p1; ++p, u ^= 1) {
+      const cx<float> z = mpart[((size_t)p * nm + m) * nv + j];
       re[u] = df_add(re[u], {z.x, 0.f});
       im[u] = df_add(im[u], {z.y, 0.f});
     }
   }
-  for (int u = 0; p < npart; ++p, ++u) {
-    const cx<float> z = mpart[((size_t)p * nm + m) * nv + j];
-    re[u] = df_add(re[u], {z.x, 0.f});
-    im[u] = df_add(im[u], {z.y, 0.f});
+  part_re[gy][jx] = df_add(re[0], re[1]);
+  part_im[gy][jx] = df_add(im[0], im[1]);
+  __syncthreads();
+  if (gy != 0 || !live) return;
+  df32 rs = part_re[0][jx], is = part_im[0][jx];
+  for (int q = 1; q < STORE_MODE_SPLIT; ++q) {
+    rs = df_add(rs, part_re[q][jx]);
+    is = df_add(is, part_im[q][jx]);
   }
-  const df32 rs = df_add(df_add(re[0], re[1]), df_add(re[2], re[3]));
-  const df32 is = df_add(df_add(im[0], im[1]), df_add(im[2], im[3]));
+  cx<float>* dst = out + (size_t)i * n_slots * nv;
   double zr = df_to_double(rs), zi = df_to_double(is);
   if (m == 0) zr += (double)nx * f0[j];
   const cx<float> z = {(float)zr, (float)zi};
@@ -262,7 +278,9 @@ cudaError_t row_nk(const vg_plan& p, RowArgs a, cudaStream_t s) {
   const int P = block / G;
   const int npairs = (p.nx + 1) / 2;
   const int ngroups = (npairs + P - 1) / P;
-  const size_t smem = (size_t)P * row32_group_bytes(N, R) + (size_t)a.n_modes * N * sizeof(cx<float>);
+  const size_t mode_bytes = (size_t)(a.want_mom ? a.n_modes : 0) * N * sizeof(cx<float>);
+  a.macc_global = (size_t)P * row32_group_bytes(N, R) + mode_bytes > ((size_t)100 << 10) ? 1 : 0;
+  const size_t smem = (size_t)P * row32_group_bytes(N, R) + (a.macc_global ? 0 : mode_bytes);
   cudaError_t err = ensure_smem((const void*)k_row_f32<N, R, KICK>, smem);
   if (err != cudaSuccess) return err;
   int occ = 1;
@@ -377,6 +395,7 @@ cudaError_t launch_row_f32(const vg_plan& p, float* g, const double* e, double d
   a.mom = p.mom;
   a.n_modes = mom ? n_modes : 0;
   a.mpart = p.f32->mpart;
+  a.macc_global = 0;
   a.F0 = p.f32->F0;
   a.tw = p.tw32;
   a.rc = p.f32->rc_dev;
@@ -404,7 +423,7 @@ cudaError_t launch_store_f32(const vg_plan& p, const float* g, const double* e, 
     return cudaGetLastError();
   }
   if (h.stored_f && !h.store_all && n_modes > 0) {
-    k_store_modes_f32<<<dim3(div_up(p.nv, 128), n_modes), 128, 0, s>>>(
+    k_store_modes_f32<<<dim3(div_up(p.nv, 32), n_modes), 32 * STORE_MODE_SPLIT, 0, s>>>(
         p.f32->mpart, p.f32->mgrid, n_modes, p.nv, p.nx, p.f_bg, h.n_slots, i, static_cast<cx<float>*>(h.stored_f));
     err = cudaGetLastError();
   }

@@ -475,6 +475,7 @@ __global__ void __launch_bounds__(sweep_row_block(N), KICK ? (sweep_row_radix(N)
   a.mom = sa.mom + (size_t)r.x_off * MOM_STRIDE;
   a.n_modes = 0;
   a.mpart = nullptr;
+  a.macc_global = 0;
   a.F0 = scp->F0[r.cls];
   a.tw = sa.tw;
   a.rc = &scp->rc[r.cls];

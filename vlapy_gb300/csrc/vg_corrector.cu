@@ -1098,13 +1098,23 @@ __device__ __forceinline__ uint64_t tc_desc_mn(uint32_t addr, uint32_t mn_stride
 constexpr int TRN_SLOTS = 4;
 constexpr int TRN_THREADS = 128 * TRN_SLOTS;
 
+// 16-byte global -> shared copies that complete asynchronously (L2 only):
+// the next row's tiles load while the current row's MMAs run
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"((uint32_t)__cvta_generic_to_shared(dst)),
+               "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
 __host__ __device__ constexpr int tmem_cols_for(int n) { return n <= 32 ? 32 : (n <= 64 ? 64 : (n <= 128 ? 128 : (n <= 256 ? 256 : 512))); }
 
 template <int CIN, int COUT>
 __host__ __device__ constexpr int trn_conv_wbytes() { return 5 * COUT * CIN * 2; }
 template <int CIN, int COUT>
 __host__ __device__ constexpr int trn_conv_smem() {
-  return trn_conv_wbytes<CIN, COUT>() + TRN_SLOTS * (CIN / 8) * TC_LBO_ACT + 8 * TRN_SLOTS + 16;
+  return trn_conv_wbytes<CIN, COUT>() + 2 * TRN_SLOTS * (CIN / 8) * TC_LBO_ACT + 8 * TRN_SLOTS + 16;
 }
 
 // MODE 0: out = relu(conv + b) (bf16); MODE 1: out[p] = conv + b, channel 0
@@ -1119,11 +1129,12 @@ __global__ void __launch_bounds__(TRN_THREADS, 1)
   constexpr int WTAP = COUT * CIN * 2;
   constexpr int W_BYTES = trn_conv_wbytes<CIN, COUT>();
   constexpr int TILE = (CIN / 8) * TC_LBO_ACT;
+  constexpr int TILES = 2 * TRN_SLOTS;  // two per slot: the current row's and the next one's
   constexpr int TMEM_COLS = tmem_cols_for(TRN_SLOTS * COUT);
   extern __shared__ __align__(128) unsigned char smem[];
   const uint32_t s_base = (uint32_t)__cvta_generic_to_shared(smem);
-  const uint32_t bar0 = s_base + W_BYTES + TRN_SLOTS * TILE;
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + W_BYTES + TRN_SLOTS * TILE + 8 * TRN_SLOTS);
+  const uint32_t bar0 = s_base + W_BYTES + TILES * TILE;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + W_BYTES + TILES * TILE + 8 * TRN_SLOTS);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
@@ -1144,8 +1155,8 @@ __global__ void __launch_bounds__(TRN_THREADS, 1)
                               : make_uint4(0u, 0u, 0u, 0u);
     *reinterpret_cast<uint4*>(smem + t * WTAP + tc_off(n, 8 * j, 16 * COUT)) = v;
   }
-  // halo rows (0, 1, 130, 131) of every slot's tile stay zero
-  for (int i = threadIdx.x; i < TRN_SLOTS * 4 * (CIN / 8); i += TRN_THREADS) {
+  // halo rows (0, 1, 130, 131) of every tile stay zero
+  for (int i = threadIdx.x; i < TILES * 4 * (CIN / 8); i += TRN_THREADS) {
     const int j = i % (CIN / 8), hr = (i / (CIN / 8)) % 4, sl = i / (4 * (CIN / 8));
     const int hrow = hr < 2 ? hr : CROWS - 4 + hr;
     *reinterpret_cast<uint4*>(smem + W_BYTES + sl * TILE + tc_off(hrow, 8 * j, TC_LBO_ACT)) =
@@ -1159,28 +1170,37 @@ __global__ void __launch_bounds__(TRN_THREADS, 1)
   const int slot = warp >> 2, quarter = warp & 3;
   const int p = 32 * quarter + lane;
   const bool issuer = (p == 0);
-  unsigned char* tile = smem + W_BYTES + slot * TILE;
-  const uint32_t tile_s = s_base + W_BYTES + slot * TILE;
   const uint32_t td = tmem + COUT * slot, lane_base = (uint32_t)(quarter * 32) << 16;
   const uint32_t bar = bar0 + 8 * slot;
   uint32_t phase = 0;
   int commits = 0;
   bool ok = true;
-  for (int row = blockIdx.x * TRN_SLOTS + slot; row < rows; row += gridDim.x * TRN_SLOTS) {
-    const size_t q = (size_t)row * CP + p;
-    const uint4* src = reinterpret_cast<const uint4*>(x + q * CIN);
+  // this thread's position of a row into row p + 2 of tile b, asynchronously
+  auto fetch = [&](int row, int b) {
+    const uint4* src = reinterpret_cast<const uint4*>(x + ((size_t)row * CP + p) * CIN);
+    unsigned char* tile = smem + W_BYTES + (2 * slot + b) * TILE;
 #pragma unroll
-    for (int j = 0; j < CIN / 8; ++j)
-      *reinterpret_cast<uint4*>(tile + tc_off(p + CHALO, 8 * j, TC_LBO_ACT)) = src[j];
+    for (int j = 0; j < CIN / 8; ++j) cp_async16(tile + tc_off(p + CHALO, 8 * j, TC_LBO_ACT), src + j);
+    cp_async_commit();
+  };
+  const int stride = gridDim.x * TRN_SLOTS;
+  int b = 0;
+  if (blockIdx.x * TRN_SLOTS + slot < rows) fetch(blockIdx.x * TRN_SLOTS + slot, 0);
+  for (int row = blockIdx.x * TRN_SLOTS + slot; row < rows; row += stride, b ^= 1) {
+    const size_t q = (size_t)row * CP + p;
+    cp_async_wait_all();
     fence_async_smem();
     tc_fence_before();
     slot_sync(slot);
     if (issuer) {
       tc_fence_after();
-      tc_layer_issue<CIN, COUT>(td, tile_s, s_base);
+      tc_layer_issue<CIN, COUT>(td, s_base + W_BYTES + (2 * slot + b) * TILE, s_base);
       tc_commit(bar);
     }
     ++commits;
+    // the next row into the other tile (its last reader, the previous row's
+    // MMAs, completed before that row's epilogue)
+    if (row + stride < rows) fetch(row + stride, b ^ 1);
     const bool done = mbar_wait(bar, phase);
     phase ^= 1u;
     if (slot_any(slot, !done)) {
@@ -1225,6 +1245,7 @@ __global__ void __launch_bounds__(TRN_THREADS, 1)
     tc_fence_before();
     slot_sync(slot);
   }
+  cp_async_wait_all();  // no copy may land after the CTA is gone
   if (!ok) {
     if (p == 0) atomicOr(err, 1);
     // no MMA of this slot may still write TMEM when it is freed
@@ -1302,35 +1323,30 @@ __global__ void __launch_bounds__(128, 1)
   bool pending[2] = {false, false};
   bool ok = true;
   int n = 0;
-  for (int row = r_begin; row < r_end; ++row, ++n) {
-    const int st = n & 1;
+  // row `row`'s input copies and dy into stage st, asynchronously (copy c
+  // holds x[r + c - 2] at row r)
+  auto fetch = [&](int row, int st) {
     unsigned char* A = smem + st * STAGE;
     unsigned char* B = A + S::A_BYTES;
-    if (pending[st]) {  // the MMAs of two rows ago read this stage
-      const bool done = mbar_wait(bar0 + 8 * st, phase[st]);
-      phase[st] ^= 1u;
-      pending[st] = false;
-      if (__syncthreads_or(!done)) {
-        ok = false;
-        break;
-      }
-      tc_fence_after();
-    }
     const size_t q = (size_t)row * CP + p;
     const uint4* xs = reinterpret_cast<const uint4*>(x + q * CIN);
     const uint4* ys = reinterpret_cast<const uint4*>(dy + q * COUTP);
 #pragma unroll
-    for (int j = 0; j < CIN / 8; ++j) {
-      const uint4 v = xs[j];
-      // copy c holds x[r + c - 2] at row r
+    for (int j = 0; j < CIN / 8; ++j)
 #pragma unroll
       for (int c = 0; c < S::NCOPY; ++c) {
         const int r = p + CHALO - c;
-        if (r >= 0 && r < S::R) *reinterpret_cast<uint4*>(A + (c * (CIN / 8) + j) * MN_A + r * 16) = v;
+        if (r >= 0 && r < S::R) cp_async16(A + (c * (CIN / 8) + j) * MN_A + r * 16, xs + j);
       }
-    }
 #pragma unroll
-    for (int j = 0; j < COUTP / 8; ++j) *reinterpret_cast<uint4*>(B + j * MN_B + p * 16) = ys[j];
+    for (int j = 0; j < COUTP / 8; ++j) cp_async16(B + j * MN_B + p * 16, ys + j);
+    cp_async_commit();
+  };
+  if (r_begin < r_end) fetch(r_begin, 0);
+  for (int row = r_begin; row < r_end; ++row, ++n) {
+    const int st = n & 1;
+    unsigned char* B = smem + st * STAGE + S::A_BYTES;
+    cp_async_wait_all();
     fence_async_smem();
     tc_fence_before();
     __syncthreads();
@@ -1349,6 +1365,20 @@ __global__ void __launch_bounds__(128, 1)
       tc_commit(bar0 + 8 * st);
     }
     pending[st] = true;
+    // the next row into the other stage, once the MMAs that read it are done
+    if (row + 1 < r_end) {
+      const int so = st ^ 1;
+      if (pending[so]) {
+        const bool done = mbar_wait(bar0 + 8 * so, phase[so]);
+        phase[so] ^= 1u;
+        pending[so] = false;
+        if (__syncthreads_or(!done)) {
+          ok = false;
+          break;
+        }
+      }
+      fetch(row + 1, so);
+    }
     // bias gradient: column sums of dy over the row's positions
     if (threadIdx.x < COUTP) {
       const int o = threadIdx.x;
@@ -1358,6 +1388,7 @@ __global__ void __launch_bounds__(128, 1)
       bsum += rs;
     }
   }
+  cp_async_wait_all();
   // the outstanding commits of both stages
   for (int st = 0; st < 2; ++st)
     if (pending[st]) {

@@ -40,6 +40,12 @@ enum {
   VG_ERR_STATE = 6         /* call out of order (e.g. history too small) */
 };
 
+/* status bits a plan, batch or sweep raises on the device (vg_*_status) */
+enum {
+  VG_FLAG_TIMEOUT = 1,    /* a bounded wait of a kernel ran out: its step is not valid */
+  VG_FLAG_NONFINITE = 2   /* a field solve produced NaN or Inf: that step and the later ones are not valid */
+};
+
 enum { VG_F64 = 0, VG_F32_DELTA_F = 1 };
 /* all_params["fokker-planck"]["type"], vlapy/core/collisions.py:292-317 */
 enum { VG_COLL_NONE = 0, VG_COLL_LB = 1, VG_COLL_DG = 2 };
@@ -103,6 +109,12 @@ typedef struct vg_prof_entry {
  * Replaces the closure factories of vlapy/core/step.py:29-113. */
 int vg_plan_create(const vg_run_desc* desc, vg_plan** out);
 int vg_plan_destroy(vg_plan* plan);
+/* Synchronises the device.  *flags: the status bits the plan's kernels raised
+ * since it was created (VG_FLAG_NONFINITE: a field solve of vg_run_steps or
+ * vg_field_solve wrote NaN or Inf, for instance from a non-finite f).
+ * Returns VG_ERR_NUMERIC when that bit is set.  No reference counterpart:
+ * NumPy would carry the NaN on without a word. */
+int vg_plan_status(vg_plan* plan, int32_t* flags);
 const char* vg_last_error(void);
 int vg_version(void);
 
@@ -206,6 +218,8 @@ int vg_field_solve_noalloc(const double* f, int32_t nx, int32_t nv, double dv, c
 typedef struct vg_batch vg_batch;
 int vg_batch_create(const vg_run_desc* runs, int32_t n_runs, vg_batch** out);
 int vg_batch_destroy(vg_batch* batch);
+/* as vg_plan_status, for the batch's field solves */
+int vg_batch_status(vg_batch* batch, int32_t* flags);
 /* total cells and x points (the e-history row length) */
 int vg_batch_sizes(const vg_batch* batch, int64_t* cells, int64_t* x_points);
 /* nsteps steps of every run, in place.  f: DEVICE float64, the runs' f[nx][nv]
@@ -294,9 +308,21 @@ int vg_sweep_damping(vg_sweep* sweep, const double* e_hist, int32_t rows, double
  * loads its tiles through the tensor-memory accelerator (cp.async.bulk.tensor;
  * every run must start on a whole row of nv floats, and the environment
  * variable VG_SWEEP_NO_TMA, read at vg_sweep_create, must be unset or "0"), and
- * *flags the bounded-wait events of that kernel since creation; VG_ERR_TIMEOUT
- * if there were any (the affected steps are not valid). */
+ * *flags the status bits since creation: VG_FLAG_TIMEOUT for a bounded wait of
+ * that kernel that ran out, VG_FLAG_NONFINITE for a field solve that wrote NaN
+ * or Inf.  Returns VG_ERR_TIMEOUT, else VG_ERR_NUMERIC, if either is set (the
+ * affected steps are not valid). */
 int vg_sweep_status(vg_sweep* sweep, int32_t* flags, int32_t* uses_tma);
+/* Limit of the TMA x-drift's waits for its tiles, in ns of the global timer
+ * (default 2e9).  A wait that runs out sets VG_FLAG_TIMEOUT, lets the copy in
+ * flight land (waiting up to the default limit) and ends its CTA, so the step
+ * is not valid. */
+int vg_sweep_set_wait_limit(vg_sweep* sweep, int64_t ns);
+/* Test hook for those waits: while on, the TMA x-drift requests no tiles, so
+ * each of its waits runs out after the wait limit, raises VG_FLAG_TIMEOUT and
+ * ends its CTA (with no copy in flight to wait for).  The steps are not valid;
+ * nothing faults or hangs, and the context stays usable. */
+int vg_sweep_inject_lost_tiles(vg_sweep* sweep, int32_t on);
 /* per-kernel timing of vg_sweep_run_steps (same contract as vg_profile_*) */
 int vg_sweep_profile_enable(vg_sweep* sweep, int32_t enable);
 int vg_sweep_profile_read(vg_sweep* sweep, vg_prof_entry* out, int32_t max, int32_t* n_out);

@@ -116,6 +116,10 @@ EXPORTS = {
                                    C.c_void_p, C.c_void_p, C.c_void_p]),
     "vg_sweep_status": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "vg_sweep_set_step_events": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.c_int32]),
+    "vg_sweep_set_wait_limit": (C.c_int, [C.c_void_p, C.c_int64]),
+    "vg_sweep_inject_lost_tiles": (C.c_int, [C.c_void_p, C.c_int32]),
+    "vg_plan_status": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
+    "vg_batch_status": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "vg_sweep_profile_enable": (C.c_int, [C.c_void_p, C.c_int32]),
     "vg_sweep_profile_read": (C.c_int, [C.c_void_p, C.POINTER(VgProfEntry), C.c_int32, C.POINTER(C.c_int32)]),
     "vg_profile_enable": (C.c_int, [C.c_void_p, C.c_int32]),

@@ -156,6 +156,14 @@ class Batch64:
         """series [rows][7] of input run i."""
         return series_hist[:, int(self.slot[i])]
 
+    def status(self):
+        """Status bits the batch's kernels raised since it was created
+        (synchronises the device); a VlagpuError with VG_ERR_NUMERIC when a
+        field solve produced NaN or Inf."""
+        flags = C.c_int32()
+        check(self._lib.vg_batch_status(self._h, C.byref(flags)), "batch status")
+        return int(flags.value)
+
     def profile(self, enable):
         check(self._lib.vg_batch_profile_enable(self._h, int(bool(enable))), "profile")
 

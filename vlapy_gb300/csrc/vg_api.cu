@@ -162,7 +162,7 @@ int dev_copy(T** dst, const T* src, size_t n, const char* what) {
 void free_plan(vg_plan* p) {
   if (!p) return;
   void* ptrs[] = {p->x, p->v, p->kx, p->kv, p->inv_kx, p->v_pow, p->f_bg, p->pulses, p->tw64, p->tw32,
-                  p->pw_v, p->pw_x, p->dens, p->mom, p->bb, p->rho, p->etmp, p->sl_m, p->sl_w};
+                  p->pw_v, p->pw_x, p->dens, p->mom, p->bb, p->rho, p->etmp, p->sl_m, p->sl_w, p->flags};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   if (p->graph_cache) {
@@ -626,6 +626,7 @@ int vg_plan_create(const vg_run_desc* d, vg_plan** out) {
   TRY(dev_copy<double>(&p->mom, nullptr, nx * MOM_STRIDE, "scratch"));
   TRY(dev_copy<double>(&p->rho, nullptr, nx, "scratch"));
   TRY(dev_copy<double>(&p->etmp, nullptr, 4 * nx + 4, "scratch"));
+  TRY(dev_copy<int>(&p->flags, nullptr, 1, "status"));
   if (d->precision == VG_F64 && d->collision != VG_COLL_NONE)
     TRY(dev_copy<double>(&p->bb, nullptr, 2 * nx * nv, "thomas scratch"));
   if (d->precision == VG_F32_DELTA_F) TRY(setup_f32(p, d));
@@ -642,6 +643,22 @@ int vg_plan_destroy(vg_plan* p) {
   if (!p) return VG_OK;
   cudaDeviceSynchronize();
   free_plan(p);
+  return VG_OK;
+}
+
+int vg_plan_status(vg_plan* p, int32_t* flags) {
+  VG_CHECK(require_plan(p));
+  if (!flags) {
+    set_error("null flags");
+    return VG_ERR_ARG;
+  }
+  int h = 0;
+  VG_CHECK(cuda_status(cudaMemcpy(&h, p->flags, sizeof(int), cudaMemcpyDeviceToHost), "plan status"));
+  *flags = h;
+  if (h & VG_FLAG_NONFINITE) {
+    set_error("a field solve produced NaN or Inf (the steps from it on are not valid)");
+    return VG_ERR_NUMERIC;
+  }
   return VG_OK;
 }
 

@@ -56,7 +56,8 @@ __global__ void __launch_bounds__(col_seqs<double>(NX) * fft_threads<double>(NX)
 template <int NX>
 __global__ void __launch_bounds__(fft_threads<double>(NX))
     k_batch_poisson(const BatchRunDev* __restrict__ runs, const int* __restrict__ ids,
-                    const double* __restrict__ dens, const cx<double>* __restrict__ tw, double* e) {
+                    const double* __restrict__ dens, const cx<double>* __restrict__ tw, double* e,
+                    int* flags) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const BatchRunDev r = runs[ids[blockIdx.x]];
   FieldTimeDev ft;
@@ -64,7 +65,7 @@ __global__ void __launch_bounds__(fft_threads<double>(NX))
   ft.t_host = 0.0;
   ft.nadd = 0;
   poisson_fft_body<NX>(dens + r.x_off, 1, r.inv_kx, nullptr, 0, nullptr, 0, nullptr, ft, tw, e + r.x_off,
-                       reinterpret_cast<cx<double>*>(smem_raw), threadIdx.x);
+                       reinterpret_cast<cx<double>*>(smem_raw), threadIdx.x, flags);
 }
 
 // tridiagonal collision solve, one thread per row of a class; rows of
@@ -137,6 +138,7 @@ struct vg_batch {
   double* fpmom = nullptr;     // [x_points][2]
   double* nudt_row = nullptr;  // [x_points]
   double* bb = nullptr;        // [max class rows][2][nv]
+  int* flags = nullptr;        // status bits raised on the device (VG_FLAG_*)
   int max_pw_x_leaves = 0;
   // nv classes: a contiguous block of runs each
   struct Cls {
@@ -234,7 +236,7 @@ cudaError_t batch_poisson_launch(const vg_batch* b, const vg_batch::XCls& xc, do
   const size_t smem = (size_t)sp_len<double>(NX) * sizeof(cx<double>);
   cudaError_t err = ensure_smem((const void*)k_batch_poisson<NX>, smem);
   if (err != cudaSuccess) return err;
-  k_batch_poisson<NX><<<xc.n_ids, G, smem, s>>>(b->runs, xc.ids, b->dens, b->tw64, e);
+  k_batch_poisson<NX><<<xc.n_ids, G, smem, s>>>(b->runs, xc.ids, b->dens, b->tw64, e, b->flags);
   return cudaGetLastError();
 }
 
@@ -488,6 +490,7 @@ int vg_batch_create(const vg_run_desc* runs, int32_t n_runs, vg_batch** out) {
   B_TRY(b_alloc(b, &b->runs, rd.size(), rd.data(), "batch runs"));
   B_TRY(b_alloc(b, &b->nudt_row, nudt_row.size(), nudt_row.data(), "batch runs"));
   B_TRY(b_alloc<double>(b, &b->dens, (size_t)xoff, nullptr, "batch scratch"));
+  B_TRY(b_alloc<int>(b, &b->flags, 1, nullptr, "batch status"));
   B_TRY(b_alloc<double>(b, &b->mom, (size_t)xoff * BATCH_MOMS, nullptr, "batch scratch"));
   B_TRY(b_alloc<double>(b, &b->fpmom, (size_t)xoff * 2, nullptr, "batch scratch"));
   B_TRY(b_alloc<double>(b, &b->bb, bb_need, nullptr, "batch thomas scratch"));
@@ -529,6 +532,21 @@ int vg_batch_destroy(vg_batch* b) {
   if (!b) return VG_OK;
   cudaDeviceSynchronize();
   free_batch(b);
+  return VG_OK;
+}
+
+int vg_batch_status(vg_batch* b, int32_t* flags) {
+  if (!b || !flags) {
+    set_error("null batch or flags");
+    return VG_ERR_ARG;
+  }
+  int h = 0;
+  B_CHECK(cuda_status(cudaMemcpy(&h, b->flags, sizeof(int), cudaMemcpyDeviceToHost), "batch status"));
+  *flags = h;
+  if (h & VG_FLAG_NONFINITE) {
+    set_error("a field solve produced NaN or Inf (the steps from it on are not valid)");
+    return VG_ERR_NUMERIC;
+  }
   return VG_OK;
 }
 

@@ -137,7 +137,7 @@ __device__ __forceinline__ void poisson_fft_body(const double* __restrict__ dens
                                                  const vg_pulse* __restrict__ P, int np,
                                                  const double* __restrict__ x, const FieldTimeDev& ft,
                                                  const cx<double>* __restrict__ tw, double* __restrict__ e,
-                                                 cx<double>* s, int t) {
+                                                 cx<double>* s, int t, int* flags) {
   constexpr int R = fft_radix<double>(NX);
   constexpr int G = NX / R;
   for (int n = t; n < NX; n += G) s[sp<double>(n)] = {is_density ? sub_rn(1.0, dens[n]) : dens[n], 0.0};
@@ -155,7 +155,9 @@ __device__ __forceinline__ void poisson_fft_body(const double* __restrict__ dens
   const double sc = 1.0 / NX;
   for (int n = t; n < NX; n += G) {
     const double self = s[sp<double>(n)].x * sc;
-    e[n] = add_rn(driver_value(driver, use_pulses, P, np, tt, x, n), self);
+    const double en = add_rn(driver_value(driver, use_pulses, P, np, tt, x, n), self);
+    e[n] = en;
+    if (flags && !isfinite(en)) atomicOr(flags, VG_FLAG_NONFINITE);
   }
 }
 

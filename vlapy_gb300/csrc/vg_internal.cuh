@@ -34,6 +34,7 @@ struct vg_plan {
   double* bb;     // [nx][2][nv] Thomas elimination scratch (pivots, upper diagonal; FP64 mode)
   double* rho;    // [nx]
   double* etmp;   // [nx]
+  int* flags;     // status bits raised on the device (VG_FLAG_*; null: none kept)
   // semi-Lagrangian steps (allocated by their first call): spline second
   // derivatives [(nx + 2) * (nv + 2)] and the Thomas pivot table [max(nx, nv)]
   double* sl_m;

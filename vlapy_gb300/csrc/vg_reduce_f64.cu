@@ -144,10 +144,10 @@ __global__ void __launch_bounds__(fft_threads<double>(NX)) k_poisson_fft_f64(
     const double* __restrict__ dens, int is_density, const double* __restrict__ inv_kx,
     const double* __restrict__ driver, int use_pulses, const vg_pulse* __restrict__ P, int np,
     const double* __restrict__ x, FieldTimeDev ft, const cx<double>* __restrict__ tw,
-    double* __restrict__ e) {
+    double* __restrict__ e, int* flags) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   poisson_fft_body<NX>(dens, is_density, inv_kx, driver, use_pulses, P, np, x, ft, tw, e,
-                       reinterpret_cast<cx<double>*>(smem_raw), threadIdx.x);
+                       reinterpret_cast<cx<double>*>(smem_raw), threadIdx.x, flags);
 }
 
 // Direct DFT for lengths that are not powers of two (O(nx^2), one CTA).
@@ -155,7 +155,7 @@ __global__ void k_poisson_dft_f64(const double* __restrict__ dens, int is_densit
                                   const double* __restrict__ inv_kx, const double* __restrict__ driver,
                                   int use_pulses, const vg_pulse* __restrict__ P, int np,
                                   const double* __restrict__ x, FieldTimeDev ft,
-                                  double* __restrict__ work, double* __restrict__ e) {
+                                  double* __restrict__ work, double* __restrict__ e, int* flags) {
   // work: [nx] rho, then [2*nx] spectrum
   double* rho = work;
   cx<double>* Y = reinterpret_cast<cx<double>*>(work + nx + (nx & 1));
@@ -183,7 +183,9 @@ __global__ void k_poisson_dft_f64(const double* __restrict__ dens, int is_densit
       sincospi(2.0 * (double)q / (double)nx, &sn, &cs);
       acc += Y[k].x * cs - Y[k].y * sn;
     }
-    e[n] = driver_value(driver, use_pulses, P, np, tt, x, n) + acc / nx;
+    const double en = driver_value(driver, use_pulses, P, np, tt, x, n) + acc / nx;
+    e[n] = en;
+    if (flags && !isfinite(en)) atomicOr(flags, VG_FLAG_NONFINITE);
   }
 }
 
@@ -196,7 +198,7 @@ cudaError_t poisson_n(const vg_plan& p, const double* dens, int is_density, cons
   cudaError_t err = ensure_smem((const void*)k_poisson_fft_f64<NX>, smem);
   if (err != cudaSuccess) return err;
   k_poisson_fft_f64<NX><<<1, G, smem, s>>>(dens, is_density, p.inv_kx, driver, ft.use_pulses, p.pulses,
-                                           p.n_pulses, p.x, to_dev(ft), p.tw64, e);
+                                           p.n_pulses, p.x, to_dev(ft), p.tw64, e, p.flags);
   return cudaGetLastError();
 }
 }  // namespace
@@ -222,7 +224,7 @@ cudaError_t launch_poisson_f64(const vg_plan& p, const double* dens, int is_dens
     }
   }
   k_poisson_dft_f64<<<1, 256, 0, s>>>(dens, is_density, p.nx, p.inv_kx, driver, ft.use_pulses, p.pulses,
-                                      p.n_pulses, p.x, to_dev(ft), p.etmp, e);
+                                      p.n_pulses, p.x, to_dev(ft), p.etmp, e, p.flags);
   return cudaGetLastError();
 }
 

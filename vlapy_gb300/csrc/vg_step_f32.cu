@@ -79,7 +79,7 @@ __global__ void __launch_bounds__(fft_threads<float>(NX)) k_field_f32(
     const double* __restrict__ rho, const double* __restrict__ inv_kx, const double* __restrict__ driver,
     int use_pulses, const vg_pulse* __restrict__ P, int np, const double* __restrict__ x, const double* t_ptr,
     double t_host, int nadd, double a0, double a1, double a2, double a3, double a4,
-    const cx<float>* __restrict__ tw, double* __restrict__ e, float* __restrict__ e32) {
+    const cx<float>* __restrict__ tw, double* __restrict__ e, float* __restrict__ e32, int* flags) {
   constexpr int G = fft_threads<float>(NX);
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cx<float>* s = reinterpret_cast<cx<float>*>(smem_raw);
@@ -105,6 +105,7 @@ __global__ void __launch_bounds__(fft_threads<float>(NX)) k_field_f32(
     const float en = drv + s[sp<float>(n)].x;
     e[n] = (double)en;
     e32[n] = en;
+    if (flags && !isfinite(en)) atomicOr(flags, VG_FLAG_NONFINITE);
   }
 }
 
@@ -266,7 +267,7 @@ cudaError_t field_n(const vg_plan& p, const double* driver, const FieldTime& ft,
   if (err != cudaSuccess) return err;
   k_field_f32<NX><<<1, G, smem, s>>>(p.rho, p.inv_kx, driver, ft.use_pulses, p.pulses, p.n_pulses, p.x, ft.t_ptr,
                                      ft.t_host, ft.nadd, ft.add[0], ft.add[1], ft.add[2], ft.add[3], ft.add[4],
-                                     p.tw32, e, p.f32->e32);
+                                     p.tw32, e, p.f32->e32, p.flags);
   return cudaGetLastError();
 }
 

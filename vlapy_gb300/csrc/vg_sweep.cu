@@ -309,7 +309,7 @@ template <int NX>
 __global__ void __launch_bounds__(SWEEP_BLOCK, sweep_col_radix(NX) == 16 ? VG_COL_MIN_BLOCKS_R16 : VG_COL_MIN_BLOCKS) k_sweep_col_tma(
     const SweepRunDev* __restrict__ runs, const int2* __restrict__ items, int n_items, float* g,
     const SweepConsts* __restrict__ scp, const cx<float>* __restrict__ tw, float2* dpart,
-    const __grid_constant__ SweepTmaps maps, int* err) {
+    const __grid_constant__ SweepTmaps maps, int* err, unsigned long long wait_ns, int no_loads) {
   constexpr int W = sweep_col_w(NX);
   constexpr uint32_t TILE = (uint32_t)sweep_col_tile_bytes<NX>();
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -337,15 +337,17 @@ __global__ void __launch_bounds__(SWEEP_BLOCK, sweep_col_radix(NX) == 16 ? VG_CO
         : "memory");
   };
   const int stride = gridDim.x;
-  if (threadIdx.x == 0 && (int)blockIdx.x < n_items) issue(blockIdx.x);
+  // (no_loads: a test hook, no tile is ever requested, so every wait runs out)
+  if (threadIdx.x == 0 && (int)blockIdx.x < n_items && !no_loads) issue(blockIdx.x);
   uint32_t parity = 0;
   for (int idx = blockIdx.x; idx < n_items; idx += stride, parity ^= 1u) {
-    const bool ok = mbar_wait_bounded(bar, parity, TMA_WAIT_NS);
+    const bool ok = mbar_wait_bounded(bar, parity, wait_ns);
     if (__syncthreads_or(!ok)) {
-      // the stage never filled: record it, let the copy in flight land, stop
+      // the stage did not fill in time: record it, let the copy in flight
+      // land (waiting up to the default limit), stop
       if (threadIdx.x == 0) {
-        atomicOr(err, 1);
-        mbar_wait_bounded(bar, parity, TMA_WAIT_NS);
+        atomicOr(err, VG_FLAG_TIMEOUT);
+        if (!no_loads) mbar_wait_bounded(bar, parity, TMA_WAIT_NS);
       }
       __syncthreads();
       return;
@@ -361,7 +363,7 @@ __global__ void __launch_bounds__(SWEEP_BLOCK, sweep_col_radix(NX) == 16 ? VG_CO
       }
       // every thread has its elements: the stage is free for the next item
       __syncthreads();
-      if (threadIdx.x == 0 && idx + stride < n_items) issue(idx + stride);
+      if (threadIdx.x == 0 && idx + stride < n_items && !no_loads) issue(idx + stride);
     });
   }
 }
@@ -371,7 +373,7 @@ template <int NX>
 __device__ __forceinline__ void sweep_field_runs(const SweepRunDev* __restrict__ runs, int first, int count,
                                                  const SweepConsts& sc, const float2* __restrict__ dpart,
                                                  const cx<float>* __restrict__ tw, double* __restrict__ e,
-                                                 float* __restrict__ e32, unsigned char* smem) {
+                                                 float* __restrict__ e32, unsigned char* smem, int* flags) {
   constexpr int G = fft_threads<float>(NX);
   const int grp = threadIdx.x / G, t = threadIdx.x - grp * G;
   cx<float>* s = reinterpret_cast<cx<float>*>(smem) + (size_t)grp * sp_len<float>(NX);
@@ -404,6 +406,7 @@ __device__ __forceinline__ void sweep_field_runs(const SweepRunDev* __restrict__
       const float ex = s[sp<float>(x)].x;
       e[r.x_off + x] = (double)ex;
       e32[r.x_off + x] = ex;
+      if (!isfinite(ex)) atomicOr(flags, VG_FLAG_NONFINITE);
     }
 }
 
@@ -412,17 +415,18 @@ __global__ void __launch_bounds__(SWEEP_FIELD_BLOCK) k_sweep_field(const SweepRu
                                                                    const SweepConsts* __restrict__ scp,
                                                                    const float2* __restrict__ dpart,
                                                                    const cx<float>* __restrict__ tw,
-                                                                   double* __restrict__ e, float* __restrict__ e32) {
+                                                                   double* __restrict__ e, float* __restrict__ e32,
+                                                                   int* flags) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int4 it = items[blockIdx.x];  // (nx, first run, count, -)
   const SweepConsts& sc = *scp;
   switch (it.x) {
-    case 8: sweep_field_runs<8>(runs, it.y, it.z, sc, dpart, tw, e, e32, smem_raw); break;
-    case 16: sweep_field_runs<16>(runs, it.y, it.z, sc, dpart, tw, e, e32, smem_raw); break;
-    case 32: sweep_field_runs<32>(runs, it.y, it.z, sc, dpart, tw, e, e32, smem_raw); break;
-    case 64: sweep_field_runs<64>(runs, it.y, it.z, sc, dpart, tw, e, e32, smem_raw); break;
-    case 128: sweep_field_runs<128>(runs, it.y, it.z, sc, dpart, tw, e, e32, smem_raw); break;
-    default: sweep_field_runs<256>(runs, it.y, it.z, sc, dpart, tw, e, e32, smem_raw); break;
+    case 8: sweep_field_runs<8>(runs, it.y, it.z, sc, dpart, tw, e, e32, smem_raw, flags); break;
+    case 16: sweep_field_runs<16>(runs, it.y, it.z, sc, dpart, tw, e, e32, smem_raw, flags); break;
+    case 32: sweep_field_runs<32>(runs, it.y, it.z, sc, dpart, tw, e, e32, smem_raw, flags); break;
+    case 64: sweep_field_runs<64>(runs, it.y, it.z, sc, dpart, tw, e, e32, smem_raw, flags); break;
+    case 128: sweep_field_runs<128>(runs, it.y, it.z, sc, dpart, tw, e, e32, smem_raw, flags); break;
+    default: sweep_field_runs<256>(runs, it.y, it.z, sc, dpart, tw, e, e32, smem_raw, flags); break;
   }
 }
 
@@ -693,7 +697,9 @@ struct vg_sweep {
   bool use_tma = false;           // some x class loads its tiles through the TMA
   std::vector<char> tma_x;        // per x class (col_nx order): this class does
   std::vector<SweepTmaps> tmaps;  // per x class, one map per nv class
-  int* err = nullptr;             // bounded-wait events of the TMA x-drift
+  int* err = nullptr;             // status bits (VG_FLAG_*): TMA waits that ran out, non-finite fields
+  unsigned long long wait_ns = 2000000000ull;  // limit of the TMA x-drift's tile waits
+  int lost_tiles = 0;             // test hook: the TMA x-drift requests no tiles
   int n_sm = 0;
   // the size classes of a phase run side by side: side streams that branch
   // from the caller's stream and join it again, and the events that do it
@@ -854,7 +860,8 @@ cudaError_t sweep_col_launch(vg_sweep* s, int c, cudaStream_t st) {
     if (err != cudaSuccess) return err;
     const int grid = std::max(1, std::min(s->col_count[c], std::max(1, per_sm) * s->n_sm));
     k_sweep_col_tma<NX><<<grid, SWEEP_BLOCK, smem, st>>>(s->runs, s->col_items + s->col_first[c], s->col_count[c],
-                                                         s->g, s->consts, s->tw32, s->dpart, s->tmaps[c], s->err);
+                                                         s->g, s->consts, s->tw32, s->dpart, s->tmaps[c], s->err,
+                                                         s->wait_ns, s->lost_tiles);
     return cudaGetLastError();
   }
   const size_t smem = sweep_col_work_bytes<NX>();
@@ -988,7 +995,7 @@ int sweep_sequence(vg_sweep* s, int nsteps, double* e_hist, double* s_hist, int 
                          "sweep x drift"));
     SW_CHECK(cuda_status(prof_call(&s->prof, SK_FIELD, st, [&] {
                            k_sweep_field<<<s->n_field, SWEEP_FIELD_BLOCK, s->field_smem, st>>>(
-                               s->field_runs, s->field_items, s->consts, s->dpart, s->tw32, s->e, s->e32);
+                               s->field_runs, s->field_items, s->consts, s->dpart, s->tw32, s->e, s->e32, s->err);
                            return cudaGetLastError();
                          }),
                          "sweep field"));
@@ -1365,10 +1372,37 @@ int vg_sweep_status(vg_sweep* s, int32_t* flags, int32_t* uses_tma) {
   SW_CHECK(cuda_status(cudaMemcpy(&h, s->err, sizeof(int), cudaMemcpyDeviceToHost), "sweep status"));
   if (flags) *flags = h;
   if (uses_tma) *uses_tma = s->use_tma ? 1 : 0;
-  if (h) {
-    set_error("a bounded wait of the TMA x-drift ran out");
+  if (h & VG_FLAG_TIMEOUT) {
+    set_error("a bounded wait of the TMA x-drift ran out (the steps it ended are not valid)");
     return VG_ERR_TIMEOUT;
   }
+  if (h & VG_FLAG_NONFINITE) {
+    set_error("a field solve produced NaN or Inf (the steps from it on are not valid)");
+    return VG_ERR_NUMERIC;
+  }
+  return VG_OK;
+}
+
+int vg_sweep_set_wait_limit(vg_sweep* s, int64_t ns) {
+  if (!s || ns < 0) {
+    set_error("null sweep or negative wait limit");
+    return VG_ERR_ARG;
+  }
+  s->wait_ns = (unsigned long long)ns;
+  // graphs captured before hold the old limit as a kernel argument
+  for (auto& kv : s->graphs) cudaGraphExecDestroy(kv.second);
+  s->graphs.clear();
+  return VG_OK;
+}
+
+int vg_sweep_inject_lost_tiles(vg_sweep* s, int32_t on) {
+  if (!s) {
+    set_error("null sweep");
+    return VG_ERR_ARG;
+  }
+  s->lost_tiles = on ? 1 : 0;
+  for (auto& kv : s->graphs) cudaGraphExecDestroy(kv.second);
+  s->graphs.clear();
   return VG_OK;
 }
 

@@ -184,6 +184,14 @@ class Plan:
         check(self._lib.vg_storage_step(self._h, ptr(f), ptr(e), ptr(de), C.byref(hist), int(i),
                                         stream_handle(stream)), "storage step")
 
+    def status(self):
+        """Status bits the plan's kernels raised since it was created
+        (synchronises the device); a VlagpuError with VG_ERR_NUMERIC when a
+        field solve produced NaN or Inf."""
+        flags = C.c_int32()
+        check(self._lib.vg_plan_status(self._h, C.byref(flags)), "plan status")
+        return int(flags.value)
+
     def profile(self, enable: bool):
         check(self._lib.vg_profile_enable(self._h, int(bool(enable))), "profile")
 

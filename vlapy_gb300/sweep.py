@@ -177,13 +177,25 @@ class Sweep:
         return e_hist[:, o:o + self.runs[i]["nx"]]
 
     def status(self):
-        """(flags, uses_tma) after synchronising the device: the bounded-wait
-        events of the TMA x-drift since creation (a VlagpuError with
-        VG_ERR_TIMEOUT when there were any) and whether the x-drift loads its
-        tiles through the TMA."""
+        """(flags, uses_tma) after synchronising the device: the status bits
+        since creation (a VlagpuError with VG_ERR_TIMEOUT when a bounded wait
+        of the TMA x-drift ran out, else with VG_ERR_NUMERIC when a field solve
+        produced NaN or Inf) and whether the x-drift loads its tiles through
+        the TMA."""
         flags, tma = C.c_int32(), C.c_int32()
         check(self._lib.vg_sweep_status(self._h, C.byref(flags), C.byref(tma)), "sweep status")
         return int(flags.value), bool(tma.value)
+
+    def set_wait_limit(self, ns):
+        """Limit, in ns, of the TMA x-drift's waits for its tiles (default
+        2e9).  A wait that runs out marks the sweep's status and ends its CTA."""
+        check(self._lib.vg_sweep_set_wait_limit(self._h, int(ns)), "sweep wait limit")
+
+    def inject_lost_tiles(self, on=True):
+        """Test hook: while on, the TMA x-drift requests no tiles, so each of
+        its waits runs out after the wait limit (the steps are not valid; the
+        status reports the timeout)."""
+        check(self._lib.vg_sweep_inject_lost_tiles(self._h, int(bool(on))), "sweep inject")
 
     def set_step_events(self, events):
         """torch.cuda.Event objects that each following run_steps call records

@@ -426,3 +426,50 @@ def test_sweep_full_horizon_against_fp64():
     assert e2_err.max() <= 0.01, (int(e2_err.argmax()), runs[int(e2_err.argmax())])
     assert f_err.max() <= 0.02, (int(f_err.argmax()), runs[int(f_err.argmax())])
     judge.close()
+
+
+def test_sweep_full_workload_full_horizon():
+    """The benchmarked workload itself, all 4096 runs over their 2000 steps
+    (one graph replay): no bounded wait ran out and no field went non-finite,
+    every stored field is finite, every run's density is conserved, and one
+    run of each (nx, nv) class (collisional and collisionless where the class
+    has both) damps at the batched FP64 step's rate within 1 %."""
+    from vlapy_gb300.batch import Batch64
+    from vlapy_gb300.diagnostics import damping_fit, mode_amplitude
+    from vlapy_gb300.sweep import Sweep, sweep_config
+    runs = sweep_config(4096, 20261203)
+    nsteps = 2000
+    sw = Sweep(runs)
+    sw.reset()
+    eh, sh = sw.history(nsteps)
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        sw.run_steps(nsteps, eh, sh, use_graph=True, stream=s)
+    torch.cuda.synchronize()
+    assert sw.status() == (0, True)
+    assert torch.isfinite(eh).all() and torch.isfinite(sh[:, :, :4]).all()
+    n = sh[:, :, 0]
+    drift = float(((n - n[:1]).abs() / n[:1].abs()).max())
+    assert drift <= 1e-6, drift
+    # one collisional and one collisionless run of each shape class
+    picked, seen = [], set()
+    for i, r in enumerate(runs):
+        key = (r["nx"], r["nv"], r["nu"] == 0.0)
+        if key not in seen:
+            seen.add(key)
+            picked.append(i)
+    assert len(picked) >= 18
+    judge = Batch64([runs[i] for i in picked])
+    f64, e64 = judge.initial_state()
+    eh64, _ = judge.history(nsteps)
+    for c0 in range(0, nsteps, 500):
+        judge.run_steps(f64, e64, 500, eh64, None, row0=c0)
+    torch.cuda.synchronize()
+    t = 0.1 * np.arange(1, nsteps + 1)
+    for j, i in enumerate(picked):
+        rf, _ = damping_fit(t, mode_amplitude(judge.e_of(eh64, j).cpu().numpy()), t_min=5.0, t_max=60.0)
+        rg, _ = damping_fit(t, mode_amplitude(sw.e_of(eh, i).cpu().numpy()), t_min=5.0, t_max=60.0)
+        assert np.isfinite(rf) and abs(rg - rf) <= 0.01 * abs(rf), (i, runs[i], rg, rf)
+    judge.close()
+    sw.close()

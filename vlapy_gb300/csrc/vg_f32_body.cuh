@@ -329,8 +329,7 @@ __device__ __forceinline__ void row_pair(const RowArgs& a, int pair, unsigned ch
       if (vb) gbp[n] = io[i].y;
     }
     sync();
-    return;
-  }
+  } else {
   // both kicks run the same code (registers in, registers out), once each in
   // a loop the compiler keeps rolled, so the kernel holds one copy of the
   // kick's FFTs instead of four differently specialised ones (instruction-
@@ -473,6 +472,7 @@ __device__ __forceinline__ void row_pair(const RowArgs& a, int pair, unsigned ch
     }
   }
   sync();
+  }
 }
 
 

@@ -137,7 +137,7 @@ class ClockSampler:
 # dram__bytes_write.sum), measured by ncu on the three full row-pass launches
 # of the 4096-run sweep (one per nv class; 179,806,208 cells in all):
 # 256: 106.42 + 53.45 MB, 512: 210.23 + 159.97 MB, 1024: 405.17 + 348.15 MB.
-ROW_PASS_DRAM_BYTES_PER_CELL = (106422272 + 53419264 + 210238464 + 160070656 + 404893696 + 363490048) / 179806208
+ROW_PASS_DRAM_BYTES_PER_CELL = (106419968 + 53376768 + 210321664 + 154533632 + 404892416 + 364435712) / 179806208
 
 
 def peaks():

@@ -70,20 +70,24 @@ constexpr int SWEEP_ROW_BLOCK = VG_SWEEP_ROW_BLOCK;
 constexpr int SWEEP_FIELD_BLOCK = 128;
 constexpr int SWEEP_MAX_CLASSES = 6;  // nv in {64, ..., 2048}
 
-// FFT radix of the sweep's x-drift: radix 16 where it saves a pass (nx in
-// the build-time mask, bit log2 nx: 128 = 16 x 8 instead of 8 x 8 x 2)
+// FFT radix of the sweep's x-drift: radix 16 for the nx in the build-time
+// mask (bit log2 nx): nx = 128 (16 x 8 instead of 8 x 8 x 2) and nx = 64
+// (16 x 4: half the threads a column pair; the autotuner's choice on a
+// GB300, 1.755 against 1.787 ms per 4096-run step)
 #ifndef VG_SWEEP_COL_R16_MASK
-#define VG_SWEEP_COL_R16_MASK 0x80
+#define VG_SWEEP_COL_R16_MASK 0xC0
 #endif
 __host__ __device__ constexpr int sweep_col_radix(int nx) {
   return (nx >= 32 && nx <= 256 && ((VG_SWEEP_COL_R16_MASK >> ilog2(nx)) & 1)) ? 16 : col32_radix(nx);
 }
 __host__ __device__ constexpr int sweep_col_w(int nx) { return 2 * (SWEEP_BLOCK / (nx / sweep_col_radix(nx))); }
-// nv classes (bit log2 nv) on radix-32 passes (32 elements a thread, a row
-// pair per warp; build-time knob).  nv = 1024 (two passes instead of 16 x
-// 16 x 4): row pass 1.333 ms against 1.365 ms on radix 16
+// nv classes (bit log2 nv) on radix-32 passes (32 elements a thread; a row
+// pair per warp at nv = 1024, per half warp at 512; build-time knob).
+// nv = 1024 (two passes instead of 16 x 16 x 4): row pass 1.333 ms against
+// 1.365 ms on radix 16; nv = 512 as well (32 x 16): 1.787 against 1.818 ms
+// per 4096-run step, the autotuner's choice on a GB300
 #ifndef VG_SWEEP_R32_MASK
-#define VG_SWEEP_R32_MASK 0x400
+#define VG_SWEEP_R32_MASK 0x600
 #endif
 #ifndef VG_ROW_MIN_BLOCKS_R32
 #define VG_ROW_MIN_BLOCKS_R32 2

@@ -48,11 +48,11 @@ from . import build as B
 
 # (constant, candidate values); the starting value is taken from the tuning in use
 KNOBS = (
-    ("VG_SWEEP_R32_MASK", (0x600, 0x400, 0x0)),      # radix 32 for nv = 512 and 1024, for 1024 only, or none
+    ("VG_SWEEP_R32_MASK", (0x600, 0x400, 0x0, 0x700)),  # radix 32 for nv = 512 and 1024, 1024 only, none, or 256 up
     ("VG_SWEEP_R16_MASK", (0x700, 0x500, 0x300)),    # radix 16 for nv in {256, 512, 1024}, or a subset
     ("VG_ROW_MIN_BLOCKS_R16", (3, 2, 4)),            # row CTAs per SM of the radix-16 classes
     ("VG_SWEEP_ROW_BLOCK", (256, 128, 64)),          # threads of a row-kernel CTA
-    ("VG_SWEEP_COL_R16_MASK", (0xC0, 0x80, 0x0, 0xE0)),  # radix 16 for the x-drift of nx = 64 and 128, 128 only, none, or 32 up
+    ("VG_SWEEP_COL_R16_MASK", (0xE0, 0xC0, 0x80, 0x0)),  # radix 16 for the x-drift of nx = 32 up, 64 up, 128 only, or none
     ("VG_COL_MIN_BLOCKS_R16", (3, 2)),               # x-drift CTAs per SM of the radix-16 classes
 )
 

@@ -71,11 +71,11 @@ constexpr int SWEEP_FIELD_BLOCK = 128;
 constexpr int SWEEP_MAX_CLASSES = 6;  // nv in {64, ..., 2048}
 
 // FFT radix of the sweep's x-drift: radix 16 for the nx in the build-time
-// mask (bit log2 nx): nx = 128 (16 x 8 instead of 8 x 8 x 2) and nx = 64
-// (16 x 4: half the threads a column pair; the autotuner's choice on a
-// GB300, 1.755 against 1.787 ms per 4096-run step)
+// mask (bit log2 nx): nx = 128 (16 x 8 instead of 8 x 8 x 2), nx = 64 (16 x 4)
+// and nx = 32 (16 x 2): fewer threads a column pair, the autotuner's choice
+// on a GB300 (1.748 ms per 4096-run step, against 1.787 with nx = 128 alone)
 #ifndef VG_SWEEP_COL_R16_MASK
-#define VG_SWEEP_COL_R16_MASK 0xC0
+#define VG_SWEEP_COL_R16_MASK 0xE0
 #endif
 __host__ __device__ constexpr int sweep_col_radix(int nx) {
   return (nx >= 32 && nx <= 256 && ((VG_SWEEP_COL_R16_MASK >> ilog2(nx)) & 1)) ? 16 : col32_radix(nx);

@@ -54,6 +54,7 @@ KNOBS = (
     ("VG_SWEEP_ROW_BLOCK", (256, 128, 64)),          # threads of a row-kernel CTA
     ("VG_SWEEP_COL_R16_MASK", (0xE0, 0xC0, 0x80, 0x0)),  # radix 16 for the x-drift of nx = 32 up, 64 up, 128 only, or none
     ("VG_COL_MIN_BLOCKS_R16", (3, 2)),               # x-drift CTAs per SM of the radix-16 classes
+    ("VG_SWEEP_COL_R32_MASK", (0x0, 0x80, 0xC0)),    # radix 32 for the x-drift: none, nx = 128, or nx = 64 and 128
 )
 
 MATCH_TOL = 1e-4  # relative L2 of the stored fields against the starting build

@@ -35,7 +35,7 @@ TUNING_FILE = os.path.join(HERE, "tuning.json")
 # the build-time constants a tuning may set, and the translation unit that reads them
 TUNABLE = ("VG_SWEEP_R32_MASK", "VG_SWEEP_R16_MASK", "VG_ROW_MIN_BLOCKS_R16", "VG_ROW_MIN_BLOCKS_R32",
            "VG_ROW_MIN_BLOCKS", "VG_SWEEP_ROW_BLOCK", "VG_SWEEP_COL_R16_MASK", "VG_COL_MIN_BLOCKS_R16",
-           "VG_COL_MIN_BLOCKS", "VG_KICK_MIN_BLOCKS")
+           "VG_COL_MIN_BLOCKS", "VG_KICK_MIN_BLOCKS", "VG_SWEEP_COL_R32_MASK", "VG_COL_MIN_BLOCKS_R32")
 TUNED_SOURCE = "vg_sweep.cu"
 
 

@@ -77,8 +77,24 @@ constexpr int SWEEP_MAX_CLASSES = 6;  // nv in {64, ..., 2048}
 #ifndef VG_SWEEP_COL_R16_MASK
 #define VG_SWEEP_COL_R16_MASK 0xE0
 #endif
+// radix 32 for the nx (>= 64) in this mask, ahead of the radix-16 one
+// (32 elements a thread; build-time knob, none by default), and the CTAs per
+// SM of those x-drift kernels
+#ifndef VG_SWEEP_COL_R32_MASK
+#define VG_SWEEP_COL_R32_MASK 0x0
+#endif
+#ifndef VG_COL_MIN_BLOCKS_R32
+#define VG_COL_MIN_BLOCKS_R32 2
+#endif
 __host__ __device__ constexpr int sweep_col_radix(int nx) {
-  return (nx >= 32 && nx <= 256 && ((VG_SWEEP_COL_R16_MASK >> ilog2(nx)) & 1)) ? 16 : col32_radix(nx);
+  return (nx >= 64 && nx <= 256 && ((VG_SWEEP_COL_R32_MASK >> ilog2(nx)) & 1))   ? 32
+         : (nx >= 32 && nx <= 256 && ((VG_SWEEP_COL_R16_MASK >> ilog2(nx)) & 1)) ? 16
+                                                                                 : col32_radix(nx);
+}
+__host__ __device__ constexpr int sweep_col_min_blocks(int nx) {
+  return sweep_col_radix(nx) == 32   ? VG_COL_MIN_BLOCKS_R32
+         : sweep_col_radix(nx) == 16 ? VG_COL_MIN_BLOCKS_R16
+                                     : VG_COL_MIN_BLOCKS;
 }
 __host__ __device__ constexpr int sweep_col_w(int nx) { return 2 * (SWEEP_BLOCK / (nx / sweep_col_radix(nx))); }
 // nv classes (bit log2 nv) on radix-32 passes (32 elements a thread; a row
@@ -240,7 +256,7 @@ __device__ __forceinline__ void sweep_col_item(const SweepRunDev& r, int tile, f
 }
 
 template <int NX>
-__global__ void __launch_bounds__(SWEEP_BLOCK, sweep_col_radix(NX) == 16 ? VG_COL_MIN_BLOCKS_R16 : VG_COL_MIN_BLOCKS) k_sweep_col(const SweepRunDev* __restrict__ runs,
+__global__ void __launch_bounds__(SWEEP_BLOCK, sweep_col_min_blocks(NX)) k_sweep_col(const SweepRunDev* __restrict__ runs,
                                                               const int2* __restrict__ items, float* g,
                                                               const SweepConsts* __restrict__ scp,
                                                               const cx<float>* __restrict__ tw, float2* dpart) {
@@ -310,7 +326,7 @@ __host__ __device__ constexpr size_t sweep_col_tma_smem() {
 }
 
 template <int NX>
-__global__ void __launch_bounds__(SWEEP_BLOCK, sweep_col_radix(NX) == 16 ? VG_COL_MIN_BLOCKS_R16 : VG_COL_MIN_BLOCKS) k_sweep_col_tma(
+__global__ void __launch_bounds__(SWEEP_BLOCK, sweep_col_min_blocks(NX)) k_sweep_col_tma(
     const SweepRunDev* __restrict__ runs, const int2* __restrict__ items, int n_items, float* g,
     const SweepConsts* __restrict__ scp, const cx<float>* __restrict__ tw, float2* dpart,
     const __grid_constant__ SweepTmaps maps, int* err, unsigned long long wait_ns, int no_loads) {

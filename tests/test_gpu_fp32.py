@@ -149,6 +149,20 @@ def test_fp32_steps_match_oracle():
     np.testing.assert_allclose(sf[:, 1], rf[:, 1], atol=2e-5 * np.abs(rf[:, 1]).max())
 
 
+@pytest.mark.parametrize("nx,nv", [(16, 4096), (8, 8192), (2, 8192)])
+def test_fp32_long_row_stored_modes(nx, nv):
+    """Rows of 4096 and 8192 with two stored x modes: the row pass keeps its
+    mode accumulators in global memory there (they do not fit in shared
+    memory beside the row-pair group); the stored modes, fields and state
+    against the FP64 oracle (nx = 2: one row pair in all)."""
+    p, f0, g, e, gst, st = _run_both(nx, nv, 4, nu=1e-4)
+    assert rel_pert(f_of(g, f0), st["f"], f0) <= TOL_STEP
+    np.testing.assert_allclose(gst["fields"]["n"].cpu().numpy(), st["fields"]["n"], rtol=1e-6)
+    sf, rf = gst["stored_f"].cpu().numpy(), st["stored_f"]
+    np.testing.assert_allclose(sf[:, 0], rf[:, 0], rtol=1e-5, atol=1e-6 * np.abs(rf[:, 0]).max())
+    np.testing.assert_allclose(sf[:, 1], rf[:, 1], atol=2e-5 * np.abs(rf[:, 1]).max())
+
+
 def test_fp32_entropy_series():
     """mean f log f of the FP32 storage step against the FP64 oracle, on a
     grid (vmax = 5) whose tails keep f > 0, so that the series is finite."""

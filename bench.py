@@ -529,7 +529,7 @@ def training_step_timing(cm, data, corr, torch, batch_runs=128, steps=20):
 
 def learned_path(args, w):
     """The learned coarse-velocity path (runs of the sweep distribution at
-    nx = 64): train the corrector on pairs from fine (nv = 1024) runs, judge
+    nx = 64): train the corrector on pairs from fine (nv = 1024) runs, check
     the corrected coarse (nv = 128) runs against the fine runs on held-out
     seeds against fine FP64 runs, and time the corrected coarse step against
     the fine FP32 sweep and the batched FP64 step of the same runs."""
@@ -557,17 +557,17 @@ def learned_path(args, w):
     zero.close()
     loss = cm.evaluate(corr, held)
     del held
-    # held-out rollouts: fine FP64 (the judge: the batched FP64 step, the
-    # reference's arithmetic), fine FP32 sweep, coarse, corrected coarse
+    # held-out rollouts: fine FP64 (the reference solution: the batched FP64
+    # step, the reference's arithmetic), fine FP32 sweep, coarse, corrected coarse
     from vlapy_gb300.batch import Batch64
     ev = cm.corrector_runs(n_eval, seed=6)
-    judge = Batch64([dict(r, nv=1024) for r in ev], vmax=w["vmax"], dt=w["dt"])
-    fj, ej = judge.initial_state()
-    eh64, sh64 = judge.history(nsteps)
+    ref64 = Batch64([dict(r, nv=1024) for r in ev], vmax=w["vmax"], dt=w["dt"])
+    fj, ej = ref64.initial_state()
+    eh64, sh64 = ref64.history(nsteps)
     chunk = 100
     t64 = time.perf_counter()
     for c0 in range(0, nsteps, chunk):
-        judge.run_steps(fj, ej, min(chunk, nsteps - c0), eh64, sh64, row0=c0)
+        ref64.run_steps(fj, ej, min(chunk, nsteps - c0), eh64, sh64, row0=c0)
     torch.cuda.synchronize()
     fp64_eval_s = time.perf_counter() - t64
     del fj, ej
@@ -583,14 +583,14 @@ def learned_path(args, w):
     cm.run_corrected(corrected, corr, nsteps, ek, sk)
     torch.cuda.synchronize()
     t = w["dt"] * np.arange(1, nsteps + 1)
-    dr_f = _damping_errors(t, judge, eh64, fine, hists[0][0])
-    dr_c = _damping_errors(t, judge, eh64, coarse, hists[1][0])
-    dr_k = _damping_errors(t, judge, eh64, corrected, ek)
+    dr_f = _damping_errors(t, ref64, eh64, fine, hists[0][0])
+    dr_c = _damping_errors(t, ref64, eh64, coarse, hists[1][0])
+    dr_k = _damping_errors(t, ref64, eh64, corrected, ek)
     # mean e^2 per run and step; the batch's series rows are in its stored order
-    e2_64 = sh64[:, torch.as_tensor(judge.slot, device=sh64.device), 3].cpu().numpy()
+    e2_64 = sh64[:, torch.as_tensor(ref64.slot, device=sh64.device), 3].cpu().numpy()
     e2 = [h[1][:, :, 3].cpu().numpy() for h in hists] + [sk[:, :, 3].cpu().numpy()]
     e2_err = [np.linalg.norm(e - e2_64, axis=0) / np.linalg.norm(e2_64, axis=0) for e in e2]
-    judge.close()
+    ref64.close()
     del eh64, sh64
 
     def stats(a):
@@ -663,7 +663,7 @@ def learned_path(args, w):
         "field_energy_history_rel_err_vs_fine_fp64": {"fine_fp32": stats(e2_err[0]), "coarse": stats(e2_err[1]),
                                                       "corrected": stats(e2_err[2])},
         "throughput_2048_runs": out,
-        "judge": "fine (nv = 1024) runs of the batched FP64 step (vg_batch: the reference's FP64 arithmetic), "
+        "reference_solution": "fine (nv = 1024) runs of the batched FP64 step (vg_batch: the reference's FP64 arithmetic), "
                  "%d runs x %d steps in %.1f s" % (n_eval, nsteps, fp64_eval_s),
     }
 

@@ -1,7 +1,7 @@
 """CPU oracle for the VlaPy time step -- TEST INFRASTRUCTURE ONLY.
 
 This module restates, in NumPy/SciPy, the arithmetic of the reference VlaPy
-time step (joglekara/VlaPy).  It is the checker for the CUDA path: only the
+time step (joglekara/VlaPy).  It is what the CUDA path is tested against: only the
 test-suite, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
 ``bench.py`` may import it.  The product package ``vlapy_gb300`` never calls
 into it and has no CPU fallback.
@@ -513,7 +513,7 @@ def envelope_fit(t, amp, t_min=None, t_max=None):
     gives the period of Re(E_k).  The reference estimator
     (vlapy/diagnostics/low_level_helpers.py:69-87) averages d log|E_k|/dt and
     is biased for undriven runs, so both the CPU oracle and the GPU runs are
-    judged with this one fit."""
+    measured with this one fit."""
     sel = np.ones_like(t, dtype=bool)
     if t_min is not None:
         sel &= t >= t_min

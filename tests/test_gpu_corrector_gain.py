@@ -1,7 +1,7 @@
 """What the trained corrector gains over the uncorrected coarse-velocity step.
 
 Trains the network with the library's own kernels on pairs from 256 fine
-runs (nv = 1024, seed 5) of the sweep distribution at nx = 64, then judges it
+runs (nv = 1024, seed 5) of the sweep distribution at nx = 64, then checks it
 on 64 held-out runs (seed 6) against the fine runs:
 - the one-step error on held-out pairs drops well below the uncorrected one;
 - the field-energy history of corrected coarse runs is closer to the fine

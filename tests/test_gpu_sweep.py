@@ -399,23 +399,23 @@ def test_sweep_full_horizon_against_fp64():
     sw.reset()
     eh, sh = sw.history(nsteps)
     sw.run_steps(nsteps, eh, sh)
-    judge = Batch64(runs)
-    f64, e64 = judge.initial_state()
-    eh64, sh64 = judge.history(nsteps)
+    ref64 = Batch64(runs)
+    f64, e64 = ref64.initial_state()
+    eh64, sh64 = ref64.history(nsteps)
     for c0 in range(0, nsteps, 250):
-        judge.run_steps(f64, e64, 250, eh64, sh64, row0=c0)
+        ref64.run_steps(f64, e64, 250, eh64, sh64, row0=c0)
     torch.cuda.synchronize()
     t = 0.1 * np.arange(1, nsteps + 1)
     rate_err, e2_err, f_err = [], [], []
     for i, r in enumerate(runs):
-        rf, _ = damping_fit(t, mode_amplitude(judge.e_of(eh64, i).cpu().numpy()), t_min=5.0, t_max=60.0)
+        rf, _ = damping_fit(t, mode_amplitude(ref64.e_of(eh64, i).cpu().numpy()), t_min=5.0, t_max=60.0)
         rg, _ = damping_fit(t, mode_amplitude(sw.e_of(eh, i).cpu().numpy()), t_min=5.0, t_max=60.0)
         assert np.isfinite(rf) and rf < 0.0, (i, r, rf)
         rate_err.append(abs(rg - rf) / abs(rf))
-        e2_ref = judge.series_of(sh64, i)[:, 3].cpu().numpy()
+        e2_ref = ref64.series_of(sh64, i)[:, 3].cpu().numpy()
         e2 = sh[:, i, 3].cpu().numpy()
         e2_err.append(np.linalg.norm(e2 - e2_ref) / np.linalg.norm(e2_ref))
-        f_ref = judge.f_of(f64, i).cpu().numpy()
+        f_ref = ref64.f_of(f64, i).cpu().numpy()
         f0 = vo.maxwellian(1, r["nv"], 6.4)[0]
         f_err.append(np.linalg.norm(sw.read_run(i)[0].cpu().numpy() - f_ref) / np.linalg.norm(f_ref - f0[None, :]))
     rate_err, e2_err, f_err = map(np.asarray, (rate_err, e2_err, f_err))
@@ -425,7 +425,7 @@ def test_sweep_full_horizon_against_fp64():
     assert rate_err.max() <= 0.01, (int(rate_err.argmax()), runs[int(rate_err.argmax())])
     assert e2_err.max() <= 0.01, (int(e2_err.argmax()), runs[int(e2_err.argmax())])
     assert f_err.max() <= 0.02, (int(f_err.argmax()), runs[int(f_err.argmax())])
-    judge.close()
+    ref64.close()
 
 
 def test_sweep_full_workload_full_horizon():
@@ -460,16 +460,16 @@ def test_sweep_full_workload_full_horizon():
             seen.add(key)
             picked.append(i)
     assert len(picked) >= 18
-    judge = Batch64([runs[i] for i in picked])
-    f64, e64 = judge.initial_state()
-    eh64, _ = judge.history(nsteps)
+    ref64 = Batch64([runs[i] for i in picked])
+    f64, e64 = ref64.initial_state()
+    eh64, _ = ref64.history(nsteps)
     for c0 in range(0, nsteps, 500):
-        judge.run_steps(f64, e64, 500, eh64, None, row0=c0)
+        ref64.run_steps(f64, e64, 500, eh64, None, row0=c0)
     torch.cuda.synchronize()
     t = 0.1 * np.arange(1, nsteps + 1)
     for j, i in enumerate(picked):
-        rf, _ = damping_fit(t, mode_amplitude(judge.e_of(eh64, j).cpu().numpy()), t_min=5.0, t_max=60.0)
+        rf, _ = damping_fit(t, mode_amplitude(ref64.e_of(eh64, j).cpu().numpy()), t_min=5.0, t_max=60.0)
         rg, _ = damping_fit(t, mode_amplitude(sw.e_of(eh, i).cpu().numpy()), t_min=5.0, t_max=60.0)
         assert np.isfinite(rf) and abs(rg - rf) <= 0.01 * abs(rf), (i, runs[i], rg, rf)
-    judge.close()
+    ref64.close()
     sw.close()

@@ -1,5 +1,5 @@
-"""The FP32 delta-f step on the two single-run workloads, judged by the FP64
-GPU step.
+"""The FP32 delta-f step on the two single-run workloads, checked against the
+FP64 GPU step.
 
 * Driven electron plasma wave: 64 x 1024, k = 0.3, vmax = 6.4, Maxwellian
   start, Dougherty collisions nu = 1e-3, dt = 0.1, 4000 steps, external field
@@ -9,7 +9,7 @@ GPU step.
   f = (M(v - 3) + M(v + 3)) / 2 (1 + 1e-3 sum_{m=1..16} cos(m k x + phi_m))
   with phi_m from default_rng(4), Dougherty nu = 1e-4, dt = 0.05.
 
-The judge is the FP64 GPU step, which follows the reference's NumPy step to
+The reference solution is the FP64 GPU step, which follows the reference's NumPy step to
 <= 1e-12 per step (tests/test_gpu_parity.py, including the reference's own
 steps of the driven workload's grid and driver in the fixture
 driven_sin2_dg_64x1024).  It stands in for the CPU oracle here because the
@@ -82,8 +82,8 @@ def _run(precision, f, f_bg, grids, nsteps, dt, nu, pulses, n_store):
 
 def test_driven_wave_fp32_against_fp64_4000_steps():
     """The driven-wave workload over its full 4000 steps (t = 0..400: the
-    sin^2 drive to t = 100, then the free wave under collisions).  The gate is
-    the benchmark spec's: field-energy history within 1e-3 of the FP64 step.  The
+    sin^2 drive to t = 100, then the free wave under collisions).  The gate:
+    field-energy history within 1e-3 of the FP64 step.  The
     e and f errors grow in the driven, nonlinear phase; a second FP64 run
     started from f perturbed by 1e-7 (relative, seeded noise: FP32's rounding
     level) shows how much of that growth is the dynamics' own sensitivity."""

@@ -1,7 +1,7 @@
 """The CPU oracle against golden vectors produced by the reference itself.
 
-These run without a GPU.  They pin the oracle: the oracle is trusted as the
-checker for the CUDA path only because it reproduces the reference's outputs
+These run without a GPU.  They pin the oracle: the CUDA path is tested
+against the oracle only because the oracle reproduces the reference's outputs
 on the fixtures in tests/golden (made by tests/golden/make_golden.py).
 """
 

@@ -96,6 +96,70 @@ def test_plan_create_rejects_bad_descriptor(lib_path):
     assert lib.vg_edfdv(None, None, None, 0.1, None) == _lib.VG_ERR_ARG
 
 
+def test_sweep_create_rejects_bad_runs(lib_path):
+    """The sweep's argument checks run before any CUDA call: no runs, a bad
+    descriptor, and runs outside the supported shape classes (the error names
+    the run)."""
+    from vlapy_gb300 import _lib
+    lib = _lib.load(lib_path)
+    h = ctypes.c_void_p()
+
+    def create(runs, n=None, collision=_lib.VG_COLL_DG, vmax=6.4):
+        arr = (_lib.VgSweepRun * max(1, len(runs)))(*[_lib.VgSweepRun(*r) for r in runs])
+        d = _lib.VgSweepDesc(len(runs) if n is None else n, collision, vmax, 0.1, arr)
+        return lib.vg_sweep_create(ctypes.byref(d), ctypes.byref(h))
+
+    ok = (32, 256, 0.3, 1e-3, 1e-3)
+    assert create([], n=0) == _lib.VG_ERR_ARG
+    assert create([ok], vmax=0.0) == _lib.VG_ERR_ARG
+    assert create([ok], collision=_lib.VG_COLL_NONE) == _lib.VG_ERR_ARG
+    assert lib.vg_sweep_create(None, ctypes.byref(h)) == _lib.VG_ERR_ARG
+    for bad in ((12, 256, 0.3, 1e-3, 1e-3),    # nx not a power of two
+                (512, 256, 0.3, 1e-3, 1e-3),   # nx above 256
+                (32, 96, 0.3, 1e-3, 1e-3),     # nv not a power of two
+                (32, 4096, 0.3, 1e-3, 1e-3),   # nv above 2048
+                (8, 256, 0.3, 1e-3, 1e-3),     # nv below the column tile width 4096 / nx
+                (32, 256, 0.0, 1e-3, 1e-3),    # k = 0
+                (32, 256, 0.3, 1e-3, -1e-3)):  # nu < 0
+        assert create([ok, bad]) == _lib.VG_ERR_UNSUPPORTED, bad
+        assert b"sweep run 1" in lib.vg_last_error()
+    assert not h.value
+
+
+def test_batch_create_rejects_bad_runs(lib_path):
+    """The FP64 batch's argument checks run before any CUDA call."""
+    from vlapy_gb300 import _lib
+    lib = _lib.load(lib_path)
+    h = ctypes.c_void_p()
+    grid = (ctypes.c_double * 64)()
+
+    def desc(nx=16, nv=32, precision=_lib.VG_F64, dt=0.1, nu=0.0, grids=True):
+        d = _lib.VgRunDesc()
+        d.nx, d.nv, d.precision, d.dt, d.nu = nx, nv, precision, dt, nu
+        d.collision, d.integrator = _lib.VG_COLL_NONE, _lib.VG_LEAPFROG
+        if grids:
+            for name in ("x", "v", "kx", "kv", "one_over_kx", "v_pow"):
+                setattr(d, name, grid)
+        return d
+
+    def create(*descs, n=None):
+        arr = (_lib.VgRunDesc * max(1, len(descs)))(*descs)
+        return lib.vg_batch_create(arr, len(descs) if n is None else n, ctypes.byref(h))
+
+    assert create(n=0) == _lib.VG_ERR_ARG
+    assert lib.vg_batch_create(None, 1, ctypes.byref(h)) == _lib.VG_ERR_ARG
+    for bad, status in ((desc(precision=_lib.VG_F32_DELTA_F), _lib.VG_ERR_UNSUPPORTED),
+                        (desc(nx=12), _lib.VG_ERR_UNSUPPORTED),
+                        (desc(nx=2048), _lib.VG_ERR_UNSUPPORTED),
+                        (desc(nv=16384), _lib.VG_ERR_UNSUPPORTED),
+                        (desc(grids=False), _lib.VG_ERR_ARG),
+                        (desc(dt=0.05), _lib.VG_ERR_ARG),
+                        (desc(nu=-1e-3), _lib.VG_ERR_ARG)):
+        assert create(desc(), bad) == status
+        assert b"batch run 1" in lib.vg_last_error()
+    assert not h.value
+
+
 def test_struct_layout_matches_header(lib_path):
     from vlapy_gb300 import _lib
     names = ["vg_run_desc", "vg_history", "vg_pulse", "vg_sweep_run", "vg_sweep_desc", "vg_prof_entry",

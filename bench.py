@@ -350,12 +350,14 @@ def run_sweep_gpu(args, w, rank, world, global_rank=0):
 def single_run_summary(args, name, precision, steps=10, warmup=3):
     """One of the single-run workloads (large: 4096 x 8192 two-stream; driven:
     64 x 1024 with the sin^2 driver) timed as the main bench times its
-    workload: CUDA events around a graph of `steps` steps, then one profiled
-    step, then e2e through the C-ABI call with the step's time and driver row
-    copied in from pinned host memory and its stored fields and series read
-    back, every step."""
+    workload: CUDA events around a graph of `steps` steps, then three profiled
+    steps (kernel times per launch: the call's leading kick, the row passes
+    with the next step's leading kick, and the call's last row pass without
+    it, apart), then e2e through the C-ABI call with the step's time and
+    driver row copied in from pinned host memory and its stored fields and
+    series read back, every step."""
     w = WORKLOADS[name]
-    sub = argparse.Namespace(steps=steps, warmup=warmup, prof_steps=1, precision=precision)
+    sub = argparse.Namespace(steps=steps, warmup=warmup, prof_steps=3, precision=precision)
     ms, prof, clk, e2e, plan = run_gpu(sub, w, 0, 1)
     cells = w["nx"] * w["nv"]
     e2e_sec, h2d, d2h = e2e
@@ -363,7 +365,8 @@ def single_run_summary(args, name, precision, steps=10, warmup=3):
            "unit": "cell-updates/s",
            "e2e": {"value": cells * steps / e2e_sec, "unit": "cell-updates/s", "h2d_bytes_per_step": h2d,
                    "d2h_bytes_per_step": d2h},
-           "kernels_ms_per_step": {k: d["total_ms"] for k, d in prof.items()}}
+           "kernels": {k: {"launches": d["launches"], "avg_ms": d["total_ms"] / d["launches"]}
+                       for k, d in prof.items()}}
     plan.close()
     if w["kind"] == "driven":
         out["dropin"] = dropin_summary(w, precision)

@@ -332,7 +332,11 @@ int vg_sweep_profile_read(vg_sweep* sweep, vg_prof_entry* out, int32_t max, int3
  * the step sequence is bracketed by CUDA events on the plan's stream and the
  * graph path is bypassed.  vg_profile_read synchronises the stream, then
  * fills up to max entries (kernel name, launches, total milliseconds,
- * algorithmic DRAM bytes per launch) and clears the record.  No reference
+ * algorithmic DRAM bytes per launch) and clears the record.  The FP32 row
+ * pass of a call's last leapfrog step, which ends without the next step's
+ * leading half kick, is recorded apart ("row_pass_last_f32", and
+ * "sweep_row_pass_last" for sweeps), so that "row_pass_f32" and
+ * "sweep_row_pass" time the pass of every other step.  No reference
  * counterpart (the reference only logs wall-clock per step,
  * vlapy/manager.py:144-146). */
 int vg_profile_enable(vg_plan* plan, int32_t enable);

@@ -163,6 +163,30 @@ def test_fp32_long_row_stored_modes(nx, nv):
     np.testing.assert_allclose(sf[:, 1], rf[:, 1], atol=2e-5 * np.abs(rf[:, 1]).max())
 
 
+def test_fp32_profile_records_the_last_row_pass_apart():
+    """The per-kernel record of a 3-step call of the FP32 plan: one leading
+    half kick, two row passes that end with the next step's leading half
+    kick, and the last step's row pass (without it) under its own name."""
+    from vlapy_gb300.plan import history_struct
+    nx, nv, n = 16, 256, 3
+    p, f, f0, _ = setup(nx, nv, nu=1e-3)
+    dev = torch.device("cuda")
+    z = lambda *s: torch.zeros(s, dtype=torch.float64, device=dev)  # noqa: E731
+    gst = {"stored_f": torch.zeros((n, 2, nv), dtype=torch.complex64, device=dev),
+           "fields": {kk: z(n, nx) for kk in vo.FIELD_KEYS},
+           "series": {kk: z(n) for kk in vo.SERIES_KEYS}}
+    g, e = g_of(f, f0), z(nx)
+    tb = torch.as_tensor(0.1 * np.arange(n), device=dev)
+    p.profile(True)
+    p.run_steps(g, e, history_struct(gst, nx, 2), tb, z(n, nx), 0, n, use_graph=False)
+    prof = p.profile_read()
+    p.profile(False)
+    launches = {k: v["launches"] for k, v in prof.items()}
+    assert launches["kick_f32"] == 1
+    assert launches["row_pass_f32"] == 2 and launches["row_pass_last_f32"] == 1
+    assert launches["x_drift_f32"] == n and launches["store_f32"] == n
+
+
 def test_fp32_entropy_series():
     """mean f log f of the FP32 storage step against the FP64 oracle, on a
     grid (vmax = 5) whose tails keep f > 0, so that the series is finite."""

@@ -473,3 +473,23 @@ def test_sweep_full_workload_full_horizon():
         assert np.isfinite(rf) and abs(rg - rf) <= 0.01 * abs(rf), (i, runs[i], rg, rf)
     ref64.close()
     sw.close()
+
+
+def test_profile_records_the_last_row_pass_apart():
+    """The per-kernel record of a 3-step call: one leading half kick, three
+    x-drifts, field solves and stores, two row passes that end with the next
+    step's leading half kick, and the last step's row pass (without it) under
+    its own name."""
+    from vlapy_gb300.sweep import Sweep
+    sw = Sweep(mixed_runs())
+    sw.reset()
+    eh, sh = sw.history(3)
+    sw.profile(True)
+    sw.run_steps(3, eh, sh)
+    prof = sw.profile_read()
+    sw.profile(False)
+    assert {k: v["launches"] for k, v in prof.items()} == {
+        "sweep_kick": 1, "sweep_x_drift": 3, "sweep_field": 3, "sweep_row_pass": 2, "sweep_store": 3,
+        "sweep_row_pass_last": 1}
+    assert all(v["total_ms"] > 0 for v in prof.values())
+    sw.close()

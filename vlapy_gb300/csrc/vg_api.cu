@@ -107,14 +107,17 @@ struct GraphCache {
   std::map<GraphKey, cudaGraphExec_t> execs;
 };
 
-// Kernel kinds of the step sequence, for vg_profile_*.
+// Kernel kinds of the step sequence, for vg_profile_*.  PK_ROW32: a leapfrog
+// step's row pass with the next step's leading half kick (and the kick-free
+// row pass of the composed integrators); PK_ROW32_LAST: the last leapfrog
+// step's of a call, which ends without it.
 enum ProfKind {
   PK_EDFDV = 0, PK_VDFDX, PK_DENSITY, PK_POISSON, PK_FP_MOMENTS, PK_FP_SOLVE, PK_STORAGE,
-  PK_X_DRIFT32, PK_FIELD32, PK_ROW32, PK_KICK32, PK_STORE32, PK_COUNT
+  PK_X_DRIFT32, PK_FIELD32, PK_ROW32, PK_KICK32, PK_STORE32, PK_ROW32_LAST, PK_COUNT
 };
 static const char* kProfNames[PK_COUNT] = {"edfdv", "vdfdx", "density", "poisson", "fp_moments", "fp_solve",
                                             "storage", "x_drift_f32", "field_f32", "row_pass_f32", "kick_f32",
-                                            "store_f32"};
+                                            "store_f32", "row_pass_last_f32"};
 
 // algorithmic DRAM bytes of one launch of each kind: the f traffic the
 // operation cannot avoid (read + write of f for in-place transforms, one
@@ -131,6 +134,7 @@ static double prof_bytes(const vg_plan* p, int kind) {
     case PK_STORAGE: return es * cells;
     case PK_X_DRIFT32:
     case PK_ROW32:
+    case PK_ROW32_LAST:
     case PK_KICK32: return 2.0 * 4.0 * cells;
     case PK_STORE32: return 8.0 * 8.0 * p->nx;
     default: return 3.0 * 8.0 * p->nx;
@@ -486,8 +490,9 @@ int step_sequence_f32(vg_plan* p, float* g, double* e, const vg_history* h, cons
       const int i = i0 + k;
       VG_CHECK(X(dt));
       VG_CHECK(F(i, {dt}));
-      const double trail = (k + 1 < nsteps) ? 0.5 * dt : 0.0;
-      VG_CHECK(cuda_status(prof_run(p, PK_ROW32, s, [&] {
+      const bool last = k + 1 == nsteps;
+      const double trail = last ? 0.0 : 0.5 * dt;
+      VG_CHECK(cuda_status(prof_run(p, last ? PK_ROW32_LAST : PK_ROW32, s, [&] {
                              return launch_row_f32(*p, g, e, 0.5 * dt, trail, 1, h != nullptr, nm, s);
                            }),
                            "row pass"));

@@ -865,9 +865,11 @@ void free_sweep(vg_sweep* s) {
   delete s;
 }
 
-enum SweepProfKind { SK_KICK = 0, SK_X_DRIFT, SK_FIELD, SK_ROW, SK_STORE, SK_COUNT };
+// SK_ROW: a step's row pass with the next step's leading half kick;
+// SK_ROW_LAST: the last step's of a call, which ends without it
+enum SweepProfKind { SK_KICK = 0, SK_X_DRIFT, SK_FIELD, SK_ROW, SK_STORE, SK_ROW_LAST, SK_COUNT };
 const char* const kSweepNames[SK_COUNT] = {"sweep_kick", "sweep_x_drift", "sweep_field", "sweep_row_pass",
-                                          "sweep_store"};
+                                          "sweep_store", "sweep_row_pass_last"};
 
 template <int NX>
 cudaError_t sweep_col_launch(vg_sweep* s, int c, cudaStream_t st) {
@@ -1021,7 +1023,8 @@ int sweep_sequence(vg_sweep* s, int nsteps, double* e_hist, double* s_hist, int 
                          "sweep field"));
     const int r = row0 + k;
     const bool store = (e_hist || s_hist) && r >= 0 && r < rows;
-    SW_CHECK(row(0.5 * dt, (k + 1 < nsteps) ? 0.5 * dt : 0.0, 1, store ? 1 : 0, SK_ROW));
+    const bool last = k + 1 == nsteps;
+    SW_CHECK(row(0.5 * dt, last ? 0.0 : 0.5 * dt, 1, store ? 1 : 0, last ? SK_ROW_LAST : SK_ROW));
     if (store) {
       double* er = e_hist ? e_hist + (size_t)r * s->x_points : nullptr;
       double* sr = s_hist ? s_hist + (size_t)r * s->n_runs * 7 : nullptr;
@@ -1452,7 +1455,7 @@ int vg_sweep_profile_read(vg_sweep* s, vg_prof_entry* out, int32_t max, int32_t*
   }
   const double cells = (double)s->cells;
   const double bytes[SK_COUNT] = {8.0 * cells, 8.0 * cells, 8.0 * 2.0 * s->x_points, 8.0 * cells,
-                                  8.0 * 9.0 * s->x_points};
+                                  8.0 * 9.0 * s->x_points, 8.0 * cells};
   int n = 0;
   SW_CHECK(prof_collect(&s->prof, SK_COUNT, kSweepNames, bytes, out, max, &n));
   *n_out = n;

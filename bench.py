@@ -314,22 +314,26 @@ def run_sweep_gpu(args, w, rank, world, global_rank=0):
         sw.run_steps(args.prof_steps, eh, sh, use_graph=False, stream=stream)
     prof = sw.profile_read()
     sw.profile(False)
-    # e2e: the K steps in one run_steps call through the C ABI, every step's e
-    # row and series taken to pinned host memory by a copy stream as soon as
-    # the step has stored them (the sweep records a CUDA event after each
-    # step), and the host waiting for each step's result in turn while the
-    # later steps run
+    # e2e: the K steps in one run_steps call through the C ABI (one replay of
+    # the graph that an untimed call with the same arguments captured), every
+    # step's e row and series taken to pinned host memory by a copy stream as
+    # soon as the step has stored them (the graph records a CUDA event after
+    # each step), and the host waiting for each step's result in turn while
+    # the later steps run
     events = [torch.cuda.Event() for _ in range(K)]
     sw.set_step_events(events)
     out_e = [torch.empty(sw.x_points, dtype=torch.float64).pin_memory()]
     out_s = [torch.empty((sw.n_runs, 7), dtype=torch.float64).pin_memory()]
     copy_stream = torch.cuda.Stream()
     ev_copy = torch.cuda.Event()
+    with torch.cuda.stream(stream):
+        sw.run_steps(K, eh, sh, use_graph=True, stream=stream)  # capture
+    torch.cuda.synchronize()
     eh.zero_()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     with torch.cuda.stream(stream):
-        sw.run_steps(K, eh, sh, use_graph=False, stream=stream)
+        sw.run_steps(K, eh, sh, use_graph=True, stream=stream)
     for k in range(K):
         copy_stream.wait_event(events[k])
         with torch.cuda.stream(copy_stream):

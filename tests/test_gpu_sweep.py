@@ -156,11 +156,14 @@ def test_sweep_classes_side_by_side_equal_serial():
         assert torch.equal(a.get_state()[0], b.get_state()[0])
 
 
-def test_sweep_step_events_stream_rows_out():
+@pytest.mark.parametrize("use_graph", [False, True])
+def test_sweep_step_events_stream_rows_out(use_graph):
     """Step events: one run_steps call records a caller event after each
     step's history row is stored, so a copy stream can take row k to the host
     while the later steps run.  Every row copied that way equals the final
-    history, and the events change nothing in the results."""
+    history, and the events change nothing in the results.  With a graph the
+    call is made twice (the capture's launch, then a replay): the events are
+    recorded by the graph itself, on every replay."""
     from vlapy_gb300.sweep import Sweep
     runs = mixed_runs()
     a, b = Sweep(runs), Sweep(runs)
@@ -175,19 +178,20 @@ def test_sweep_step_events_stream_rows_out():
     stream.wait_stream(torch.cuda.current_stream())
     host_e = torch.zeros((n, a.x_points), dtype=torch.float64).pin_memory()
     host_s = torch.zeros((n, a.n_runs, 7), dtype=torch.float64).pin_memory()
-    with torch.cuda.stream(stream):
-        a.run_steps(n, ea, sa, stream=stream)
-    for k in range(n):
-        copy_stream.wait_event(events[k])
-        with torch.cuda.stream(copy_stream):
-            host_e[k].copy_(ea[k], non_blocking=True)
-            host_s[k].copy_(sa[k], non_blocking=True)
+    for _ in range(2 if use_graph else 1):
+        with torch.cuda.stream(stream):
+            a.run_steps(n, ea, sa, use_graph=use_graph, stream=stream)
+        for k in range(n):
+            copy_stream.wait_event(events[k])
+            with torch.cuda.stream(copy_stream):
+                host_e[k].copy_(ea[k], non_blocking=True)
+                host_s[k].copy_(sa[k], non_blocking=True)
+        b.run_steps(n, eb, sb)
+        torch.cuda.synchronize()
+        assert torch.equal(host_e, ea.cpu()) and torch.equal(ea, eb)
+        torch.testing.assert_close(host_s, sa.cpu(), rtol=0, atol=0, equal_nan=True)
+        torch.testing.assert_close(sa, sb, rtol=0, atol=0, equal_nan=True)
     a.set_step_events([])
-    b.run_steps(n, eb, sb)
-    torch.cuda.synchronize()
-    assert torch.equal(host_e, ea.cpu()) and torch.equal(ea, eb)
-    torch.testing.assert_close(host_s, sa.cpu(), rtol=0, atol=0, equal_nan=True)
-    torch.testing.assert_close(sa, sb, rtol=0, atol=0, equal_nan=True)
     assert torch.equal(a.get_state()[0], b.get_state()[0])
 
 

@@ -1034,8 +1034,17 @@ int sweep_sequence(vg_sweep* s, int nsteps, double* e_hist, double* s_hist, int 
                            }),
                            "sweep store"));
     }
-    if (k < (int)s->step_events.size() && s->step_events[k])
-      SW_CHECK(cuda_status(cudaEventRecord(s->step_events[k], st), "sweep step event"));
+    if (k < (int)s->step_events.size() && s->step_events[k]) {
+      // under stream capture a plain record only orders the captured work;
+      // an external record puts the record itself into the graph, so that
+      // every replay records the caller's event
+      cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+      SW_CHECK(cuda_status(cudaStreamIsCapturing(st, &cap), "sweep step event"));
+      SW_CHECK(cuda_status(cudaEventRecordWithFlags(s->step_events[k], st,
+                                                    cap == cudaStreamCaptureStatusActive ? cudaEventRecordExternal
+                                                                                         : cudaEventRecordDefault),
+                           "sweep step event"));
+    }
   }
   return VG_OK;
 }

@@ -1331,6 +1331,11 @@ int vg_sweep_set_step_events(vg_sweep* s, void* const* events, int32_t n) {
   s->step_events.assign(n, nullptr);
   for (int k = 0; k < n; ++k) s->step_events[k] = (cudaEvent_t)events[k];
   ++s->events_gen;
+  // graphs captured before record the previous events (or none) and are
+  // never replayed again: free them (one still in flight is freed when it
+  // completes)
+  for (auto& kv : s->graphs) cudaGraphExecDestroy(kv.second);
+  s->graphs.clear();
   return VG_OK;
 }
 

@@ -8,8 +8,9 @@
  * pointers owned by the caller (PyTorch tensors in the Python host layer);
  * the plan owns only its constants and scratch.  Every call returns an int
  * status (VG_OK == 0); vg_last_error() gives the message of the last failure
- * on the calling thread.  Calls on one plan must be serialised on one stream;
- * different plans are independent.
+ * on the calling thread.  Calls on one object (plan, batch, sweep,
+ * corrector) must come from one host thread at a time and be serialised on
+ * one stream; different objects are independent.
  *
  * Layouts (C order, as in the reference): f[nx][nv] with v contiguous,
  * e[nx], driver[nx].  In VG_F64 mode f is float64 and the arithmetic follows
